@@ -1,0 +1,38 @@
+"""Copy the reference's own full-case fixtures into tests/golden/.
+
+Run once in a container where the reference checkout exists:
+
+    python tests/golden/make_golden.py /root/reference
+
+It copies, unchanged, the inputs (config.nml, geom01.nml, PLOT3D blade file)
+and the reference results (referenceResults/*.ref) of the reference's two
+integration cases, tests/katzNplotkin-AR04.case and tests/elevateTest.case.
+These are the golden vectors the oracle is pinned to; the GPU machine has no
+reference checkout, so the copies travel with the repository.
+"""
+import shutil
+import sys
+from pathlib import Path
+
+CASES = {
+    "katzNplotkin-AR04": ["config.nml", "geom01.nml"],
+    "elevateTest": ["config.nml", "geom01.nml", "elevate.xyz"],
+}
+
+
+def main(ref_root: str) -> None:
+    ref = Path(ref_root)
+    out_root = Path(__file__).resolve().parent
+    for case, inputs in CASES.items():
+        src = ref / "tests" / f"{case}.case"
+        dst = out_root / case
+        dst.mkdir(parents=True, exist_ok=True)
+        for f in inputs:
+            shutil.copyfile(src / f, dst / f)
+        for f in sorted((src / "referenceResults").glob("*.ref")):
+            shutil.copyfile(f, dst / f.name)
+        print(f"{case}: {sorted(p.name for p in dst.iterdir())}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,189 @@
+"""Case-file generation: the reference's ``config.nml`` / ``geomXX.nml`` formats.
+
+VOLCANOR reads a case from namelist files (``readConfig``,
+src/libCommon.f90:51-108, format version 0.5; ``rotor_readGeom``,
+src/classdef.f90:2541-2767, format version 0.15).  This module writes those
+files from Python keyword arguments, with every key present, so a case built
+here runs unchanged in the reference and in this package.
+
+It also defines the benchmark workloads as concrete case files:
+
+* :func:`wing_ar4` -- flat rectangular wing, chord 1 m, aspect ratio 4,
+  4 x 13 rings (cosine spanwise), alpha 5 deg, 10 m/s, dt = c/(4V), 200 steps.
+* :func:`rotor_2blade_hover` -- 2-blade hovering rotor, R = 1 m, root cut 0.2R,
+  chord 0.08 m, collective 8 deg, Omega = 100 rad/s, 1 x 24 rings per blade,
+  dt = 5 deg, 1440 steps, wake truncated after 6 revs (432 steps), viscous
+  core growth on.
+* :func:`rotor_4blade_forward` -- 4-blade rotor in forward flight (R = 2 m,
+  c = 0.12 m, -8 deg linear twist via a PLOT3D blade, collective 10 deg,
+  advance ratio 0.1, shaft tilt -4 deg, 1 x 32 rings per blade, dt = 5 deg).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Dict, Optional
+
+CONFIG_DEFAULTS: Dict[str, Dict[str, object]] = {
+    "VERSION": {"fileFormatVersion": "0.5"},
+    "PARAMS": {"nt": -10, "dt": 0.0, "nr": 1, "density": 1.0, "velSound": 330.0, "kinematicVisc": 0.000018},
+    "OPTIONS": {
+        "restartWriteNt": 0, "restartFromNt": 0, "ntSub": 0, "ntSubInit": 0,
+        "wakePlot": 0, "wakeTipPlot": 0, "rotorForcePlot": 1, "gridPlot": 0,
+        "wakeDissipation": 0, "wakeStrain": 0, "wakeBurst": 0, "wakeSuppress": 0,
+        "slowStart": 0, "slowStartNt": 0, "fdScheme": 3, "initWakeVelNt": 0, "probe": 0,
+    },
+}
+
+GEOM_DEFAULTS: Dict[str, Dict[str, object]] = {
+    "VERSION": {"fileFormatVersion": "0.15"},
+    "SURFACE": {"surfaceType": 0, "imagePlane": 3, "imageRotorNum": 1},
+    "PANELS": {"nb": 1, "propConvention": 0, "spanSpacing": 2, "chordSpacing": 1,
+               "geometryFile": "0", "nCamberFiles": 0, "nc": 4, "ns": 13, "nNwake": 160},
+    "CAMBERSECTIONS": {"camberSectionLimit": 1.0, "camberFile": "0"},
+    "ORIENT": {"hubCoords": (0.0, 0.0, 0.0), "cgCoords": (0.0, 0.0, 0.0),
+               "fromCoords": (0.0, 0.0, 0.0), "phiThetaPsi": (0.0, 0.0, 0.0)},
+    "GEOMPARAMS": {
+        "span": 4.0, "rootcut": 0.0, "chord": 1.0, "preconeAngle": 0.0, "Omega": 0.0,
+        "shaftAxis": (0.0, 0.0, 1.0), "theta0": 5.0, "thetaC": 0.0, "thetaS": 0.0, "thetaTwist": 0.0,
+        "ductSwitch": 0, "axisymmetrySwitch": 0, "pivotLE": 0.0, "flapHinge": 0.0,
+        "spanwiseLiftSwitch": 0, "symmetricTau": 1, "customTrajectorySwitch": 0,
+        "velBody": (-10.0, 0.0, 0.0), "omegaBody": (0.0, 0.0, 0.0), "forceCalcSwitch": 0, "nAirfoils": 0,
+    },
+    "WAKEPARAMS": {
+        "apparentViscCoeff": 1.0, "decayCoeff": 0.0, "wakeTruncateNt": 0, "prescWakeAfterTruncNt": 0,
+        "prescWakeGenNt": 0, "spanwiseCore": 0.04, "streamwiseCoreVec": 0.04, "rollupStartRadius": 0.75,
+        "rollupEndRadius": 1.0, "initWakeVel": 0.0, "psiStart": 0.0, "skewLimit": 0.5,
+    },
+    "DYNAMICS": {
+        "bladeDynamicsSwitch": 0, "flapInitial": 0.0, "dflapInitial": 0.0, "Iflap": 0.0, "cflap": 0.0,
+        "kflap": 0.0, "MflapConstant": 0.0, "pitchDynamicsSwitch": 0, "dpitch": 0.0,
+        "bodyDynamicsSwitch": 0, "bodyDynamicsIOVars": 0,
+    },
+    "WINDFRAME": {"dragUnitVec": (0.0, 0.0, 0.0), "sideUnitVec": (0.0, 0.0, 0.0), "liftUnitVec": (0.0, 0.0, 0.0)},
+    "PLOTS": {"inflowPlotSwitch": 0, "gammaPlotSwitch": 0, "skewPlotSwitch": 0},
+    "AIRFOILS": {"airfoilSectionLimit": 1.0, "alpha0": 0.0, "airfoilFile": "0"},
+}
+
+
+def _fmt(v: object) -> str:
+    if isinstance(v, (tuple, list)):
+        return ", ".join(_fmt(x) for x in v)
+    if isinstance(v, bool):
+        return "1" if v else "0"
+    if isinstance(v, int):
+        return str(v)
+    if isinstance(v, float):
+        return repr(v)
+    return str(v)
+
+
+def _render(defaults: Dict[str, Dict[str, object]], overrides: Dict[str, object]) -> str:
+    groups = {g: dict(kv) for g, kv in defaults.items()}
+    keymap = {k.lower(): (g, k) for g, kv in defaults.items() for k in kv}
+    for k, v in overrides.items():
+        if k.lower() not in keymap:
+            raise KeyError(f"unknown namelist key {k!r}")
+        g, kk = keymap[k.lower()]
+        groups[g][kk] = v
+    out = []
+    for g, kv in groups.items():
+        out.append(f"&{g}")
+        for k, v in kv.items():
+            out.append(f"{k} = {_fmt(v)}")
+        out.append("/")
+        out.append("")
+    return "\n".join(out)
+
+
+def config_text(**overrides: object) -> str:
+    """config.nml text (version 0.5) with every key present."""
+    return _render(CONFIG_DEFAULTS, overrides)
+
+
+def geom_text(**overrides: object) -> str:
+    """geomXX.nml text (version 0.15) with every key present."""
+    return _render(GEOM_DEFAULTS, overrides)
+
+
+@dataclass
+class Case:
+    """A case directory's contents: config.nml, geom01.nml and extra files."""
+
+    name: str
+    config: str
+    geom: str
+    files: Dict[str, str] = field(default_factory=dict)
+
+    def write(self, directory: str | Path) -> Path:
+        d = Path(directory)
+        d.mkdir(parents=True, exist_ok=True)
+        (d / "config.nml").write_text(self.config)
+        (d / "geom01.nml").write_text(self.geom)
+        for fname, text in self.files.items():
+            (d / fname).write_text(text)
+        return d
+
+
+def wing_ar4(nt: int = 200, fd_scheme: int = 1, n_nwake: Optional[int] = None) -> Case:
+    """Flat wing, c = 1 m, AR 4, 4 x 13 rings, alpha 5 deg, V = 10 m/s, dt = c/(4V)."""
+    cfg = config_text(nt=nt, dt=0.025, density=1.0, fdScheme=fd_scheme, wakeDissipation=0)
+    geo = geom_text(nb=1, nc=4, ns=13, nNwake=nt if n_nwake is None else n_nwake, span=4.0, rootcut=0.0,
+                    chord=1.0, Omega=0.0, theta0=5.0, velBody=(-10.0, 0.0, 0.0), spanSpacing=2,
+                    chordSpacing=1, spanwiseCore=0.03, streamwiseCoreVec=0.03, apparentViscCoeff=5.0,
+                    symmetricTau=1)
+    return Case("wing_ar4", cfg, geo)
+
+
+def rotor_2blade_hover(nt: int = 1440, n_nwake: int = 260, truncate_nt: int = 432, fd_scheme: int = 3) -> Case:
+    """2-blade hover rotor, R = 1 m, 1 x 24 rings/blade, dt = 5 deg, truncation at 6 revs."""
+    cfg = config_text(nt=nt, dt=0.0, density=1.2, kinematicVisc=1.5e-5, fdScheme=fd_scheme, wakeDissipation=1)
+    geo = geom_text(nb=2, nc=1, ns=24, nNwake=n_nwake, span=1.0, rootcut=0.2, chord=0.08, Omega=100.0,
+                    shaftAxis=(0.0, 0.0, 1.0), theta0=8.0, velBody=(0.0, 0.0, 0.0), spanSpacing=1,
+                    chordSpacing=1, spanwiseCore=0.05, streamwiseCoreVec=0.05, apparentViscCoeff=5.0,
+                    wakeTruncateNt=truncate_nt, symmetricTau=0, pivotLE=0.25)
+    return Case("rotor_2blade_hover", cfg, geo)
+
+
+def plot3d_twisted_blade(nc: int, ns: int, radius: float, chord: float, root_cut: float,
+                         twist_deg: float, pivot: float = 0.25) -> str:
+    """PLOT3D (nx = nc+1, ny = ns+1, nz = 1) flat blade with linear twist.
+
+    ``thetaTwist`` is read by the reference but never applied to the geometry
+    (src/classdef.f90:3129), so twist enters through ``geometryFile``
+    (``rotor_plot3dtoblade``, src/classdef.f90:3957-4020).  x runs from the
+    leading edge (-chord) to the trailing edge (0); the section is twisted
+    about the quarter chord by twist_deg * (r - r0)/(R - r0).
+    """
+    nx, ny = nc + 1, ns + 1
+    r0 = root_cut * radius
+    xs, ys, zs = [], [], []
+    for j in range(ny):
+        r = r0 + (radius - r0) * j / ns
+        th = math.radians(twist_deg) * (r - r0) / (radius - r0)
+        for i in range(nx):
+            xc = -chord + chord * i / nc  # LE -> TE
+            xp = -chord + pivot * chord
+            dx = xc - xp
+            # nose-up twist rotates the LE up (+z) for positive theta
+            xs.append(xp + dx * math.cos(th))
+            ys.append(r)
+            zs.append(-dx * math.sin(th))
+    def block(vals):
+        return "\n".join(" ".join(f"{v:.15e}" for v in vals[k:k + 6]) for k in range(0, len(vals), 6))
+    return f"{nx} {ny} 1\n{block(xs)}\n{block(ys)}\n{block(zs)}\n"
+
+
+def rotor_4blade_forward(nt: int = 2880, n_nwake: int = 72, omega: float = 100.0, mu: float = 0.1,
+                         fd_scheme: int = 3, truncate_nt: int = 0) -> Case:
+    """4-blade rotor, R = 2 m, c = 0.12 m, -8 deg twist, theta0 = 10 deg, mu = 0.1, shaft tilt -4 deg."""
+    radius, chord, nc, ns = 2.0, 0.12, 1, 32
+    cfg = config_text(nt=nt, dt=0.0, density=1.2, kinematicVisc=1.5e-5, fdScheme=fd_scheme, wakeDissipation=1)
+    geo = geom_text(nb=4, nc=nc, ns=ns, nNwake=n_nwake, span=radius, rootcut=0.2, chord=chord, Omega=omega,
+                    shaftAxis=(0.0, 0.0, 1.0), theta0=10.0, velBody=(-mu * omega * radius, 0.0, 0.0),
+                    phiThetaPsi=(0.0, -4.0, 0.0), geometryFile="blade.xyz", spanSpacing=1, chordSpacing=1,
+                    spanwiseCore=0.05, streamwiseCoreVec=0.05, apparentViscCoeff=5.0,
+                    wakeTruncateNt=truncate_nt, symmetricTau=0, pivotLE=0.25)
+    return Case("rotor_4blade_forward", cfg, geo,
+                files={"blade.xyz": plot3d_twisted_blade(nc, ns, radius, chord, 0.2, -8.0)})
