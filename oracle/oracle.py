@@ -48,6 +48,7 @@ def lib():
         L.or_sim_free.argtypes = [vp]
         L.or_set_threads.argtypes = [i32]
         L.or_sim_start.argtypes = [vp]
+        L.or_set_sum_chunk.argtypes = [vp, i32]
         L.or_sim_step.argtypes = [vp, i32]
         L.or_rot_pitch.argtypes = [vp, i32, ctypes.c_double]
         L.or_gettheta.argtypes = [vp, ctypes.c_double, i32]
@@ -63,7 +64,7 @@ def lib():
         L.or_get.argtypes = [vp, cp, i32, dp, i64]
         L.or_get.restype = i64
         L.or_sim_vind_points.argtypes = [vp, dp, i64, dp, i32]
-        L.or_vind_rings.argtypes = [dp, dp, dp, i64, dp, i64, dp]
+        L.or_vind_rings.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
         L.or_vf_vind.argtypes = [dp, dp, ctypes.c_double, dp, dp]
         L.or_inv2.argtypes = [dp, i32, dp]
         L.or_matvec.argtypes = [dp, dp, i32, dp]
@@ -113,6 +114,10 @@ class Sim:
         if h:
             lib().or_sim_free(h)
             self._h = None
+
+    def set_sum_chunk(self, c: int):
+        """Chunked Biot-Savart summation order (0 = the reference's sequential order)."""
+        lib().or_set_sum_chunk(self._h, int(c))
 
     # main program
     def start(self):
@@ -169,14 +174,14 @@ class Sim:
         return V
 
 
-def vind_rings(corners, rvc, gam, P) -> np.ndarray:
-    """V[m] = sum_n vr_vind(ring n, P[m]) * gam[n] (reference accumulation order)."""
+def vind_rings(corners, rvc, gam, P, chunk: int = 0) -> np.ndarray:
+    """V[m] = sum_n vr_vind(ring n, P[m]) * gam[n] (reference order; chunked when chunk > 0)."""
     corners = _f64(corners).reshape(-1, 4, 3)
     rvc = _f64(rvc).reshape(-1, 4)
     gam = _f64(gam).reshape(-1)
     P = _f64(P).reshape(-1, 3)
     V = np.zeros_like(P)
-    _check(lib().or_vind_rings(_ptr(corners), _ptr(rvc), _ptr(gam), corners.shape[0], _ptr(P), P.shape[0], _ptr(V)))
+    _check(lib().or_vind_rings(_ptr(corners), _ptr(rvc), _ptr(gam), corners.shape[0], _ptr(P), P.shape[0], _ptr(V), int(chunk)))
     return V
 
 

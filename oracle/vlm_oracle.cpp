@@ -345,6 +345,27 @@ inline V3 vr_vind(const VR& r, V3 P) {
   return v;
 }
 
+// Deterministic chunked summation.  chunk <= 0 reproduces the reference's
+// sequential accumulation exactly; chunk = C splits a blade's source sequence
+// into consecutive blocks of C records (skipped records still count), sums
+// each block from zero and adds the block sums in order.  The GPU FP64 path
+// uses the same order, so both produce identical bits for the same C.
+struct ChunkSum {
+  int C;
+  int cnt = 0;
+  V3 tot, part;
+  explicit ChunkSum(int c) : C(c) {}
+  void add(V3 x) {
+    if (C <= 0) { tot = tot + x; return; }
+    part = part + x;
+    tick();
+  }
+  void tick() {
+    if (C > 0 && ++cnt == C) { tot = tot + part; part = V3(); cnt = 0; }
+  }
+  V3 result() const { return (C > 0 && cnt > 0) ? tot + part : tot; }
+};
+
 struct FW {            // classdef.f90:198-220
   VF vf;
   double gam = 0;
@@ -547,6 +568,7 @@ struct Sim {
   double t = 0;
   std::vector<std::vector<double>> ctHist;  // rows of [iter, CL/CT, CD, CLu, CDi, CD0, CDu, CFx, CFy, CFz]
   int nthreads = 0;
+  int sumChunk = 0;  // see ChunkSum
   bool started = false;
 
   // ---- blade kinematics -------------------------------------------------
@@ -896,10 +918,10 @@ struct Sim {
     V3 acc;
     for (int ib = 0; ib < R.nb; ++ib) {
       const Blade& b = R.blade[ib];
-      V3 s;
+      ChunkSum s(sumChunk);
       for (int j = 0; j < b.ns; ++j)
-        for (int i = 0; i < b.nc; ++i) s = s + vr_vind(b.w(i, j).vr, P) * b.w(i, j).vr.gam;
-      acc = acc + s;
+        for (int i = 0; i < b.nc; ++i) s.add(vr_vind(b.w(i, j).vr, P) * b.w(i, j).vr.gam);
+      acc = acc + s.result();
     }
     return acc;
   }
@@ -930,24 +952,27 @@ struct Sim {
       const Blade& b = R.blade[ib];
       const std::vector<VR>& wn = pred ? b.waNP : b.waN;
       const std::vector<FW>& wf = pred ? b.waFP : b.waF;
-      V3 s;
+      ChunkSum s(sumChunk);
       for (int j = 0; j < b.ns; ++j)
         for (int i = R.rowNear - 1; i < NW; ++i) {
           const VR& r = wn[i + NW * j];
-          if (std::fabs(r.gam) > EPS) s = s + vr_vind(r, P) * r.gam;
+          if (std::fabs(r.gam) > EPS) s.add(vr_vind(r, P) * r.gam);
+          else s.tick();
         }
       if (R.rowFar <= NF) {
+        // s - v*gam == s + v*(-gam) bit for bit
         for (int j = 0; j < b.ns; ++j) {
           const VR& r = wn[(NW - 1) + NW * j];
-          s = s - vf_vind(r.vf[1], P) * r.gam;
+          s.add(vf_vind(r.vf[1], P) * (-r.gam));
         }
         for (int i = R.rowFar - 1; i < NF; ++i) {
           const FW& f = wf[i];
-          if (std::fabs(f.gam) > EPS) s = s + vf_vind(f.vf, P) * f.gam;
+          if (std::fabs(f.gam) > EPS) s.add(vf_vind(f.vf, P) * f.gam);
+          else s.tick();
         }
         // prescribed far wake: circulation stays 0 (not generated), so skipped
       }
-      acc = acc + s;
+      acc = acc + s.result();
     }
     return acc;
   }
@@ -1988,6 +2013,8 @@ void or_set_threads(int n) {
 #endif
 }
 
+void or_set_sum_chunk(void* h, int c) { static_cast<Sim*>(h)->sumChunk = c; }
+
 int or_sim_start(void* h) { return guarded([&]() { static_cast<Sim*>(h)->start(); }); }
 int or_sim_step(void* h, int nsteps) {
   return guarded([&]() {
@@ -2155,10 +2182,11 @@ int or_sim_vind_points(void* h, const double* P, long M, double* V, int pred) {
 }
 
 // Isolated ring kernel: V[m] = sum_n vr_vind(ring n, P[m]) * gam[n], rings in
-// order n = 0..N-1 (blade_vind_bywing's accumulation).  corners: N x 4 x 3,
+// order n = 0..N-1 (blade_vind_bywing's accumulation), in chunked order when
+// chunk > 0 (see ChunkSum).  corners: N x 4 x 3,
 // rvc: N x 4 (core radius of filament k = corner k -> corner k+1), P and V: M x 3.
 int or_vind_rings(const double* corners, const double* rvc, const double* gam, long N,
-                  const double* P, long M, double* V) {
+                  const double* P, long M, double* V, int chunk) {
   return guarded([&]() {
     std::vector<VR> rings(N);
     for (long n = 0; n < N; ++n) {
@@ -2174,9 +2202,10 @@ int or_vind_rings(const double* corners, const double* rvc, const double* gam, l
 #pragma omp parallel for schedule(static)
     for (long m = 0; m < M; ++m) {
       V3 p = mk(P[3 * m], P[3 * m + 1], P[3 * m + 2]);
-      V3 s;
-      for (long n = 0; n < N; ++n) s = s + vr_vind(rings[n], p) * rings[n].gam;
-      V[3 * m] = s.x; V[3 * m + 1] = s.y; V[3 * m + 2] = s.z;
+      ChunkSum s(chunk);
+      for (long n = 0; n < N; ++n) s.add(vr_vind(rings[n], p) * rings[n].gam);
+      V3 r = V3() + s.result();
+      V[3 * m] = r.x; V[3 * m + 1] = r.y; V[3 * m + 2] = r.z;
     }
   });
 }

@@ -1,0 +1,124 @@
+"""GPU free-wake solver against the oracle (same summation blocks -> same bits)
+and against the reference's full-case golden CT histories."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from volcanor_gb300 import cases as C
+from volcanor_gb300 import lib
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(cfg, geo, nsteps, base="", chunk=256, precision=lib.PREC_FP64):
+    g = lib.Case(cfg, geo, base, precision=precision, sum_chunk=chunk)
+    g.start()
+    g.step(nsteps)
+    r = O.Sim(cfg, geo, base)
+    r.set_sum_chunk(chunk)
+    r.start()
+    r.step(nsteps)
+    return g, r
+
+
+def small_wing(fd, nt=14, nnw=6, trunc=10, **kw):
+    cfg = C.config_text(nt=nt, dt=0.025, density=1.0, fdScheme=fd, **kw)
+    geo = C.geom_text(nb=1, nc=3, ns=5, nNwake=nnw, span=2.0, chord=0.5, theta0=6.0, velBody=(-10.0, 0.0, 0.0),
+                      wakeTruncateNt=trunc, spanwiseCore=0.04, streamwiseCoreVec=0.04)
+    return cfg, geo
+
+
+def assert_same_state(g, r, nb=1):
+    np.testing.assert_array_equal(g.ct_hist(), r.ct_hist())
+    np.testing.assert_array_equal(g.get("gamVec"), r.get("gamVec"))
+    for b in range(1, nb + 1):
+        gw = g.get("waN", b).reshape(-1, 4, 3)
+        rw = r.get("waN", b).reshape(-1, 4, 2, 3)[:, :, 0]
+        np.testing.assert_array_equal(gw, rw)
+        np.testing.assert_array_equal(g.get("waN_gam", b), r.get("waN_gam", b))
+        np.testing.assert_array_equal(g.get("waN_rvc", b), r.get("waN_rvc", b))
+        np.testing.assert_array_equal(g.get("waF", b), r.get("waF", b))
+        np.testing.assert_array_equal(g.get("waF_gam", b), r.get("waF_gam", b))
+
+
+@pytest.mark.parametrize("fd", [0, 1, 2, 3, 4, 5])
+def test_fd_schemes_bitwise(fd):
+    cfg, geo = small_wing(fd)
+    g, r = run_both(cfg, geo, 14, chunk=16)
+    assert_same_state(g, r)
+
+
+def test_dissipation_strain_initwake_bitwise():
+    cfg, geo = small_wing(3, wakeDissipation=1, wakeStrain=1, initWakeVelNt=5)
+    geo = geo.replace("initWakeVel = 0.0", "initWakeVel = 1.5")
+    g, r = run_both(cfg, geo, 14, chunk=16)
+    assert_same_state(g, r)
+
+
+def test_reference_sequential_order_bitwise():
+    """sum_chunk = 0: the reference's own summation order."""
+    cfg, geo = small_wing(3)
+    g, r = run_both(cfg, geo, 12, chunk=0)
+    assert_same_state(g, r)
+
+
+def test_rotor_two_blades_truncation_bitwise():
+    c = C.rotor_2blade_hover(nt=40, n_nwake=12, truncate_nt=20)
+    g, r = run_both(c.config, c.geom, 40, chunk=64)
+    assert_same_state(g, r, nb=2)
+    assert g.geti("rowFar") == 1 and g.geti("rowNear") == 1
+
+
+def test_elevate_axisymmetric_plot3d_bitwise(golden_dir):
+    """tests/elevateTest.case (5 blades, axisymmetry, PLOT3D, dissipation, truncation), 90 steps."""
+    d = golden_dir / "elevateTest"
+    cfg, geo = (d / "config.nml").read_text(), (d / "geom01.nml").read_text()
+    g, r = run_both(cfg, geo, 90, base=d, chunk=256)
+    assert_same_state(g, r, nb=5)
+
+
+def test_katz_plotkin_full_case_vs_reference_golden(golden_dir):
+    """All 161 CT rows of tests/katzNplotkin-AR04.case to the reference's printed 7 digits."""
+    d = golden_dir / "katzNplotkin-AR04"
+    g = lib.Case.from_case_dir(d, precision=lib.PREC_FP64, sum_chunk=256)
+    g.start()
+    g.step(160)
+    ct = g.ct_hist()
+    ref = np.loadtxt(d / "r01ForceNonDim.csv.ref", skiprows=1)
+    rel = np.abs(ct[:, 1] - ref[:, 1]) / np.abs(ref[:, 1])
+    assert rel.max() <= 5.1e-7, rel.max()
+
+
+def test_elevate_full_case_vs_reference_golden(golden_dir):
+    d = golden_dir / "elevateTest"
+    g = lib.Case.from_case_dir(d, precision=lib.PREC_FP64, sum_chunk=256)
+    g.start()
+    g.step(150)
+    ct = g.ct_hist()
+    ref = np.loadtxt(d / "r01ForceNonDim.csv.ref", skiprows=1)
+    rel = np.abs(ct[:, 1] - ref[:, 1]) / np.abs(ref[:, 1])
+    assert rel.max() <= 5.1e-7, rel.max()
+
+
+@pytest.mark.parametrize("prec", [lib.PREC_FP32, lib.PREC_FP32_NEAR64])
+def test_fp32_solver_ct_error(prec):
+    c = C.rotor_2blade_hover(nt=60, n_nwake=20, truncate_nt=40)
+    g64 = lib.Case(c.config, c.geom, precision=lib.PREC_FP64)
+    g64.start()
+    a = g64.step(60)[:, 1]
+    g32 = lib.Case(c.config, c.geom, precision=prec)
+    g32.start()
+    b = g32.step(60)[:, 1]
+    assert np.max(np.abs(b - a) / np.abs(a)) < 1e-4
+
+
+def test_errors_and_state_checks():
+    cfg, geo = small_wing(3)
+    g = lib.Case(cfg, geo)
+    with pytest.raises(lib.VlmError):
+        g.step(1)  # before start
+    g.start()
+    with pytest.raises(lib.VlmError):
+        g.step(100)  # past nt
+    with pytest.raises(lib.VlmError):
+        lib.Case(cfg.replace("fdScheme = 3", "fdScheme = 9"), geo)

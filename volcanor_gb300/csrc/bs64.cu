@@ -1,0 +1,146 @@
+// FP64 Biot-Savart partial sums in the reference's arithmetic, the chunk
+// combiner, and the chunk-table builder.
+//
+// Compiled with -fmad=false: every multiply and add rounds separately, as in
+// the oracle (built with -ffp-contract=off), so a chunked FP64 evaluation
+// equals the oracle's evaluation with the same chunk size bit for bit.
+#include <algorithm>
+#include <atomic>
+
+#include "vlm_bs.h"
+#include "vlm_math.h"
+
+namespace vlm {
+
+namespace {
+
+constexpr int kThreads64 = 128;  // targets per block
+constexpr int kTile64 = 32;      // records staged per shared-memory tile
+
+// One block = kThreads64 targets x one chunk.  Each thread sums its target's
+// contributions over the chunk sequentially from zero (blade_vind_bywing /
+// blade_vind_bywake accumulation, src/classdef.f90:1342-1513).
+__global__ void __launch_bounds__(kThreads64) k_partial64(const double* __restrict__ rec,
+                                                         const Chunk* __restrict__ chunks,
+                                                         const double* __restrict__ P, int M,
+                                                         double* __restrict__ part) {
+  __shared__ double tile[kTile64 * kRec64];
+  const Chunk ch = chunks[blockIdx.y];
+  const int m = blockIdx.x * kThreads64 + threadIdx.x;
+  const bool active = m < M;
+  d3 p = zero3();
+  if (active) p = mk3(P[3 * (size_t)m], P[3 * (size_t)m + 1], P[3 * (size_t)m + 2]);
+  d3 acc = zero3();
+  for (int t0 = 0; t0 < ch.rec_count; t0 += kTile64) {
+    const int nt = min(kTile64, ch.rec_count - t0);
+    __syncthreads();
+    const double* src = rec + (size_t)(ch.rec_begin + t0) * kRec64;
+    for (int k = threadIdx.x; k < nt * kRec64; k += kThreads64) tile[k] = src[k];
+    __syncthreads();
+    if (!active) continue;
+    for (int r = 0; r < nt; ++r) {
+      const double* R = tile + r * kRec64;
+      const int flags = (int)R[17];
+      const double g = R[16];
+      if ((flags & REC_SKIP) && !(fabs(g) > kEps)) continue;
+      d3 v;
+      if (flags & REC_FIL) {
+        v = fil_vind64(p, mk3(R[0], R[1], R[2]), mk3(R[3], R[4], R[5]), R[12]);
+      } else {
+        d3 c[4] = {mk3(R[0], R[1], R[2]), mk3(R[3], R[4], R[5]), mk3(R[6], R[7], R[8]), mk3(R[9], R[10], R[11])};
+        v = vr_vind64(p, c, R + 12);
+      }
+      acc = acc + v * g;
+    }
+  }
+  if (active) {
+    double* o = part + ((size_t)blockIdx.y * M + m) * 3;
+    o[0] = acc.x;
+    o[1] = acc.y;
+    o[2] = acc.z;
+  }
+}
+
+__global__ void k_combine(const double* __restrict__ part, int M, const Group* __restrict__ groups, int ngroups,
+                          int mode, double* __restrict__ out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  d3 wing = zero3(), wake = zero3();
+  for (int g = 0; g < ngroups; ++g) {
+    const Group G = groups[g];
+    d3 gs = zero3();
+    for (int q = G.chunk_begin; q < G.chunk_begin + G.chunk_count; ++q) {
+      const double* pp = part + ((size_t)q * M + m) * 3;
+      gs = gs + mk3(pp[0], pp[1], pp[2]);
+    }
+    if (G.kind == 0) wing = wing + gs;
+    else wake = wake + gs;
+  }
+  d3 v;
+  if (mode == 0) v = zero3() + (wing + wake);
+  else if (mode == 1) v = wake;
+  else v = wing + wake;
+  out[3 * (size_t)m] = v.x;
+  out[3 * (size_t)m + 1] = v.y;
+  out[3 * (size_t)m + 2] = v.z;
+}
+
+__global__ void k_rings_to_rec64(const double* __restrict__ corners, const double* __restrict__ rvc,
+                                 const double* __restrict__ gam, int64_t N, double* __restrict__ rec) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double* R = rec + n * kRec64;
+  for (int k = 0; k < 12; ++k) R[k] = corners[n * 12 + k];
+  for (int k = 0; k < 4; ++k) R[12 + k] = rvc[n * 4 + k];
+  R[16] = gam[n];
+  R[17] = 0.0;
+}
+
+}  // namespace
+
+static std::atomic<long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(); }
+
+int build_chunks(Group* groups, int ngroups, int chunk_size, Chunk* chunks, int cap) {
+  int nq = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    Group& G = groups[g];
+    G.chunk_begin = nq;
+    G.chunk_count = 0;
+    if (G.rec_count <= 0) continue;
+    const int C = chunk_size > 0 ? chunk_size : G.rec_count;
+    for (int r = 0; r < G.rec_count; r += C) {
+      if (nq >= cap) return -1;
+      chunks[nq].rec_begin = G.rec_begin + r;
+      chunks[nq].rec_count = std::min(C, G.rec_count - r);
+      ++nq;
+      ++G.chunk_count;
+    }
+  }
+  return nq;
+}
+
+void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,
+                      cudaStream_t s) {
+  if (M <= 0 || nchunks <= 0) return;
+  dim3 grid((M + kThreads64 - 1) / kThreads64, nchunks);
+  count_launch();
+  k_partial64<<<grid, kThreads64, 0, s>>>(rec, chunks, P, M, part);
+}
+
+void launch_combine(const double* part, int M, const Group* groups, int ngroups, int mode, double* out,
+                    cudaStream_t s) {
+  if (M <= 0) return;
+  count_launch();
+  k_combine<<<(M + 127) / 128, 128, 0, s>>>(part, M, groups, ngroups, mode, out);
+}
+
+void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,
+                           cudaStream_t s) {
+  if (N <= 0) return;
+  count_launch();
+  k_rings_to_rec64<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(corners, rvc, gam, N, rec);
+}
+
+}  // namespace vlm

@@ -1,0 +1,97 @@
+// Source records, chunk tables and launchers of the Biot-Savart N-body kernels.
+//
+// A Biot-Savart evaluation sums, for every target point, the unit-strength
+// Vatistas velocity of a sequence of vortex sources times their circulation.
+// The sequence is split into GROUPS -- the reference's per-blade sums
+// (rotor_vind_bywing / rotor_vind_bywake, src/classdef.f90:4424-4479) -- and
+// every group into CHUNKS of consecutive records.  One kernel computes a
+// partial sum per (target, chunk); a second adds the chunk partials of each
+// group in order and the group sums in order, reproducing the reference's
+// accumulation exactly when a chunk spans a whole group.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vlm {
+
+// Number of kernels this library has launched (all threads, all cases).
+void count_launch();
+long launch_count();
+
+// FP64 source record, 18 doubles:
+//   [0..11] ring corners c0..c3 (xyz); a single filament uses [0..5] = fc1, fc2
+//   [12..15] core radius of filament k (c_k -> c_{k+1}); a filament uses [12]
+//   [16] circulation (a horseshoe closing filament stores -gam)
+//   [17] flags: REC_FIL (single filament) | REC_SKIP (skip if |gam| <= eps)
+constexpr int kRec64 = 18;
+constexpr int REC_FIL = 1;
+constexpr int REC_SKIP = 2;
+
+// FP32 source record, 48 floats (192 B, 16-byte aligned for bulk copies):
+//   [0..11]  corners c0..c3
+//   [12..23] edge vectors e_k = c_{k+1} - c_k
+//   [24..27] |e_k|^2
+//   [28..31] (rvc_k |e_k|)^4
+//   [32..35] near-field threshold on |r1 x r2|^2: (near_factor rvc_k |e_k|)^2, -1 if off
+//   [36..39] w_k = gam / (4 pi) for active edges, 0 for inactive / skipped
+//   [40..43] near-field slack along the filament: near_factor rvc_k |e_k|
+//   [44]     squared radius about corner 0 outside which no filament of the
+//            record can be near (-1 when the near-field path is off)
+//   [45..47] unused
+// A pair is near when the target lies within near_factor core radii of the
+// filament SEGMENT: |r1 x r2|^2 < [32+k] and -[40+k] < e.r1 < |e|^2 + [40+k].
+constexpr int kRec32 = 48;
+
+// One near-field pair found by the FP32 kernel: target m, chunk q (partial
+// sum to correct), global record index, filament k.
+struct NearPair {
+  int32_t m, q, rec, k;
+};
+
+struct Group {
+  int32_t rec_begin;    // first record (index into the record array)
+  int32_t rec_count;    // number of records
+  int32_t chunk_begin;  // first chunk of this group in the chunk table
+  int32_t chunk_count;
+  int32_t kind;         // 0 = wing sum, 1 = wake sum
+  int32_t blade;        // blade whose wing or wake the group sums
+  int32_t pad[2];
+};
+
+struct Chunk {
+  int32_t rec_begin;
+  int32_t rec_count;
+};
+
+// Builds the chunk table for `groups` (in place: fills chunk_begin/count).
+// Returns the number of chunks.
+int build_chunks(Group* groups, int ngroups, int chunk_size, Chunk* chunks, int cap);
+
+// FP64 reference-arithmetic partial sums: part[(q * M + m) * 3 + k].
+void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,
+                      cudaStream_t s);
+// FP32 pairs with FP64 accumulation.  When near is non-null, pairs inside the
+// records' near-field thresholds are left out of the FP32 sums, listed in
+// near (capacity near_cap, count in ctl[1]) and then evaluated in FP64 from
+// rec64 and added to their partial sums by a second kernel.  ctl[0] receives
+// a nonzero code if a bounded wait on the tile pipeline expired or the near
+// list overflowed.  ctl must be zeroed before the call.
+void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
+                      int M, double* part, int* ctl, NearPair* near, int near_cap, cudaStream_t s);
+// Converts FP64 records to FP32 records (near_factor <= 0 disables near-field).
+void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s);
+
+// Combines partials: total = sum over wing groups + sum over wake groups,
+// each group the in-order sum of its chunk partials, each from zero.
+//   mode 0: out[m] = 0 + (wing + wake)      (wake-node velocity, libCommon.f90:114-211)
+//   mode 1: out[m] = wake                   (rotor_vind_bywake at a collocation point)
+//   mode 2: out[m] = wing + wake            (point query)
+void launch_combine(const double* part, int M, const Group* groups, int ngroups, int mode, double* out,
+                    cudaStream_t s);
+
+// Isolated rings (vlm_biot_savart_rings): AoS corners (N x 4 x 3), rvc (N x 4), gam (N) -> FP64 records.
+void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,
+                           cudaStream_t s);
+
+}  // namespace vlm

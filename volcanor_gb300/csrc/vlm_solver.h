@@ -1,0 +1,137 @@
+// Device state of one rotor case and the launchers of the time-step kernels.
+//
+// Storage (all FP64, all blades, device memory owned by the case):
+//   wing panel p of blade b        -> index b*npan + (i + nc*j)      (src/classdef.f90 wiP(i,j))
+//   near-wake ring (i,j) of blade b -> index b*NW*ns + (i + NW*j)     (waN(i,j))
+//   far-wake filament i of blade b  -> index b*NF + i                (waF(i))
+//   node velocity (i,j), j <= ns    -> index b*NW*(ns+1) + (i + NW*j) (velNwake(:,i,j))
+// A near-wake ring stores its 4 corners (12 doubles): corner k is both
+// vf(k)%fc(:,1) and vf(k-1)%fc(:,2) of the reference ring, which the
+// reference always assigns, shifts and rotates together.
+//
+// Per-step wing kinematics are computed on the host (the prescribed motion
+// does not depend on the solution) and uploaded as one FRAME per timestep:
+//   PAN: per blade, per panel: corners[12] CP[3] nCap[3] tauC[3] tauS[3] velKin[3]  (27)
+//   SEC: per blade, per section: secTauC[3] secNormal[3] secCP[3] PC1(1,is)[3]      (12)
+//   AX:  per blade: xAxisAziFlap[3] yAxisAziFlap[3] zAxisAziFlap[3]                 (9)
+//   ROT: zAxisBody[3] hub[3] shaftAxis[3] omegaSlow, then for blades 2..nb the
+//        3x3 wake-copy rotation (row major)                                        (10 + 9(nb-1))
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vlm_bs.h"
+
+namespace vlm {
+
+constexpr int kPan = 27;
+constexpr int kSec = 12;
+
+struct FrameLayout {
+  int pan, sec, ax, rot, size;
+};
+
+inline FrameLayout frame_layout(int nb, int nc, int ns) {
+  FrameLayout f;
+  f.pan = 0;
+  f.sec = f.pan + nb * nc * ns * kPan;
+  f.ax = f.sec + nb * ns * kSec;
+  f.rot = f.ax + nb * 9;
+  f.size = f.rot + 10 + 9 * (nb > 1 ? nb - 1 : 0);
+  return f;
+}
+
+struct Dims {
+  int nb, nc, ns, npan, n, NW, NF, nbC;
+  int axisym;
+  int spanwiseLift;
+  int rollupStart, rollupEnd;  // 1-based, as the reference
+  int suppressFwake;
+  double omega, theta0, density, dt, nonDimDenom, dissipAdd, decay;
+  FrameLayout fl;
+};
+
+struct DevState {
+  // wing (static)
+  double *wRvc, *panArea, *panMeanChord, *panMeanSpan, *secArea;
+  // frames [(nt+1) * fl.size]
+  double* frames;
+  // wing dynamic
+  double *wGam, *gamPrev, *gamVec, *gamVecPrev, *RHS, *velCP, *velCPTotal;
+  double *AIC, *AICinv, *LU;
+  int* piv;
+  // near wake
+  double *nC, *nCP, *nGam, *nRvc, *nAge, *nTmp;
+  // far wake
+  double *fC, *fCP, *fGam, *fRvc, *fRvc0, *fL0, *fLc, *fAge, *fTmp;
+  // node velocities: 0 vel, 1 vel1, 2 vel2, 3 vel3, 4 velPredicted, 5 velStep, 6 scratch
+  double* vN[7];
+  double* vF[7];
+  // loads outputs (per blade, per section, xyz)
+  double *secResVel, *secLiftDir, *secDragDir, *secLift, *secForceInertial, *secLiftUnsteady, *secLiftInPlane,
+      *secLiftOutPlane, *secCL, *secCD, *secCLu;
+  double *bladeForce;  // [nb][4][3]: forceInertial, lift, drag(0), liftUnsteady
+  double* rotorLift;   // [3] previous-step lift (liftPrev)
+  double* ctHist;      // [(nt+1) * 10]
+  // N-body scratch
+  double *rec64, *targets, *part, *outv;
+  float* rec32;
+  NearPair* near;
+  int nearCap;
+  int* err;  // [0] LU/inverse check, [2] FP32 pipeline or near-list error, [3] near-pair count
+};
+
+// ---- wake bookkeeping (src/classdef.f90:4297-4605, 1515-1702, 4786-4830) ----
+void launch_shed(const Dims& d, const DevState& s, const double* frame, int rowNear, bool leadingEdge, cudaStream_t st);
+void launch_age(const Dims& d, const DevState& s, int rowNear, int rowFar, cudaStream_t st);
+void launch_dissipate(const Dims& d, const DevState& s, int rowNear, int rowFar, cudaStream_t st);
+void launch_copy_predicted(const Dims& d, const DevState& s, int rowNear, int rowFar, cudaStream_t st);
+// shift (pred: predicted wake with the reference's row-1 loop) + continuity + axisymmetric copies
+void launch_convect(const Dims& d, const DevState& s, const double* frame, int rowNear, int rowFar, bool pred,
+                    cudaStream_t st);
+void launch_strain(const Dims& d, const DevState& s, int rowFar, cudaStream_t st);
+void launch_rollup(const Dims& d, const DevState& s, int rowFar, cudaStream_t st);
+// velocity-history algebra over full arrays (blades < nbC)
+enum VelOp {
+  VOP_COPY_0_TO_1,     // v1 = v
+  VOP_COPY_0_TO_2,     // v2 = v
+  VOP_COPY_0_TO_3,     // v3 = v
+  VOP_AB2,             // st = 0.5(3v - v1); v1 = st; v = st
+  VOP_AM2_PRED,        // st = v; v = 0.5(3v - v1)
+  VOP_AM2_CORR,        // v = (vp + st) 0.5
+  VOP_STEP_TO_1,       // v1 = st
+  VOP_AM3_PRED,        // st = v; v = (23v - 16v2 + 5v1)/12
+  VOP_AM3_CORR,        // v = (5vp + 8st - v2)/12
+  VOP_AM3_SHIFT,       // v1 = v2; v2 = st
+  VOP_AM4_PRED,        // st = v; v = (55v - 59v3 + 37v2 - 9v1)/24
+  VOP_AM4_CORR,        // v = (9vp + 19st - 5v3 + v2)/24
+  VOP_AM4_SHIFT,       // v1 = v2; v2 = v3; v3 = st
+};
+void launch_velop(const Dims& d, const DevState& s, VelOp op, cudaStream_t st);
+// PC2 averaging (src/libCommon.f90:213-258)
+void launch_order2(const Dims& d, const DevState& s, int rowNear, int rowFar, cudaStream_t st);
+
+// ---- Biot-Savart evaluations ---------------------------------------------
+// targets: wake nodes of blades < nbC (count returned by node_target_count)
+int node_target_count(const Dims& d, int rowNear, int rowFar);
+void launch_node_targets(const Dims& d, const DevState& s, int rowNear, int rowFar, bool pred, double* P,
+                         cudaStream_t st);
+void launch_cp_targets(const Dims& d, const double* frame, double* P, cudaStream_t st);
+// record gather for the given groups (kind 0 wing, kind 1 wake)
+void launch_gather(const Dims& d, const DevState& s, const double* frame, const Group* groups, int ngroups,
+                   int nrec, int rowNear, int rowFar, bool pred, cudaStream_t st);
+// node velocities from outv (0 + v), plus the initial wake velocity terms
+void launch_scatter_nodes(const Dims& d, const DevState& s, const double* frame, int rowNear, int rowFar, bool pred,
+                          double initWakeVel, cudaStream_t st);
+
+// ---- circulation and loads -----------------------------------------------
+void launch_aic(const Dims& d, const DevState& s, const double* frame, cudaStream_t st);
+void launch_lu_inverse(const Dims& d, const DevState& s, cudaStream_t st);
+void launch_is_inverse(const Dims& d, const DevState& s, cudaStream_t st);
+// velCP = velKin (+ wake velocity in outv if withWake); RHS; gamVec = AICinv RHS; map to wing gam
+void launch_solve(const Dims& d, const DevState& s, const double* frame, bool withWake, cudaStream_t st);
+// velCPTotal, sectional resultant velocity, lift direction, forces, CT row
+void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st);
+
+}  // namespace vlm

@@ -1,0 +1,224 @@
+"""ctypes binding of libvlm_gb300.so (the C ABI in include/vlm.h).
+
+The Python classes mirror the reference's object API for the hot path: a
+:class:`Case` is one rotor/wing case read from ``config.nml`` +
+``geom01.nml`` (the reference's ``rotor`` object after ``readGeom`` and
+``init``), advanced with :meth:`Case.step` (one iteration of
+src/main.f90:400-1452 per step).  There is no CPU fallback: if the CUDA
+library is missing or no GPU is usable, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+PREC_FP64 = 0
+PREC_FP32 = 1
+PREC_FP32_NEAR64 = 2
+
+VLM_OK = 0
+_STATUS = {1: "invalid argument", 2: "CUDA error", 3: "I/O error", 4: "unsupported case feature",
+           5: "singular AIC", 6: "non-finite result", 7: "call out of order"}
+
+
+class VlmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("sum_chunk", ctypes.c_int), ("near_factor", ctypes.c_double),
+                ("device", ctypes.c_int), ("use_graph", ctypes.c_int)]
+
+
+# exported symbols and their signatures (include/vlm.h)
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64 = ctypes.c_int64
+_vp = ctypes.c_void_p
+SIGNATURES = {
+    "vlm_version": (ctypes.c_char_p, []),
+    "vlm_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "vlm_default_options": (None, [ctypes.POINTER(Options)]),
+    "vlm_kernel_launch_count": (_i64, []),
+    "vlm_device_info": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_int)]),
+    "vlm_biot_savart_rings": (ctypes.c_int, [_dp, _dp, _dp, _i64, _dp, _i64, _dp, ctypes.c_int]),
+    "vlm_biot_savart_rings_device": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_int, _vp]),
+    "vlm_biot_savart_rings_scratch_bytes": (_i64, [_i64, _i64, ctypes.c_int]),
+    "vlm_biot_savart_rings_sum_chunk": (_i64, [_i64, _i64, ctypes.c_int]),
+    "vlm_case_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(Options),
+                                       ctypes.POINTER(_vp)]),
+    "vlm_case_create_from_dir": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
+    "vlm_case_destroy": (ctypes.c_int, [_vp]),
+    "vlm_case_start": (ctypes.c_int, [_vp]),
+    "vlm_case_step": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "vlm_case_get_int": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_i64)]),
+    "vlm_case_get": (_i64, [_vp, ctypes.c_char_p, ctypes.c_int, _dp, _i64]),
+    "vlm_case_vind_points": (ctypes.c_int, [_vp, _dp, _i64, _dp]),
+    "vlm_case_last_step_ms": (ctypes.c_int, [_vp, _dp]),
+    "vlm_case_profile_eval": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libvlm_gb300.so (building it in-tree if it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        if build_if_missing:
+            _build.build()
+        if not _build.LIB.exists():
+            raise RuntimeError(f"{_build.LIB} not built; run __graft_entry__.build()")
+        L = ctypes.CDLL(str(_build.LIB))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _err(code: int):
+    if code != VLM_OK:
+        buf = ctypes.create_string_buffer(1024)
+        load().vlm_last_error(buf, 1024)
+        raise VlmError(code, buf.value.decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _c64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def options(precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
+            device: int = 0, use_graph: bool = True) -> Options:
+    o = Options()
+    load().vlm_default_options(ctypes.byref(o))
+    o.precision = precision
+    if sum_chunk is not None:
+        o.sum_chunk = sum_chunk
+    if near_factor is not None:
+        o.near_factor = near_factor
+    o.device = device
+    o.use_graph = int(use_graph)
+    return o
+
+
+def launch_count() -> int:
+    """Kernels this library has launched so far."""
+    return int(load().vlm_kernel_launch_count())
+
+
+def device_info(device: int = 0):
+    sm, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _err(load().vlm_device_info(device, ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)))
+    return sm.value, ma.value, mi.value
+
+
+def biot_savart_rings(corners, rvc, gam, P, precision: int = PREC_FP64) -> np.ndarray:
+    """Ring-sum Biot-Savart through the host-buffer C entry point."""
+    corners = _c64(corners).reshape(-1, 4, 3)
+    rvc = _c64(rvc).reshape(-1, 4)
+    gam = _c64(gam).reshape(-1)
+    P = _c64(P).reshape(-1, 3)
+    V = np.zeros_like(P)
+    _err(load().vlm_biot_savart_rings(_ptr(corners), _ptr(rvc), _ptr(gam), corners.shape[0], _ptr(P), P.shape[0],
+                                      _ptr(V), precision))
+    return V
+
+
+def rings_sum_chunk(N: int, M: int, precision: int = PREC_FP64) -> int:
+    """Summation block size of the ring kernel for (N, M): see include/vlm.h."""
+    return int(load().vlm_biot_savart_rings_sum_chunk(N, M, precision))
+
+
+def biot_savart_rings_device(corners_ptr: int, rvc_ptr: int, gam_ptr: int, N: int, P_ptr: int, M: int, V_ptr: int,
+                             precision: int = PREC_FP64, stream: int = 0) -> None:
+    """Device-buffer entry point: raw CUDA pointers (e.g. torch tensor data_ptr())."""
+    _err(load().vlm_biot_savart_rings_device(corners_ptr, rvc_ptr, gam_ptr, N, P_ptr, M, V_ptr, precision,
+                                             stream or None))
+
+
+class Case:
+    """One rotor case on the GPU: the reference's rotor object + time loop."""
+
+    def __init__(self, config_text: str, geom_text: str, base_dir: str | os.PathLike = "",
+                 precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None):
+        L = load()
+        self._h = _vp()
+        self.opt = options(precision, sum_chunk, near_factor)
+        _err(L.vlm_case_create(config_text.encode(), geom_text.encode(), str(base_dir).encode(),
+                               ctypes.byref(self.opt), ctypes.byref(self._h)))
+
+    @classmethod
+    def from_case_dir(cls, case_dir: str | os.PathLike, **kw) -> "Case":
+        d = Path(case_dir)
+        return cls((d / "config.nml").read_text(), (d / "geom01.nml").read_text(), d, **kw)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().vlm_case_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def start(self):
+        _err(load().vlm_case_start(self._h))
+
+    def step(self, n: int = 1, with_ct: bool = True) -> Optional[np.ndarray]:
+        rows = np.zeros((n, 10)) if with_ct else None
+        _err(load().vlm_case_step(self._h, int(n), _ptr(rows) if with_ct else None))
+        return rows
+
+    def geti(self, name: str) -> int:
+        v = _i64()
+        _err(load().vlm_case_get_int(self._h, name.encode(), ctypes.byref(v)))
+        return int(v.value)
+
+    def get(self, name: str, blade: int = 1) -> np.ndarray:
+        L = load()
+        n = L.vlm_case_get(self._h, name.encode(), blade, None, 0)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(max(n, 1))
+        L.vlm_case_get(self._h, name.encode(), blade, _ptr(out), n)
+        return out[:n]
+
+    def ct_hist(self) -> np.ndarray:
+        return self.get("ct_hist").reshape(-1, 10)
+
+    def vind_points(self, P) -> np.ndarray:
+        P = _c64(P).reshape(-1, 3)
+        V = np.zeros_like(P)
+        _err(load().vlm_case_vind_points(self._h, _ptr(P), P.shape[0], _ptr(V)))
+        return V
+
+    def profile_eval(self, reps: int = 10):
+        """(ms per launch, ring-target pairs, filament-target pairs) of the hot kernel."""
+        ms, rp, fp = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _err(load().vlm_case_profile_eval(self._h, reps, ctypes.byref(ms), ctypes.byref(rp), ctypes.byref(fp)))
+        return ms.value, rp.value, fp.value
+
+    def last_step_ms(self) -> float:
+        ms = ctypes.c_double()
+        _err(load().vlm_case_last_step_ms(self._h, ctypes.byref(ms)))
+        return ms.value
