@@ -87,6 +87,24 @@ int64_t vlm_biot_savart_rings_scratch_bytes(int64_t N, int64_t M, int precision)
  * block sums then added in order (N = one block = the reference's order). */
 int64_t vlm_biot_savart_rings_sum_chunk(int64_t N, int64_t M, int precision);
 
+/* Allocation-free form of the device-buffer ring kernel.  It has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory when they call it (a host solver that reserves its device
+ * memory once at start-up, a process under a hard device-memory cap, or a
+ * caller that must not trigger the device-wide synchronisation an allocation
+ * may cause): its scratch is one fixed 8 MiB array compiled into the library,
+ * held on every device that loads the library until the process exits.
+ * Limits: N <= 16384 rings, M <= 65536 points, at most 65536 near-field
+ * pairs (VLM_PREC_FP32_NEAR64); larger sizes return VLM_ERR_INVALID with a
+ * message.  The rings are summed in one block, i.e. in the reference's order.
+ * The first call on a device looks up the scratch array's device address,
+ * so make that first call before any CUDA stream capture.  All calls on a
+ * device share the scratch and the call returns after its stream has
+ * finished; calls that overlap on the GPU (other host threads or streams at
+ * the same time) race on the scratch and must be serialised by the caller. */
+int vlm_biot_savart_rings_noalloc(const double* corners, const double* rvc, const double* gam, int64_t N,
+                                  const double* P, int64_t M, double* V, int precision, void* stream);
+
 /* ---- one rotor case ----------------------------------------------------------
  * Replaces readConfig + rotor%readGeom + rotor%init (src/main.f90:12-40,
  * src/libCommon.f90:51-108, src/classdef.f90:2541-3891).  config_text and

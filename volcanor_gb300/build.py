@@ -21,6 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_EXACT = ["bs64.cu", "solver.cu"]
 CU_FAST = ["bs32.cu"]
+CU_PLAIN = ["noalloc.cu"]
 CXX = ["wing.cpp", "case.cpp"]
 
 
@@ -32,7 +33,7 @@ def _cuda_home() -> Path:
 
 
 def sources():
-    return [SRC / f for f in CU_EXACT + CU_FAST + CXX] + list(SRC.glob("*.h")) + [PKG.parent / "include" / "vlm.h"]
+    return [SRC / f for f in CU_EXACT + CU_FAST + CU_PLAIN + CXX] + list(SRC.glob("*.h")) + [PKG.parent / "include" / "vlm.h"]
 
 
 def up_to_date() -> bool:
@@ -59,6 +60,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         o = BUILD / (f + ".o")
         jobs.append([nvcc, *common, "-ftz=true", "-prec-div=false", "-prec-sqrt=false", "-c", str(SRC / f), "-o",
                      str(o)])
+        objs.append(o)
+    for f in CU_PLAIN:
+        o = BUILD / (f + ".o")
+        jobs.append([nvcc, *common, "-c", str(SRC / f), "-o", str(o)])
         objs.append(o)
     for f in CXX:
         o = BUILD / (f + ".o")

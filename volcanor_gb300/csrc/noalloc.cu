@@ -1,0 +1,146 @@
+// vlm_biot_savart_rings_noalloc: the ring kernel without any device
+// allocation, for callers that cannot allocate device memory.
+//
+// Some hosts of this path cannot call cudaMalloc at the moment they need a
+// Biot-Savart sum: a solver that reserves all of its device memory once at
+// start-up and must not grow afterwards, code running under a hard device
+// memory cap, or a caller that cannot afford the implicit device-wide
+// synchronisation an allocation or free may trigger.  This entry point takes
+// all of its scratch from one fixed array compiled into the library, so it
+// never allocates; the price is a fixed maximum problem size.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/vlm.h"
+#include "vlm_bs.h"
+
+namespace vlm {
+
+extern thread_local std::string g_err;
+
+namespace {
+
+// Limits of the fixed scratch (see include/vlm.h).
+constexpr int64_t kMaxRings = 16384;
+constexpr int64_t kMaxPoints = 65536;
+constexpr int64_t kMaxNear = 65536;
+
+constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t kOffRec64 = 0;
+constexpr size_t kOffRec32 = kOffRec64 + align256(kMaxRings * kRec64 * sizeof(double));
+constexpr size_t kOffPart = kOffRec32 + align256(kMaxRings * kRec32 * sizeof(float));
+constexpr size_t kOffNear = kOffPart + align256(kMaxPoints * 3 * sizeof(double));
+constexpr size_t kOffTables = kOffNear + align256(kMaxNear * sizeof(NearPair));
+constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words
+
+// One fixed scratch area per device that loads the library, held until exit.
+// In host code this name is only a stand-in for the device object: kernels
+// get its device address from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_mu;
+unsigned char* g_base[64] = {nullptr};
+
+// Resets the per-call tables in the scratch: one chunk spanning all rings
+// (the reference's summation order), one wing-kind group, zeroed control
+// words (error flag and near-pair count).
+__global__ void k_noalloc_tables(unsigned char* base, int N) {
+  if (threadIdx.x != 0) return;
+  Chunk* ch = reinterpret_cast<Chunk*>(base + kOffTables);
+  Group* g = reinterpret_cast<Group*>(base + kOffTables + 64);
+  int* ctl = reinterpret_cast<int*>(base + kOffTables + 128);
+  ch->rec_begin = 0;
+  ch->rec_count = N;
+  g->rec_begin = 0;
+  g->rec_count = N;
+  g->chunk_begin = 0;
+  g->chunk_count = N > 0 ? 1 : 0;
+  g->kind = 0;
+  g->blade = 0;
+  for (int k = 0; k < 4; ++k) ctl[k] = 0;
+}
+
+__global__ void k_zero(double* v, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) v[i] = 0.0;
+}
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+}  // namespace
+
+}  // namespace vlm
+
+using namespace vlm;
+
+extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double* rvc, const double* gam, int64_t N,
+                                             const double* P, int64_t M, double* V, int precision, void* stream) {
+  if (precision < VLM_PREC_FP64 || precision > VLM_PREC_FP32_NEAR64) return fail(VLM_ERR_INVALID, "precision must be 0, 1 or 2");
+  if (N < 0 || M < 0) return fail(VLM_ERR_INVALID, "N and M must not be negative");
+  if (N > kMaxRings)
+    return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc: N = " + std::to_string(N) + " rings exceeds the fixed scratch limit of " +
+                                     std::to_string(kMaxRings));
+  if (M > kMaxPoints)
+    return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc: M = " + std::to_string(M) + " points exceeds the fixed scratch limit of " +
+                                     std::to_string(kMaxPoints));
+  if (M == 0) return VLM_OK;
+  if ((N > 0 && (!corners || !rvc || !gam)) || !P || !V) return fail(VLM_ERR_INVALID, "null device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(VLM_ERR_CUDA, "device ordinal out of range");
+  unsigned char* base = nullptr;
+  {
+    // set-up, once per device, with that device current: the device address
+    // of the scratch array (the host-side symbol is not a device address)
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_base[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) return fail(VLM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_base[dev] = static_cast<unsigned char*>(p);
+    }
+    base = g_base[dev];
+  }
+  double* rec64 = reinterpret_cast<double*>(base + kOffRec64);
+  float* rec32 = reinterpret_cast<float*>(base + kOffRec32);
+  double* part = reinterpret_cast<double*>(base + kOffPart);
+  NearPair* near = reinterpret_cast<NearPair*>(base + kOffNear);
+  Chunk* chunks = reinterpret_cast<Chunk*>(base + kOffTables);
+  Group* group = reinterpret_cast<Group*>(base + kOffTables + 64);
+  int* ctl = reinterpret_cast<int*>(base + kOffTables + 128);
+
+  count_launch();
+  k_noalloc_tables<<<1, 32, 0, st>>>(base, (int)N);
+  if (N > 0) {
+    launch_rings_to_rec64(corners, rvc, gam, N, rec64, st);
+    if (precision == VLM_PREC_FP64) {
+      launch_partial64(rec64, chunks, 1, P, (int)M, part, st);
+    } else {
+      const bool nearOn = precision == VLM_PREC_FP32_NEAR64;
+      launch_pack32(rec64, (int)N, nearOn ? 4.0 : 0.0, rec32, st);
+      launch_partial32(rec32, rec64, chunks, 1, P, (int)M, part, ctl, nearOn ? near : nullptr, (int)kMaxNear, st);
+    }
+    launch_combine(part, (int)M, group, 1, 2, V, st);
+  } else {
+    count_launch();
+    k_zero<<<(unsigned)((3 * M + 255) / 256), 256, 0, st>>>(V, 3 * M);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  // the scratch is shared by every call on this device: finish this one
+  // before returning, and read its error flag
+  int flags[2] = {0, 0};
+  e = cudaMemcpyAsync(flags, ctl, sizeof(flags), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+  if (flags[0] == 3) return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc: more than 65536 near-field pairs");
+  if (flags[0]) return fail(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
+  return VLM_OK;
+}

@@ -53,6 +53,7 @@ SIGNATURES = {
     "vlm_biot_savart_rings_device": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_int, _vp]),
     "vlm_biot_savart_rings_scratch_bytes": (_i64, [_i64, _i64, ctypes.c_int]),
     "vlm_biot_savart_rings_sum_chunk": (_i64, [_i64, _i64, ctypes.c_int]),
+    "vlm_biot_savart_rings_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_int, _vp]),
     "vlm_case_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(Options),
                                        ctypes.POINTER(_vp)]),
     "vlm_case_create_from_dir": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
@@ -152,6 +153,17 @@ def biot_savart_rings_device(corners_ptr: int, rvc_ptr: int, gam_ptr: int, N: in
     """Device-buffer entry point: raw CUDA pointers (e.g. torch tensor data_ptr())."""
     _err(load().vlm_biot_savart_rings_device(corners_ptr, rvc_ptr, gam_ptr, N, P_ptr, M, V_ptr, precision,
                                              stream or None))
+
+
+def biot_savart_rings_noalloc(corners_ptr: int, rvc_ptr: int, gam_ptr: int, N: int, P_ptr: int, M: int, V_ptr: int,
+                              precision: int = PREC_FP64, stream: int = 0) -> None:
+    """Allocation-free device-buffer ring kernel (fixed scratch; N <= 16384, M <= 65536).
+
+    For callers that cannot allocate device memory at call time; see
+    include/vlm.h for the limits and the shared-scratch rules.
+    """
+    _err(load().vlm_biot_savart_rings_noalloc(corners_ptr, rvc_ptr, gam_ptr, N, P_ptr, M, V_ptr, precision,
+                                              stream or None))
 
 
 class Case:
