@@ -1,25 +1,28 @@
 // FP32 Biot-Savart N-body kernel with FP64 accumulation and an FP64
 // near-field path, for sm_103a.  Compiled with -ftz=true.
 //
-// Layout: one block = 256 threads x 2 targets per thread, one chunk of source
-// records.  Source records (48 floats, 192 B) stream through a two-stage
-// shared-memory pipeline filled by bulk asynchronous copies (cp.async.bulk,
-// completion tracked on an mbarrier, every wait bounded); each staged record
-// is read with broadcast LDS.128 and evaluated for both targets of a thread.
+// Layout: one block = 8 consumer warps (256 threads x 2 targets per thread)
+// plus one producer warp, one chunk of source records.  Source records
+// (48 floats, 192 B) stream through a 4-stage shared-memory ring filled by
+// bulk asynchronous copies (cp.async.bulk) from the producer; FULL/EMPTY
+// mbarriers hand stages between producer and consumers (every wait bounded),
+// so consumer warps never wait for one another.  Each staged record is read
+// with broadcast LDS.128 and evaluated for both targets of a thread.
 //
 // Per target and ring: 4 corner vectors r_k = P - c_k with rsqrt norms, then
 // per filament k -> j = k+1 the Vatistas n=2 kernel (src/classdef.f90:476-503)
 //   v = (r_k x r_j) w_k (e.r_k/|r_k| - e.r_j/|r_j|) / sqrt((rvc|e|)^4 + |r_k x r_j|^4)
 // with e.r_j = e.r_k - |e|^2 and the source-only terms hoisted into the
-// record (w_k = gam/4pi).  A target on the filament line has r_k x r_j = 0
-// exactly, so its (finite) factor contributes exactly zero; the reference's
-// eps^2 cut-off needs no separate test.  FP32 partial sums are promoted to
+// record, the weight w_k = gam/4pi folded into e.  A target on the filament
+// line has r_k x r_j = 0 exactly, so its (finite) factor contributes exactly
+// zero; the reference's eps^2 cut-off needs no separate test.  FP32 partial sums are promoted to
 // the FP64 accumulator after every tile.
 //
 // Near field: one compare per ring (distance to corner 0 against the
-// record's reach) selects the rare candidates; their filaments inside
-// near_factor core radii of the segment are left out of the FP32 sum and
-// appended to a list that k_near64 evaluates coherently in FP64.
+// record's reach) selects the rare candidates; an out-of-line fix-up removes
+// the FP32 contributions of their filaments inside near_factor core radii of
+// the segment and lists them for k_near64, which evaluates them coherently in
+// FP64.
 #include <stdint.h>
 
 #include "vlm_bs.h"
@@ -31,10 +34,8 @@ namespace {
 
 constexpr int kThreads32 = 256;
 constexpr int kTPT = 2;         // targets per thread
-constexpr int kTile32 = 128;    // records per stage (128 x 192 B = 24 KB)
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr float kS2Min = 1e-30f;
-constexpr float kDenMin = 1.17549435e-38f;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -67,18 +68,107 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Near-field fix-up for one (target, record) candidate: recomputes the FP32
+// contributions of the record's filaments, removes those of the filaments
+// within the near zone from the FP32 sums and lists them for the FP64 pass.
+__device__ __noinline__ void near_fix(const float* __restrict__ R, float px, float py, float pz, float& ax, float& ay,
+                                      float& az, int m, int q, int rec, int* __restrict__ ctl,
+                                      NearPair* __restrict__ near, int near_cap) {
+  float rx[4], ry[4], rz[4], inv[4];
+  for (int k = 0; k < 4; ++k) {
+    rx[k] = px - R[3 * k];
+    ry[k] = py - R[3 * k + 1];
+    rz[k] = pz - R[3 * k + 2];
+    inv[k] = rsqrtf(fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], fmaf(rz[k], rz[k], kS2Min))));
+  }
+  for (int k = 0; k < 4; ++k) {
+    const int j = (k + 1) & 3;
+    const float kx = fmaf(ry[k], rz[j], -rz[k] * ry[j]);
+    const float ky = fmaf(rz[k], rx[j], -rx[k] * rz[j]);
+    const float kz = fmaf(rx[k], ry[j], -ry[k] * rx[j]);
+    const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
+    // geometric test with the unweighted edge
+    const float ex = R[3 * j] - R[3 * k], ey = R[3 * j + 1] - R[3 * k + 1], ez = R[3 * j + 2] - R[3 * k + 2];
+    const float te = fmaf(ex, rx[k], fmaf(ey, ry[k], ez * rz[k]));
+    const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez)), sl = R[40 + k];
+    if (c2 < R[32 + k] && c2 > kS2Min && te > -sl && te < ee + sl) {
+      // the exact FP32 contribution the main loop added
+      const float tt = fmaf(R[12 + 3 * k], rx[k], fmaf(R[13 + 3 * k], ry[k], R[14 + 3 * k] * rz[k]));
+      const float d = fmaf(tt, inv[k], -(tt - R[24 + k]) * inv[j]);
+      const float f = d * rsqrtf(fmaf(c2, c2, R[28 + k]));
+      ax = fmaf(-f, kx, ax);
+      ay = fmaf(-f, ky, ay);
+      az = fmaf(-f, kz, az);
+      const int slot = atomicAdd(ctl + 1, 1);
+      if (slot < near_cap) {
+        NearPair np;
+        np.m = m;
+        np.q = q;
+        np.rec = rec;
+        np.k = k;
+        near[slot] = np;
+      } else {
+        atomicExch(ctl, 3);
+      }
+    }
+  }
+}
+
+// One block = 8 consumer warps (256 threads x 2 targets) + 1 producer warp.
+// The producer's lane 0 streams the chunk's records through kStages shared
+// stages with bulk copies; consumers wait on a stage's FULL barrier, compute,
+// and release it through its EMPTY barrier (one arrival per consumer warp).
+constexpr int kStages = 4;
+constexpr int kTileW = 64;                  // records per stage (12 KB)
+constexpr int kConsumerWarps = 8;
+constexpr int kBlockW = (kConsumerWarps + 1) * 32;
+
 template <bool NEAR>
-__global__ void __launch_bounds__(kThreads32, 2) k_partial32(const float* __restrict__ rec32,
-                                                            const Chunk* __restrict__ chunks,
-                                                            const double* __restrict__ P, int M,
-                                                            double* __restrict__ part, int* __restrict__ ctl,
-                                                            NearPair* __restrict__ near, int near_cap) {
-  extern __shared__ __align__(16) float stage[];  // [2][kTile32 * kRec32]
-  __shared__ __align__(8) uint64_t bars[2];
+__global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restrict__ rec32,
+                                                         const Chunk* __restrict__ chunks,
+                                                         const double* __restrict__ P, int M,
+                                                         double* __restrict__ part, int* __restrict__ ctl,
+                                                         NearPair* __restrict__ near, int near_cap) {
+  extern __shared__ __align__(16) float stage[];  // [kStages][kTileW * kRec32]
+  __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ __align__(8) uint64_t empty[kStages];
   const int q = blockIdx.y;
   const Chunk ch = chunks[q];
   const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int ntiles = (ch.rec_count + kTileW - 1) / kTileW;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();  // the only block-wide barrier: roles split below
 
+  if (warp == kConsumerWarps) {
+    // ---- producer ----
+    if (lane == 0) {
+      for (int t = 0; t < ntiles; ++t) {
+        const int s = t % kStages;
+        if (t >= kStages && !mbar_wait(&empty[s], ((t / kStages) - 1) & 1)) atomicExch(ctl, 1);
+        const int n = min(kTileW, ch.rec_count - t * kTileW);
+        const uint32_t bytes = (uint32_t)n * kRec32 * 4u;
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(stage + s * kTileW * kRec32, rec32 + (size_t)(ch.rec_begin + t * kTileW) * kRec32, bytes, &full[s]);
+      }
+      // the block must not retire with a copy still writing its shared memory
+      for (int t = max(0, ntiles - kStages); t < ntiles; ++t)
+        if (!mbar_wait(&full[t % kStages], (t / kStages) & 1)) atomicExch(ctl, 2);
+    }
+    return;
+  }
+
+  // ---- consumers ----
   int mt[kTPT];
   float px[kTPT], py[kTPT], pz[kTPT];
   double acc64[kTPT][3];
@@ -91,41 +181,16 @@ __global__ void __launch_bounds__(kThreads32, 2) k_partial32(const float* __rest
     pz[u] = (float)P[3 * (size_t)mm + 2];
     acc64[u][0] = acc64[u][1] = acc64[u][2] = 0.0;
   }
-
-  const int ntiles = (ch.rec_count + kTile32 - 1) / kTile32;
-  if (tid == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  auto issue = [&](int t) {
-    const int n = min(kTile32, ch.rec_count - t * kTile32);
-    const uint32_t bytes = (uint32_t)n * kRec32 * 4u;
-    uint64_t* bar = &bars[t & 1];
-    mbar_expect_tx(bar, bytes);
-    bulk_g2s(stage + (t & 1) * kTile32 * kRec32, rec32 + (size_t)(ch.rec_begin + t * kTile32) * kRec32, bytes, bar);
-  };
-  // pend[b]: tile whose copy into stage b thread 0 has not yet seen complete
-  int pend[2] = {-1, -1};
-  if (tid == 0 && ntiles > 0) {
-    issue(0);
-    pend[0] = 0;
-  }
   bool ok = true;
   for (int t = 0; t < ntiles; ++t) {
-    if (tid == 0 && ok && t + 1 < ntiles) {
-      issue(t + 1);
-      pend[(t + 1) & 1] = t + 1;
-    }
-    if (ok && !mbar_wait(&bars[t & 1], (t >> 1) & 1)) {
+    const int s = t % kStages;
+    if (!mbar_wait(&full[s], (t / kStages) & 1)) {
       ok = false;
       atomicExch(ctl, 1);
     }
-    if (ok && tid == 0) pend[t & 1] = -1;
     if (ok) {
-      const int n = min(kTile32, ch.rec_count - t * kTile32);
-      const float* tile = stage + (t & 1) * kTile32 * kRec32;
+      const int n = min(kTileW, ch.rec_count - t * kTileW);
+      const float* tile = stage + s * kTileW * kRec32;
       float ax[kTPT], ay[kTPT], az[kTPT];
 #pragma unroll
       for (int u = 0; u < kTPT; ++u) ax[u] = ay[u] = az[u] = 0.f;
@@ -134,7 +199,7 @@ __global__ void __launch_bounds__(kThreads32, 2) k_partial32(const float* __rest
         const float4* R4 = reinterpret_cast<const float4*>(tile + r * kRec32);
         const float4 q0 = R4[0], q1 = R4[1], q2 = R4[2];  // corners
         const float4 q3 = R4[3], q4 = R4[4], q5 = R4[5];  // edges
-        const float4 ee = R4[6], a4 = R4[7], w = R4[9];
+        const float4 ee = R4[6], a4 = R4[7];
         const float cx[4] = {q0.x, q0.w, q1.z, q2.y};
         const float cy[4] = {q0.y, q1.x, q1.w, q2.z};
         const float cz[4] = {q0.z, q1.y, q2.x, q2.w};
@@ -143,22 +208,18 @@ __global__ void __launch_bounds__(kThreads32, 2) k_partial32(const float* __rest
         const float ez[4] = {q3.z, q4.y, q5.x, q5.w};
         const float eev[4] = {ee.x, ee.y, ee.z, ee.w};
         const float a4v[4] = {a4.x, a4.y, a4.z, a4.w};
-        const float wv[4] = {w.x, w.y, w.z, w.w};
-        float reach2 = -1.f;
-        if (NEAR) reach2 = tile[r * kRec32 + 44];
+        const float reach2 = NEAR ? tile[r * kRec32 + 44] : -1.f;
 #pragma unroll
         for (int u = 0; u < kTPT; ++u) {
-          float rx[4], ry[4], rz[4], inv[4], s0 = 0.f;
+          float rx[4], ry[4], rz[4], inv[4];
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             rx[k] = px[u] - cx[k];
             ry[k] = py[u] - cy[k];
             rz[k] = pz[u] - cz[k];
-            const float s = fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], rz[k] * rz[k]));
-            if (k == 0) s0 = s;
-            inv[k] = rsqrtf(fmaxf(s, kS2Min));
+            // |r|^2 + 1e-30: a target on a corner gets a finite 1/|r| (times r = 0)
+            inv[k] = rsqrtf(fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], fmaf(rz[k], rz[k], kS2Min))));
           }
-          const bool cand = NEAR && s0 < reach2 && mt[u] < M;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const int j = (k + 1) & 3;
@@ -166,31 +227,19 @@ __global__ void __launch_bounds__(kThreads32, 2) k_partial32(const float* __rest
             const float ky = fmaf(rz[k], rx[j], -rx[k] * rz[j]);
             const float kz = fmaf(rx[k], ry[j], -ry[k] * rx[j]);
             const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
+            // w (e.r_k/|r_k| - e.r_j/|r_j|) with the weight folded into e
             const float tt = fmaf(ex[k], rx[k], fmaf(ey[k], ry[k], ez[k] * rz[k]));
             const float d = fmaf(tt, inv[k], -(tt - eev[k]) * inv[j]);
-            const float den = fmaxf(fmaf(c2, c2, a4v[k]), kDenMin);
-            float f = wv[k] * d * rsqrtf(den);
-            if (NEAR && cand) {
-              const float nfk = tile[r * kRec32 + 32 + k];
-              const float slk = tile[r * kRec32 + 40 + k];
-              if (c2 < nfk && c2 > kS2Min && tt > -slk && tt < eev[k] + slk) {
-                f = 0.f;
-                const int slot = atomicAdd(ctl + 1, 1);
-                if (slot < near_cap) {
-                  NearPair np;
-                  np.m = mt[u];
-                  np.q = q;
-                  np.rec = ch.rec_begin + t * kTile32 + r;
-                  np.k = k;
-                  near[slot] = np;
-                } else {
-                  atomicExch(ctl, 3);
-                }
-              }
-            }
+            const float f = d * rsqrtf(fmaf(c2, c2, a4v[k]));
             ax[u] = fmaf(f, kx, ax[u]);
             ay[u] = fmaf(f, ky, ay[u]);
             az[u] = fmaf(f, kz, az[u]);
+          }
+          if (NEAR) {
+            const float s0 = fmaf(rx[0], rx[0], fmaf(ry[0], ry[0], rz[0] * rz[0]));
+            if (s0 < reach2 && mt[u] < M)
+              near_fix(tile + r * kRec32, px[u], py[u], pz[u], ax[u], ay[u], az[u], mt[u], q,
+                       ch.rec_begin + t * kTileW + r, ctl, near, near_cap);
           }
         }
       }
@@ -201,13 +250,8 @@ __global__ void __launch_bounds__(kThreads32, 2) k_partial32(const float* __rest
         acc64[u][2] += (double)az[u];
       }
     }
-    __syncthreads();
-  }
-  if (tid == 0) {
-    // a copy issued by this thread but never seen complete may still be
-    // writing the stage buffers: wait for it (bounded) before the block exits
-    for (int b = 0; b < 2; ++b)
-      if (pend[b] >= 0 && !mbar_wait(&bars[b], (pend[b] >> 1) & 1)) atomicExch(ctl, 2);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
@@ -283,15 +327,16 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
     o[3 * k] = (float)c[k].x;
     o[3 * k + 1] = (float)c[k].y;
     o[3 * k + 2] = (float)c[k].z;
-    o[12 + 3 * k] = (float)e.x;
-    o[12 + 3 * k + 1] = (float)e.y;
-    o[12 + 3 * k + 2] = (float)e.z;
-    o[24 + k] = (float)ee;
-    o[28 + k] = (float)pow4(s);
+    const double wk = (act[k] && !skipped) ? w : 0.0;
+    o[12 + 3 * k] = (float)(wk * e.x);
+    o[12 + 3 * k + 1] = (float)(wk * e.y);
+    o[12 + 3 * k + 2] = (float)(wk * e.z);
+    o[24 + k] = (float)(wk * ee);
+    o[28 + k] = (float)fmax(pow4(s), 1e-36);
     const bool on = act[k] && !skipped && near_factor > 0.0;
     const double nfs = near_factor * s;
     o[32 + k] = on ? (float)(nfs * nfs) : -1.f;
-    o[36 + k] = (act[k] && !skipped) ? (float)w : 0.f;
+    o[36 + k] = (float)wk;
     o[40 + k] = on ? (float)nfs : 0.f;
     if (on) {
       anyNear = true;
@@ -315,7 +360,7 @@ void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
                       int M, double* part, int* ctl, NearPair* near, int near_cap, cudaStream_t s) {
   if (M <= 0 || nchunks <= 0) return;
-  const int smem = 2 * kTile32 * kRec32 * (int)sizeof(float);
+  const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -325,11 +370,11 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   dim3 grid((M + kTPT * kThreads32 - 1) / (kTPT * kThreads32), nchunks);
   count_launch();
   if (near) {
-    k_partial32<true><<<grid, kThreads32, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
     count_launch();
     k_near64<<<4 * 152, 128, 0, s>>>(near, ctl, near_cap, rec64, P, M, part);
   } else {
-    k_partial32<false><<<grid, kThreads32, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
   }
 }
 

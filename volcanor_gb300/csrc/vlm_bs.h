@@ -30,17 +30,18 @@ constexpr int REC_SKIP = 2;
 
 // FP32 source record, 48 floats (192 B, 16-byte aligned for bulk copies):
 //   [0..11]  corners c0..c3
-//   [12..23] edge vectors e_k = c_{k+1} - c_k
-//   [24..27] |e_k|^2
-//   [28..31] (rvc_k |e_k|)^4
+//   [12..23] weighted edge vectors w_k e_k, e_k = c_{k+1} - c_k, w_k = gam/(4 pi)
+//   [24..27] w_k |e_k|^2
+//   [28..31] (rvc_k |e_k|)^4, floored at 1e-36 so the kernel needs no clamp
 //   [32..35] near-field threshold on |r1 x r2|^2: (near_factor rvc_k |e_k|)^2, -1 if off
-//   [36..39] w_k = gam / (4 pi) for active edges, 0 for inactive / skipped
+//   [36..39] w_k for active edges, 0 for inactive / skipped
 //   [40..43] near-field slack along the filament: near_factor rvc_k |e_k|
 //   [44]     squared radius about corner 0 outside which no filament of the
 //            record can be near (-1 when the near-field path is off)
 //   [45..47] unused
 // A pair is near when the target lies within near_factor core radii of the
-// filament SEGMENT: |r1 x r2|^2 < [32+k] and -[40+k] < e.r1 < |e|^2 + [40+k].
+// filament SEGMENT: |r1 x r2|^2 < [32+k] and -[40+k] < e.r1 < |e|^2 + [40+k]
+// (e recomputed from the corners).
 constexpr int kRec32 = 48;
 
 // One near-field pair found by the FP32 kernel: target m, chunk q (partial
