@@ -257,6 +257,8 @@ def run_ours(args):
         pass
     # roofline of the dominant kernel on the live steady-state state
     ms_l, rp, fp = case.profile_eval(20)
+    near_pairs = case.geti("nearPairs") if prec == lib.PREC_FP32_NEAR64 else 0
+    node_chunks = case.geti("nodeChunks")
     flops = RING_FLOP * rp + FIL_FLOP * fp
     achieved = flops / (ms_l / 1e3) / 1e12
     pk = peaks()
@@ -287,6 +289,7 @@ def run_ours(args):
                      "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4), "traffic": None,
                      "kernel": "k_partial32" if prec != lib.PREC_FP64 else "k_partial64",
                      "ms_per_launch": round(ms_l, 4), "ring_pairs_per_launch": rp, "fil_pairs_per_launch": fp,
+                     "near_pairs_per_launch": near_pairs, "chunks": node_chunks,
                      "peak_note": "nominal FP32 CUDA-core peak (SMs x 128 lanes x 2 x max SM clock); "
                                   "MEASURED_PEAKS.json has no FP32 figure"},
         "clocks": clocks,

@@ -125,7 +125,9 @@ int vlm_case_start(vlm_case* c);
  * CFz) -- the rXXForceNonDim.csv columns (src/libPostprocess.f90:814-838). */
 int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows);
 /* Integer state: nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter,
- * nbConvect, wakeTruncateNt. */
+ * nbConvect, wakeTruncateNt; nearPairs (near-field filament-target pairs of the
+ * last FP32 evaluation) and nodeChunks (chunks of the next step's wake-node
+ * evaluation) describe this library's kernels. */
 int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
 /* Copy a named array (see the design doc for the list and layouts) into out.
  * Returns the element count, or -1 for an unknown name. */

@@ -54,3 +54,15 @@ def test_case_text_roundtrip_through_the_oracle_reader():
     s = O.Sim(c.config, c.geom)
     assert s.geti("nb") == 2 and s.geti("ns") == 24 and s.geti("nNwake") == 6 and s.geti("nFwake") == 3
     np.testing.assert_allclose(s.get("dt"), [5.0 * np.pi / 180.0 / 100.0], rtol=1e-15)
+
+
+def test_fp32_chunk_plan_shapes():
+    """The FP32 chunk planner: one chunk when the target blocks alone fill the
+    GPU many times, small chunks when a few targets face many rings."""
+    big = lib.rings_sum_chunk(1 << 18, 1 << 20, lib.PREC_FP32)
+    assert (1 << 18) // 16 <= big <= 1 << 18
+    small = lib.rings_sum_chunk(12480, 24, lib.PREC_FP32)
+    assert 16 <= small <= 128
+    mid = lib.rings_sum_chunk(12480, 13395, lib.PREC_FP32_NEAR64)
+    assert 128 <= mid < 12480
+    assert lib.rings_sum_chunk(0, 100, lib.PREC_FP32) == 0

@@ -18,12 +18,17 @@
 // zero; the reference's eps^2 cut-off needs no separate test.  FP32 partial sums are promoted to
 // the FP64 accumulator after every tile.
 //
-// Near field: one compare per ring (distance to corner 0 against the
-// record's reach) selects the rare candidates; an out-of-line fix-up removes
-// the FP32 contributions of their filaments inside near_factor core radii of
-// the segment and lists them for k_near64, which evaluates them coherently in
-// FP64.
+// Near field: one compare per target and ring (distance to corner 0 against
+// the record's reach) and a warp vote select the records some lane of the
+// warp may be near; for those the warp evaluates the record with a per-
+// filament near-zone test that leaves near filaments out of the FP32 sum and
+// appends one (target, record, filament) entry per near filament to a list.  k_near64 evaluates
+// the list coherently in FP64 into order-independent fixed-point
+// accumulators, and k_near_apply adds them to the chunk partial sums, so the
+// result does not depend on the order of the list.
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "vlm_bs.h"
 #include "vlm_math.h"
@@ -72,50 +77,83 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Near-field fix-up for one (target, record) candidate: recomputes the FP32
-// contributions of the record's filaments, removes those of the filaments
-// within the near zone from the FP32 sums and lists them for the FP64 pass.
-__device__ __noinline__ void near_fix(const float* __restrict__ R, float px, float py, float pz, float& ax, float& ay,
-                                      float& az, int m, int q, int rec, int* __restrict__ ctl,
-                                      NearPair* __restrict__ near, int near_cap) {
-  float rx[4], ry[4], rz[4], inv[4];
-  for (int k = 0; k < 4; ++k) {
-    rx[k] = px - R[3 * k];
-    ry[k] = py - R[3 * k + 1];
-    rz[k] = pz - R[3 * k + 2];
-    inv[k] = rsqrtf(fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], fmaf(rz[k], rz[k], kS2Min))));
+constexpr unsigned kFull = 0xffffffffu;
+
+// Appends one list entry per near filament (bits of msk) of this warp's
+// lanes: a warp prefix sum of the bit counts, one atomic per warp.
+__device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec, int lane, int* __restrict__ ctl,
+                                            NearPair* __restrict__ near, int near_cap) {
+  const int cnt = __popc(msk);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += v;
   }
+  const int total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(ctl + 1, total);
+  base = __shfl_sync(kFull, base, 0);
+  int slot = base + incl - cnt;
+  for (unsigned b = msk; b; b &= b - 1u, ++slot) {
+    if (slot < near_cap) {
+      NearPair np;
+      np.m = m;
+      np.q = q;
+      np.rec = rec;
+      np.k = __ffs(b) - 1;
+      near[slot] = np;
+    } else {
+      atomicExch(ctl, 3);
+    }
+  }
+}
+
+// Adds the FP32 velocity of one record at one target (corner vectors r_k and
+// rsqrt norms given).  CHECK: also tests every filament against its near
+// zone, leaves the near ones out and returns their bit mask.
+template <bool CHECK>
+__device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, const float (&rx)[4], const float (&ry)[4],
+                                              const float (&rz)[4], const float (&inv)[4], float& ax, float& ay,
+                                              float& az) {
+  const float4 q3 = R4[3], q4 = R4[4], q5 = R4[5];  // weighted edges
+  const float4 ee = R4[6], a4 = R4[7];
+  const float ex[4] = {q3.x, q3.w, q4.z, q5.y};
+  const float ey[4] = {q3.y, q4.x, q4.w, q5.z};
+  const float ez[4] = {q3.z, q4.y, q5.x, q5.w};
+  const float eev[4] = {ee.x, ee.y, ee.z, ee.w};
+  const float a4v[4] = {a4.x, a4.y, a4.z, a4.w};
+  float thr[4], lo[4], hi[4];
+  if (CHECK) {
+    const float4 t = R4[8], l = R4[9], h = R4[10];
+    thr[0] = t.x, thr[1] = t.y, thr[2] = t.z, thr[3] = t.w;
+    lo[0] = l.x, lo[1] = l.y, lo[2] = l.z, lo[3] = l.w;
+    hi[0] = h.x, hi[1] = h.y, hi[2] = h.z, hi[3] = h.w;
+  }
+  unsigned msk = 0u;
+#pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int j = (k + 1) & 3;
     const float kx = fmaf(ry[k], rz[j], -rz[k] * ry[j]);
     const float ky = fmaf(rz[k], rx[j], -rx[k] * rz[j]);
     const float kz = fmaf(rx[k], ry[j], -ry[k] * rx[j]);
     const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
-    // geometric test with the unweighted edge
-    const float ex = R[3 * j] - R[3 * k], ey = R[3 * j + 1] - R[3 * k + 1], ez = R[3 * j + 2] - R[3 * k + 2];
-    const float te = fmaf(ex, rx[k], fmaf(ey, ry[k], ez * rz[k]));
-    const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez)), sl = R[40 + k];
-    if (c2 < R[32 + k] && c2 > kS2Min && te > -sl && te < ee + sl) {
-      // the exact FP32 contribution the main loop added
-      const float tt = fmaf(R[12 + 3 * k], rx[k], fmaf(R[13 + 3 * k], ry[k], R[14 + 3 * k] * rz[k]));
-      const float d = fmaf(tt, inv[k], -(tt - R[24 + k]) * inv[j]);
-      const float f = d * rsqrtf(fmaf(c2, c2, R[28 + k]));
-      ax = fmaf(-f, kx, ax);
-      ay = fmaf(-f, ky, ay);
-      az = fmaf(-f, kz, az);
-      const int slot = atomicAdd(ctl + 1, 1);
-      if (slot < near_cap) {
-        NearPair np;
-        np.m = m;
-        np.q = q;
-        np.rec = rec;
-        np.k = k;
-        near[slot] = np;
-      } else {
-        atomicExch(ctl, 3);
-      }
+    // w (e.r_k/|r_k| - e.r_j/|r_j|) with the weight folded into e
+    const float tt = fmaf(ex[k], rx[k], fmaf(ey[k], ry[k], ez[k] * rz[k]));
+    const float d = fmaf(tt, inv[k], -(tt - eev[k]) * inv[j]);
+    float f = d * rsqrtf(fmaf(c2, c2, a4v[k]));
+    if (CHECK) {
+      // exact zeros (target on the filament line) stay in the FP32 sum
+      const bool nr = c2 < thr[k] && c2 > kS2Min && tt > lo[k] && tt < hi[k];
+      f = nr ? 0.f : f;
+      msk |= nr ? (1u << k) : 0u;
     }
+    ax = fmaf(f, kx, ax);
+    ay = fmaf(f, ky, ay);
+    az = fmaf(f, kz, az);
   }
+  return msk;
 }
 
 // One block = 8 consumer warps (256 threads x 2 targets) + 1 producer warp.
@@ -126,6 +164,7 @@ constexpr int kStages = 4;
 constexpr int kTileW = 64;                  // records per stage (12 KB)
 constexpr int kConsumerWarps = 8;
 constexpr int kBlockW = (kConsumerWarps + 1) * 32;
+static_assert(kConsumerWarps * 32 * kTPT == kTargetsPerBlock32, "targets per block");
 
 template <bool NEAR>
 __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restrict__ rec32,
@@ -170,12 +209,14 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
 
   // ---- consumers ----
   int mt[kTPT];
+  bool valid[kTPT];
   float px[kTPT], py[kTPT], pz[kTPT];
   double acc64[kTPT][3];
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
     mt[u] = (blockIdx.x * kTPT + u) * kThreads32 + tid;
-    const int mm = mt[u] < M ? mt[u] : M - 1;
+    valid[u] = mt[u] < M;
+    const int mm = valid[u] ? mt[u] : M - 1;
     px[u] = (float)P[3 * (size_t)mm];
     py[u] = (float)P[3 * (size_t)mm + 1];
     pz[u] = (float)P[3 * (size_t)mm + 2];
@@ -184,9 +225,10 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   bool ok = true;
   for (int t = 0; t < ntiles; ++t) {
     const int s = t % kStages;
-    if (!mbar_wait(&full[s], (t / kStages) & 1)) {
+    // the warp goes on only if every lane saw the stage arrive
+    if (!__all_sync(kFull, mbar_wait(&full[s], (t / kStages) & 1))) {
       ok = false;
-      atomicExch(ctl, 1);
+      if (lane == 0) atomicExch(ctl, 1);
     }
     if (ok) {
       const int n = min(kTileW, ch.rec_count - t * kTileW);
@@ -198,49 +240,35 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
       for (int r = 0; r < n; ++r) {
         const float4* R4 = reinterpret_cast<const float4*>(tile + r * kRec32);
         const float4 q0 = R4[0], q1 = R4[1], q2 = R4[2];  // corners
-        const float4 q3 = R4[3], q4 = R4[4], q5 = R4[5];  // edges
-        const float4 ee = R4[6], a4 = R4[7];
         const float cx[4] = {q0.x, q0.w, q1.z, q2.y};
         const float cy[4] = {q0.y, q1.x, q1.w, q2.z};
         const float cz[4] = {q0.z, q1.y, q2.x, q2.w};
-        const float ex[4] = {q3.x, q3.w, q4.z, q5.y};
-        const float ey[4] = {q3.y, q4.x, q4.w, q5.z};
-        const float ez[4] = {q3.z, q4.y, q5.x, q5.w};
-        const float eev[4] = {ee.x, ee.y, ee.z, ee.w};
-        const float a4v[4] = {a4.x, a4.y, a4.z, a4.w};
-        const float reach2 = NEAR ? tile[r * kRec32 + 44] : -1.f;
+        float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
+        bool cand = false;
 #pragma unroll
         for (int u = 0; u < kTPT; ++u) {
-          float rx[4], ry[4], rz[4], inv[4];
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            rx[k] = px[u] - cx[k];
-            ry[k] = py[u] - cy[k];
-            rz[k] = pz[u] - cz[k];
+            rx[u][k] = px[u] - cx[k];
+            ry[u][k] = py[u] - cy[k];
+            rz[u][k] = pz[u] - cz[k];
             // |r|^2 + 1e-30: a target on a corner gets a finite 1/|r| (times r = 0)
-            inv[k] = rsqrtf(fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], fmaf(rz[k], rz[k], kS2Min))));
+            const float s2 = fmaf(rx[u][k], rx[u][k], fmaf(ry[u][k], ry[u][k], fmaf(rz[u][k], rz[u][k], kS2Min)));
+            inv[u][k] = rsqrtf(s2);
+            if (NEAR && k == 0) cand |= valid[u] && s2 < tile[r * kRec32 + 44];
           }
+        }
+        if (NEAR && __any_sync(kFull, cand)) {
+          // some lane of the warp is within reach of this record
+          const int rec = ch.rec_begin + t * kTileW + r;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int j = (k + 1) & 3;
-            const float kx = fmaf(ry[k], rz[j], -rz[k] * ry[j]);
-            const float ky = fmaf(rz[k], rx[j], -rx[k] * rz[j]);
-            const float kz = fmaf(rx[k], ry[j], -ry[k] * rx[j]);
-            const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
-            // w (e.r_k/|r_k| - e.r_j/|r_j|) with the weight folded into e
-            const float tt = fmaf(ex[k], rx[k], fmaf(ey[k], ry[k], ez[k] * rz[k]));
-            const float d = fmaf(tt, inv[k], -(tt - eev[k]) * inv[j]);
-            const float f = d * rsqrtf(fmaf(c2, c2, a4v[k]));
-            ax[u] = fmaf(f, kx, ax[u]);
-            ay[u] = fmaf(f, ky, ay[u]);
-            az[u] = fmaf(f, kz, az[u]);
+          for (int u = 0; u < kTPT; ++u) {
+            unsigned msk = ring_fp32<true>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
+            near_append(valid[u] ? msk : 0u, mt[u], q, rec, lane, ctl, near, near_cap);
           }
-          if (NEAR) {
-            const float s0 = fmaf(rx[0], rx[0], fmaf(ry[0], ry[0], rz[0] * rz[0]));
-            if (s0 < reach2 && mt[u] < M)
-              near_fix(tile + r * kRec32, px[u], py[u], pz[u], ax[u], ay[u], az[u], mt[u], q,
-                       ch.rec_begin + t * kTileW + r, ctl, near, near_cap);
-          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < kTPT; ++u) ring_fp32<false>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
         }
       }
 #pragma unroll
@@ -255,7 +283,7 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   }
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
-    if (mt[u] < M) {
+    if (valid[u]) {
       double* o = part + ((size_t)q * M + mt[u]) * 3;
       o[0] = acc64[u][0];
       o[1] = acc64[u][1];
@@ -264,11 +292,12 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   }
 }
 
-// FP64 evaluation of the listed near-field pairs (reference arithmetic),
-// added to the partial sums of their chunks.
-__global__ void k_near64(const NearPair* __restrict__ near, const int* __restrict__ ctl, int near_cap,
+// FP64 evaluation of the listed near-field filament-target pairs (reference
+// arithmetic: filament velocity times the circulation), added in fixed point
+// to the accumulators of their (chunk, target).
+__global__ void k_near64(const NearPair* __restrict__ near, int* __restrict__ ctl, int near_cap,
                          const double* __restrict__ rec64, const double* __restrict__ P, int M,
-                         double* __restrict__ part) {
+                         unsigned long long* __restrict__ nacc) {
   const int n = min(ctl[1], near_cap);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const NearPair np = near[i];
@@ -283,10 +312,26 @@ __global__ void k_near64(const NearPair* __restrict__ near, const int* __restric
                     make_corner64(p, mk3(R[3 * j], R[3 * j + 1], R[3 * j + 2])), R[12 + k]);
     }
     v = v * R[16];
-    double* o = part + ((size_t)np.q * M + np.m) * 3;
-    atomicAdd(o, v.x);
-    atomicAdd(o + 1, v.y);
-    atomicAdd(o + 2, v.z);
+    unsigned long long* o = nacc + ((size_t)np.q * M + np.m) * 3;
+    const double c[3] = {v.x, v.y, v.z};
+    for (int a = 0; a < 3; ++a) {
+      if (!(fabs(c[a]) < kNearMax)) {
+        atomicExch(ctl, 4);
+        continue;
+      }
+      atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
+    }
+  }
+}
+
+// part += nacc / 2^44, and nacc back to zero for the next evaluation.
+__global__ void k_near_apply(double* __restrict__ part, long long* __restrict__ nacc, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const long long a = nacc[i];
+    if (a != 0) {
+      part[i] += (double)a * (1.0 / kNearScale);
+      nacc[i] = 0;
+    }
   }
 }
 
@@ -336,8 +381,10 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
     const bool on = act[k] && !skipped && near_factor > 0.0;
     const double nfs = near_factor * s;
     o[32 + k] = on ? (float)(nfs * nfs) : -1.f;
-    o[36 + k] = (float)wk;
-    o[40 + k] = on ? (float)nfs : 0.f;
+    // -s < e.r1 < |e|^2 + s, multiplied by w_k
+    const double blo = -nfs * wk, bhi = (ee + nfs) * wk;
+    o[36 + k] = on ? (float)fmin(blo, bhi) : 0.f;
+    o[40 + k] = on ? (float)fmax(blo, bhi) : 0.f;
     if (on) {
       anyNear = true;
       // farthest point of this filament's near zone from corner 0
@@ -358,7 +405,7 @@ void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec
 }
 
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
-                      int M, double* part, int* ctl, NearPair* near, int near_cap, cudaStream_t s) {
+                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s) {
   if (M <= 0 || nchunks <= 0) return;
   const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
   static bool attr = false;
@@ -367,15 +414,34 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
     cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  dim3 grid((M + kTPT * kThreads32 - 1) / (kTPT * kThreads32), nchunks);
+  dim3 grid((M + kTargetsPerBlock32 - 1) / kTargetsPerBlock32, nchunks);
   count_launch();
   if (near) {
     k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
     count_launch();
-    k_near64<<<4 * 152, 128, 0, s>>>(near, ctl, near_cap, rec64, P, M, part);
+    k_near64<<<4 * 152, 128, 0, s>>>(near, ctl, near_cap, rec64, P, M, reinterpret_cast<unsigned long long*>(nacc));
+    const size_t n = (size_t)M * nchunks * 3;
+    count_launch();
+    k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, 8 * 152), 256, 0, s>>>(part, nacc, n);
   } else {
     k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
   }
+}
+
+int partial32_slots() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 2 * 152;
+  if (!cache[dev]) {
+    int sms = 0, per = 0;
+    const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
+    cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true>, kBlockW, smem);
+    cache[dev] = std::max(1, sms) * std::max(1, per);
+  }
+  return cache[dev];
 }
 
 }  // namespace vlm

@@ -69,7 +69,22 @@ __global__ void k_combine(const double* __restrict__ part, int M, const Group* _
   for (int g = 0; g < ngroups; ++g) {
     const Group G = groups[g];
     d3 gs = zero3();
-    for (int q = G.chunk_begin; q < G.chunk_begin + G.chunk_count; ++q) {
+    int q = G.chunk_begin;
+    const int qe = G.chunk_begin + G.chunk_count;
+    // loads issued 16 at a time (the adds stay in chunk order): a collocation-
+    // point evaluation has few targets and hundreds of chunks
+    constexpr int kB = 16;
+    for (; q + kB <= qe; q += kB) {
+      d3 buf[kB];
+#pragma unroll
+      for (int i = 0; i < kB; ++i) {
+        const double* pp = part + ((size_t)(q + i) * M + m) * 3;
+        buf[i] = mk3(pp[0], pp[1], pp[2]);
+      }
+#pragma unroll
+      for (int i = 0; i < kB; ++i) gs = gs + buf[i];
+    }
+    for (; q < qe; ++q) {
       const double* pp = part + ((size_t)q * M + m) * 3;
       gs = gs + mk3(pp[0], pp[1], pp[2]);
     }
@@ -83,6 +98,44 @@ __global__ void k_combine(const double* __restrict__ part, int M, const Group* _
   out[3 * (size_t)m] = v.x;
   out[3 * (size_t)m + 1] = v.y;
   out[3 * (size_t)m + 2] = v.z;
+}
+
+// Unordered combine (FP32 paths, whose summation order is free): G lanes
+// per target (G a power of two <= 32); lane l of a target adds chunk
+// partials l, l + G, ... of a group in order, then a butterfly over the G
+// lanes.  The tree has a fixed shape, so the result is reproducible run to
+// run; the serial chain is chunks/G adds long.
+__global__ void k_combine_tree(const double* __restrict__ part, int M, const Group* __restrict__ groups, int ngroups,
+                               int mode, int G, double* __restrict__ out) {
+  const size_t gt = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int m = (int)(gt / G), l = (int)(gt % G);
+  const bool live = m < M;  // dead lanes still take part in the shuffles
+  d3 wing = zero3(), wake = zero3();
+  for (int g = 0; g < ngroups; ++g) {
+    const Group G_ = groups[g];
+    d3 gs = zero3();
+    if (live)
+      for (int q = G_.chunk_begin + l; q < G_.chunk_begin + G_.chunk_count; q += G) {
+        const double* pp = part + ((size_t)q * M + m) * 3;
+        gs = gs + mk3(pp[0], pp[1], pp[2]);
+      }
+    for (int o = G >> 1; o > 0; o >>= 1) {
+      gs.x = gs.x + __shfl_xor_sync(0xffffffffu, gs.x, o, G);
+      gs.y = gs.y + __shfl_xor_sync(0xffffffffu, gs.y, o, G);
+      gs.z = gs.z + __shfl_xor_sync(0xffffffffu, gs.z, o, G);
+    }
+    if (G_.kind == 0) wing = wing + gs;
+    else wake = wake + gs;
+  }
+  if (live && l == 0) {
+    d3 v;
+    if (mode == 0) v = zero3() + (wing + wake);
+    else if (mode == 1) v = wake;
+    else v = wing + wake;
+    out[3 * (size_t)m] = v.x;
+    out[3 * (size_t)m + 1] = v.y;
+    out[3 * (size_t)m + 2] = v.z;
+  }
 }
 
 __global__ void k_rings_to_rec64(const double* __restrict__ corners, const double* __restrict__ rvc,
@@ -134,6 +187,17 @@ void launch_combine(const double* part, int M, const Group* groups, int ngroups,
   if (M <= 0) return;
   count_launch();
   k_combine<<<(M + 127) / 128, 128, 0, s>>>(part, M, groups, ngroups, mode, out);
+}
+
+void launch_combine_unordered(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
+                              double* out, cudaStream_t s) {
+  if (M <= 0) return;
+  // about 8 chunk partials per lane, at most a warp per target
+  int G = 1;
+  while (G < 32 && G * 8 < max_chunks) G <<= 1;
+  const size_t threads = (size_t)M * G;
+  count_launch();
+  k_combine_tree<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(part, M, groups, ngroups, mode, G, out);
 }
 
 void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,

@@ -52,6 +52,7 @@ struct EvalPlan {
   int goff = 0, ngroups = 0;  // into the step plan's group table
   int coff = 0, nchunks = 0;  // into the chunk table
   int nrec = 0;
+  int maxq = 0;  // most chunks of one group
 };
 struct StepPlan {
   int rowNear = 0, rowFar = 0;
@@ -74,9 +75,11 @@ struct Case {
   Chunk* dChunks = nullptr;
   int iter = 0;
   bool started = false;
-  int chunk64 = 0, chunk32 = 0;
+  int chunk64 = 0;
+  int slots32 = 0;  // resident FP32-kernel blocks on the device (chunk planner input)
   double lastMs = 0;
   int maxTargets = 0, maxRecords = 0, maxChunks = 0;
+  int64_t maxPart = 1;  // largest (chunks x targets) of any evaluation
 
   ~Case() {
     if (stream) cudaStreamSynchronize(stream);
@@ -87,11 +90,16 @@ struct Case {
     if (stream) cudaStreamDestroy(stream);
   }
 
-  int chunkSize() const { return opt.precision == VLM_PREC_FP64 ? chunk64 : chunk32; }
+  // chunk table of one evaluation: the FP64 summation order, or the FP32
+  // kernel's planned chunks for M targets
+  int chunkTable(Group* g, int ng, int M, Chunk* out, int cap) const {
+    if (opt.precision == VLM_PREC_FP64) return build_chunks(g, ng, chunk64, out, cap);
+    return plan_chunks32(g, ng, M, slots32, out, cap);
+  }
 
   // groups of one evaluation: wing sums (kind 0) for every blade when
   // withWing, then wake sums (kind 1) for every blade
-  void addEval(EvalPlan& e, bool withWing, int rowNear, int rowFar) {
+  void addEval(EvalPlan& e, bool withWing, int rowNear, int rowFar, int M) {
     const int NW = d.NW, NF = d.NF, ns = d.ns;
     e.goff = (int)hGroups.size();
     int rec = 0;
@@ -121,12 +129,14 @@ struct Case {
     e.nrec = rec;
     e.coff = (int)hChunks.size();
     std::vector<Chunk> tmp(rec + e.ngroups + 1);
-    const int nq = build_chunks(hGroups.data() + e.goff, e.ngroups, chunkSize(), tmp.data(), (int)tmp.size());
+    const int nq = chunkTable(hGroups.data() + e.goff, e.ngroups, M, tmp.data(), (int)tmp.size());
     if (nq < 0) throw std::runtime_error("chunk table overflow");
     hChunks.insert(hChunks.end(), tmp.begin(), tmp.begin() + nq);
     e.nchunks = nq;
+    for (int g = e.goff; g < e.goff + e.ngroups; ++g) e.maxq = std::max(e.maxq, hGroups[g].chunk_count);
     maxRecords = std::max(maxRecords, rec);
     maxChunks = std::max(maxChunks, nq);
+    maxPart = std::max(maxPart, (int64_t)nq * M);
   }
 
   void create(const std::string& cfg, const std::string& geo, const std::string& base, const vlm_options* o) {
@@ -134,7 +144,6 @@ struct Case {
     if (o) opt = *o;
     if (opt.precision < 0 || opt.precision > 2) throw StatusError(VLM_ERR_INVALID, "precision must be 0, 1 or 2");
     chunk64 = opt.sum_chunk;
-    chunk32 = 2048;
     W.load(cfg, geo, base);
     const RotorParams& P = W.P;
     d.nb = P.nb;
@@ -163,6 +172,7 @@ struct Case {
     const int nt = W.nt;
 
     VLM_CUDA(cudaSetDevice(opt.device));
+    slots32 = partial32_slots();
     VLM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     VLM_CUDA(cudaEventCreate(&ev0));
     VLM_CUDA(cudaEventCreate(&ev1));
@@ -188,8 +198,8 @@ struct Case {
       pl.rowNear = rowNear;
       pl.rowFar = rowFar;
       if (d.NW > 0) {
-        addEval(pl.rhs, false, rowNear, rowFar);
-        addEval(pl.node, true, rowNear, rowFar);
+        addEval(pl.rhs, false, rowNear, rowFar, d.nbC * d.npan);
+        addEval(pl.node, true, rowNear, rowFar, node_target_count(d, rowNear, rowFar));
         maxTargets = std::max(maxTargets, node_target_count(d, rowNear, rowFar));
       }
     }
@@ -292,9 +302,11 @@ struct Case {
     s.rec32 = dalloc<float>((size_t)maxRecords * kRec32, owned);
     s.targets = dalloc<double>((size_t)maxTargets * 3, owned);
     s.outv = dalloc<double>((size_t)maxTargets * 3, owned);
-    s.part = dalloc<double>((size_t)maxTargets * std::max(maxChunks, 1) * 3, owned);
+    s.part = dalloc<double>((size_t)maxPart * 3, owned);
     s.nearCap = opt.precision == VLM_PREC_FP32_NEAR64 ? 256 * maxTargets : 1;
     s.near = dalloc<NearPair>((size_t)s.nearCap, owned);
+    // zero here; every near-field evaluation leaves them zero
+    s.nacc = dalloc<long long>(opt.precision == VLM_PREC_FP32_NEAR64 ? (size_t)maxPart * 3 : 1, owned);
     dGroups = dalloc<Group>(std::max<size_t>(hGroups.size(), 1), owned);
     dChunks = dalloc<Chunk>(std::max<size_t>(hChunks.size(), 1), owned);
     if (!hGroups.empty())
@@ -315,9 +327,10 @@ struct Case {
       launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream);
       VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
       launch_partial32(s.rec32, s.rec64, ch, e.nchunks, s.targets, M, s.part, s.err + 2, nearOn ? s.near : nullptr,
-                       s.nearCap, stream);
+                       s.nearCap, s.nacc, stream);
     }
-    launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, s.outv, stream);
+    if (opt.precision == VLM_PREC_FP64) launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, s.outv, stream);
+    else launch_combine_unordered(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, s.outv, stream);
   }
 
   void evalNodes(int k, bool pred) {
@@ -464,6 +477,7 @@ struct Case {
     lastMs = ms;
     iter += nsteps;
     if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
+    if (err == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
     if (err) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
     if (ctRows)
       for (int k = 0; k < 10 * nsteps; ++k)
@@ -491,7 +505,7 @@ struct Case {
       else {
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
         launch_partial32(s.rec32, s.rec64, ch, pl.node.nchunks, s.targets, M, s.part, s.err + 2,
-                         opt.precision == VLM_PREC_FP32_NEAR64 ? s.near : nullptr, s.nearCap, stream);
+                         opt.precision == VLM_PREC_FP32_NEAR64 ? s.near : nullptr, s.nearCap, s.nacc, stream);
       }
     };
     launch();  // warm
@@ -591,7 +605,8 @@ struct Case {
         g.push_back(q);
       }
     std::vector<Chunk> ch(rec + g.size() + 1);
-    const int nq = build_chunks(g.data(), (int)g.size(), chunkSize(), ch.data(), (int)ch.size());
+    const int nq = chunkTable(g.data(), (int)g.size(), (int)M, ch.data(), (int)ch.size());
+    if (nq < 0) throw std::runtime_error("chunk table overflow");
     std::vector<void*> tmpOwned;
     Group* dg = dalloc<Group>(g.size(), tmpOwned);
     Chunk* dc = dalloc<Chunk>(nq, tmpOwned);
@@ -617,10 +632,16 @@ struct Case {
         launch_pack32(rec64, rec, nearOn ? opt.near_factor : 0.0, rec32, stream);
         const int cap = nearOn ? (int)std::min<int64_t>(64 * M + (1 << 16), 1 << 26) : 1;
         NearPair* np = dalloc<NearPair>(cap, tmpOwned);
+        long long* nacc = dalloc<long long>(nearOn ? (size_t)M * nq * 3 : 1, tmpOwned);
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
-        launch_partial32(rec32, rec64, dc, nq, dP, (int)M, part, s.err + 2, nearOn ? np : nullptr, cap, stream);
+        launch_partial32(rec32, rec64, dc, nq, dP, (int)M, part, s.err + 2, nearOn ? np : nullptr, cap, nacc, stream);
       }
-      launch_combine(part, (int)M, dg, (int)g.size(), 2, dV, stream);
+      if (opt.precision == VLM_PREC_FP64) launch_combine(part, (int)M, dg, (int)g.size(), 2, dV, stream);
+      else {
+        int maxq = 0;
+        for (const Group& q : g) maxq = std::max(maxq, q.chunk_count);
+        launch_combine_unordered(part, (int)M, dg, (int)g.size(), maxq, 2, dV, stream);
+      }
       VLM_CUDA(cudaMemcpyAsync(V, dV, (size_t)M * 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
       VLM_CUDA(cudaStreamSynchronize(stream));
     } catch (...) {
@@ -642,7 +663,8 @@ struct RingScratch {
   Group* group = nullptr;
   int* err = nullptr;
   NearPair* near = nullptr;
-  size_t cap64 = 0, cap32 = 0, capPart = 0, capChunks = 0, capNear = 0;
+  long long* nacc = nullptr;  // zero between calls
+  size_t cap64 = 0, cap32 = 0, capPart = 0, capChunks = 0, capNear = 0, capNacc = 0;
 };
 static RingScratch g_ring[64];
 
@@ -663,13 +685,48 @@ static int ring_chunk(int64_t N, int64_t M, int precision) {
   return (int)((N + q - 1) / q);
 }
 
+// Chunk table of an isolated ring evaluation (one group of N rings): the
+// FP64 summation blocks, or the FP32 kernel's planned chunks.
+static int ring_plan(int64_t N, int64_t M, int precision, Group& g, std::vector<Chunk>& ch) {
+  g = Group{};
+  g.rec_begin = 0;
+  g.rec_count = (int)N;
+  g.kind = 0;
+  if (N <= 0) {
+    ch.assign(1, Chunk{});
+    return 0;
+  }
+  if (precision == VLM_PREC_FP64) {
+    const int C = ring_chunk(N, M, precision);
+    ch.assign((size_t)((N + C - 1) / C), Chunk{});
+    return build_chunks(&g, 1, C, ch.data(), (int)ch.size());
+  }
+  ch.assign((size_t)std::min<int64_t>(N, 1 << 16) + 1, Chunk{});
+  const int nq = plan_chunks32(&g, 1, (int)M, partial32_slots(), ch.data(), (int)ch.size());
+  if (nq < 0) throw std::runtime_error("chunk table overflow");
+  return nq;
+}
+
+static int64_t ring_near_cap(int64_t M) { return std::min<int64_t>(16 * M + (1 << 20), 1 << 27); }
+
 int64_t ring_scratch_bytes(int64_t N, int64_t M, int precision) {
-  const int C = ring_chunk(N, M, precision);
-  const int64_t Q = (N + C - 1) / C;
+  Group g;
+  std::vector<Chunk> ch;
+  const int64_t Q = std::max(1, ring_plan(N, M, precision, g, ch));
   int64_t b = N * kRec64 * 8 + M * Q * 3 * 8 + Q * (int64_t)sizeof(Chunk) + 64;
   if (precision != VLM_PREC_FP64) b += N * kRec32 * 4;
-  if (precision == VLM_PREC_FP32_NEAR64) b += std::min<int64_t>(16 * M + (1 << 20), 1 << 27) * (int64_t)sizeof(NearPair);
+  if (precision == VLM_PREC_FP32_NEAR64) b += ring_near_cap(M) * (int64_t)sizeof(NearPair) + M * Q * 3 * 8;
   return b;
+}
+
+int64_t ring_sum_chunk(int64_t N, int64_t M, int precision) {
+  if (N <= 0) return 0;
+  Group g;
+  std::vector<Chunk> ch;
+  const int nq = ring_plan(N, M, precision, g, ch);
+  int64_t c = 0;
+  for (int i = 0; i < nq; ++i) c = std::max<int64_t>(c, ch[i].rec_count);
+  return c;
 }
 
 void rings_device(const double* corners, const double* rvc, const double* gam, int64_t N, const double* P, int64_t M,
@@ -681,22 +738,22 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   VLM_CUDA(cudaGetDevice(&dev));
   RingScratch& R = g_ring[dev & 63];
   std::lock_guard<std::mutex> lock(R.mu);
-  const int C = N > 0 ? ring_chunk(N, M, precision) : 1;
-  const int Q = N > 0 ? (int)((N + C - 1) / C) : 1;
+  Group g;
+  std::vector<Chunk> ch;
+  const int nq = ring_plan(N, M, precision, g, ch);
+  const int Q = std::max(nq, 1);
   grow((void**)&R.rec64, R.cap64, (size_t)std::max<int64_t>(N, 1) * kRec64 * 8);
   if (precision != VLM_PREC_FP64) grow((void**)&R.rec32, R.cap32, (size_t)std::max<int64_t>(N, 1) * kRec32 * 4);
   grow((void**)&R.part, R.capPart, (size_t)M * Q * 3 * 8);
   grow((void**)&R.chunks, R.capChunks, (size_t)Q * sizeof(Chunk) + sizeof(Group) + 64);
   R.group = reinterpret_cast<Group*>(R.chunks + Q);
   if (!R.err) VLM_CUDA(cudaMalloc(&R.err, 4 * sizeof(int)));
-  const int nearCap = precision == VLM_PREC_FP32_NEAR64 ? (int)std::min<int64_t>(16 * M + (1 << 20), 1 << 27) : 1;
+  const int nearCap = precision == VLM_PREC_FP32_NEAR64 ? (int)ring_near_cap(M) : 1;
   grow((void**)&R.near, R.capNear, (size_t)nearCap * sizeof(NearPair));
-  std::vector<Chunk> ch(Q);
-  Group g{};
-  g.rec_begin = 0;
-  g.rec_count = (int)N;
-  g.kind = 0;
-  const int nq = N > 0 ? build_chunks(&g, 1, C, ch.data(), Q) : 0;
+  if (precision == VLM_PREC_FP32_NEAR64 && (size_t)M * Q * 3 * 8 > R.capNacc) {
+    grow((void**)&R.nacc, R.capNacc, (size_t)M * Q * 3 * 8);
+    VLM_CUDA(cudaMemset(R.nacc, 0, R.capNacc));
+  }
   // the tables are tiny; copy them synchronously with the stream so that the
   // caller's later reuse of the scratch is ordered after this launch
   VLM_CUDA(cudaMemcpyAsync(R.chunks, ch.data(), sizeof(Chunk) * std::max(nq, 1), cudaMemcpyHostToDevice, st));
@@ -709,9 +766,11 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
     } else {
       const bool nearOn = precision == VLM_PREC_FP32_NEAR64;
       launch_pack32(R.rec64, (int)N, nearOn ? 4.0 : 0.0, R.rec32, st);
-      launch_partial32(R.rec32, R.rec64, R.chunks, nq, P, (int)M, R.part, R.err, nearOn ? R.near : nullptr, nearCap, st);
+      launch_partial32(R.rec32, R.rec64, R.chunks, nq, P, (int)M, R.part, R.err, nearOn ? R.near : nullptr, nearCap,
+                       R.nacc, st);
     }
-    launch_combine(R.part, (int)M, R.group, 1, 2, V, st);
+    if (precision == VLM_PREC_FP64) launch_combine(R.part, (int)M, R.group, 1, 2, V, st);
+    else launch_combine_unordered(R.part, (int)M, R.group, 1, nq, 2, V, st);
   } else {
     VLM_CUDA(cudaMemsetAsync(V, 0, (size_t)M * 3 * 8, st));
   }
@@ -722,6 +781,7 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   VLM_CUDA(cudaMemcpyAsync(ctl, R.err, sizeof(ctl), cudaMemcpyDeviceToHost, st));
   VLM_CUDA(cudaStreamSynchronize(st));
   if (ctl[0] == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
+  if (ctl[0] == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
   if (ctl[0]) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
 }
 
@@ -797,7 +857,7 @@ int64_t vlm_biot_savart_rings_scratch_bytes(int64_t N, int64_t M, int precision)
 }
 
 int64_t vlm_biot_savart_rings_sum_chunk(int64_t N, int64_t M, int precision) {
-  return N > 0 ? ring_chunk(N, M, precision) : 0;
+  return ring_sum_chunk(N, M, precision);
 }
 
 int vlm_biot_savart_rings(const double* corners, const double* rvc, const double* gam, int64_t N, const double* P,
@@ -895,7 +955,21 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value) {
   else if (k == "iter") *value = C.iter;
   else if (k == "nbConvect") *value = C.d.nbC;
   else if (k == "wakeTruncateNt") *value = C.W.P.wakeTruncateNt;
-  else {
+  else if (k == "nearPairs" || k == "nodeChunks") {
+    // near-field filament-target pairs of the last FP32 evaluation; chunks
+    // of the next step's wake-node evaluation
+    if (k == "nodeChunks") {
+      *value = C.iter < C.W.nt ? C.plans[C.iter + 1].node.nchunks : 0;
+    } else {
+      int v = 0;
+      if (cudaStreamSynchronize(C.stream) != cudaSuccess ||
+          cudaMemcpy(&v, C.s.err + 3, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        g_err = "cannot read the near-pair count";
+        return VLM_ERR_CUDA;
+      }
+      *value = v;
+    }
+  } else {
     g_err = std::string("unknown integer ") + name;
     return VLM_ERR_INVALID;
   }

@@ -32,10 +32,13 @@ constexpr size_t kOffRec64 = 0;
 constexpr size_t kOffRec32 = kOffRec64 + align256(kMaxRings * kRec64 * sizeof(double));
 constexpr size_t kOffPart = kOffRec32 + align256(kMaxRings * kRec32 * sizeof(float));
 constexpr size_t kOffNear = kOffPart + align256(kMaxPoints * 3 * sizeof(double));
-constexpr size_t kOffTables = kOffNear + align256(kMaxNear * sizeof(NearPair));
+constexpr size_t kOffNacc = kOffNear + align256(kMaxNear * sizeof(NearPair));
+constexpr size_t kOffTables = kOffNacc + align256(kMaxPoints * 3 * sizeof(long long));
 constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words
 
 // One fixed scratch area per device that loads the library, held until exit.
+// It starts zeroed; the near-field accumulators in it are left zero by every
+// call.
 // In host code this name is only a stand-in for the device object: kernels
 // get its device address from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -112,6 +115,7 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   float* rec32 = reinterpret_cast<float*>(base + kOffRec32);
   double* part = reinterpret_cast<double*>(base + kOffPart);
   NearPair* near = reinterpret_cast<NearPair*>(base + kOffNear);
+  long long* nacc = reinterpret_cast<long long*>(base + kOffNacc);
   Chunk* chunks = reinterpret_cast<Chunk*>(base + kOffTables);
   Group* group = reinterpret_cast<Group*>(base + kOffTables + 64);
   int* ctl = reinterpret_cast<int*>(base + kOffTables + 128);
@@ -125,7 +129,7 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
     } else {
       const bool nearOn = precision == VLM_PREC_FP32_NEAR64;
       launch_pack32(rec64, (int)N, nearOn ? 4.0 : 0.0, rec32, st);
-      launch_partial32(rec32, rec64, chunks, 1, P, (int)M, part, ctl, nearOn ? near : nullptr, (int)kMaxNear, st);
+      launch_partial32(rec32, rec64, chunks, 1, P, (int)M, part, ctl, nearOn ? near : nullptr, (int)kMaxNear, nacc, st);
     }
     launch_combine(part, (int)M, group, 1, 2, V, st);
   } else {
@@ -141,6 +145,7 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
   if (flags[0] == 3) return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc: more than 65536 near-field pairs");
+  if (flags[0] == 4) return fail(VLM_ERR_NONFINITE, "vlm_biot_savart_rings_noalloc: near-field velocity outside the fixed-point range");
   if (flags[0]) return fail(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
   return VLM_OK;
 }

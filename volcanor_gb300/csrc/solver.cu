@@ -442,9 +442,12 @@ __device__ __forceinline__ void decode_node(const Dims& d, int rowNear, int rowF
   b = m / per;
   const int l = m % per;
   if (l < rowsN * (d.ns + 1)) {
+    // span station fastest: a warp's consecutive targets are a compact strip
+    // of the wake sheet (a few rows across the span), not a helix turn of one
+    // station, so few source rings come near any of them
     far = 0;
-    j = l / rowsN;
-    i = rowNear - 1 + l % rowsN;
+    j = l % (d.ns + 1);
+    i = rowNear - 1 + l / (d.ns + 1);
   } else {
     far = 1;
     j = 0;
@@ -703,46 +706,66 @@ __device__ __forceinline__ void wing_ring(const Dims& d, const double* fr, int b
   c[3] = ld3(w + 9);
 }
 
-__global__ void k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+// Velocity at collocation point t including the wing's own induced velocity
+// minus its bound vortices (src/classdef.f90 calc_force's velCPTotal): one
+// block per collocation point.  The threads evaluate the four filament
+// velocities of a batch of panels in parallel (one filament each) into shared
+// memory, and thread 0 forms the terms and adds them in the reference's
+// order: the ring term ((f1 + f2) + f3) + f4 is vr_vind's sum, the bound pair
+// f2 + f4 and the trailing-edge f2 are the single-filament calls, all of
+// which evaluate the same filament function on the same corners.
+constexpr int kVcPanels = 32;  // panels per batch (4 filaments each, 128 threads)
+__global__ void __launch_bounds__(128) k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk) {
+  __shared__ double F[kVcPanels * 4 * 3];
+  const int t = blockIdx.x;
   if (t >= d.nbC * d.npan) return;
   const d3 P = ld3(panRec(d, fr, t / d.npan, t % d.npan) + 12);
-  d3 bound = zero3();
+  d3 bound = zero3(), wing = zero3();
   for (int b = 0; b < d.nb; ++b) {
     d3 sb = zero3();
-    for (int j = 0; j < d.ns; ++j)
-      for (int i = 0; i < d.nc; ++i) {
-        const int p = i + d.nc * j;
-        d3 c[4];
-        wing_ring(d, fr, b, p, c);
-        const double* rv = s.wRvc + 4 * ((size_t)b * d.npan + p);
-        const d3 v = fil_vind64(P, c[1], c[2], rv[1]) + fil_vind64(P, c[3], c[0], rv[3]);
-        sb = sb + v * s.wGam[(size_t)b * d.npan + p];
+    ChunkAcc acc(sumChunk);
+    for (int p0 = 0; p0 < d.npan; p0 += kVcPanels) {
+      const int n = min(kVcPanels, d.npan - p0);
+      for (int i = threadIdx.x; i < 4 * n; i += blockDim.x) {
+        const int p = p0 + (i >> 2), k = i & 3;
+        const double* w = panRec(d, fr, b, p);
+        const corner64 ka = make_corner64(P, ld3(w + 3 * k)), kb = make_corner64(P, ld3(w + 3 * ((k + 1) & 3)));
+        st3(F + 3 * i, vf_vind64(ka, kb, s.wRvc[4 * ((size_t)b * d.npan + p) + k]));
       }
-    for (int j = 0; j < d.ns; ++j) {
-      const int p = (d.nc - 1) + d.nc * j;
-      d3 c[4];
-      wing_ring(d, fr, b, p, c);
-      sb = sb - fil_vind64(P, c[1], c[2], s.wRvc[4 * ((size_t)b * d.npan + p) + 1]) * s.wGam[(size_t)b * d.npan + p];
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int i = 0; i < n; ++i) {
+          const int p = p0 + i;
+          const double g = s.wGam[(size_t)b * d.npan + p];
+          const d3 f0 = ld3(F + 12 * i), f1 = ld3(F + 12 * i + 3), f2 = ld3(F + 12 * i + 6), f3 = ld3(F + 12 * i + 9);
+          sb = sb + (f1 + f3) * g;
+          acc.add((((f0 + f1) + f2) + f3) * g);
+        }
+      __syncthreads();
+    }
+    // trailing-edge panels (i = nc - 1) of every section j, in order of j
+    for (int j0 = 0; j0 < d.ns; j0 += 4 * kVcPanels) {
+      const int n = min(4 * kVcPanels, d.ns - j0);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int p = (d.nc - 1) + d.nc * (j0 + i);
+        const double* w = panRec(d, fr, b, p);
+        const corner64 ka = make_corner64(P, ld3(w + 3)), kb = make_corner64(P, ld3(w + 6));
+        st3(F + 3 * i, vf_vind64(ka, kb, s.wRvc[4 * ((size_t)b * d.npan + p) + 1]) * s.wGam[(size_t)b * d.npan + p]);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int i = 0; i < n; ++i) sb = sb - ld3(F + 3 * i);
+      __syncthreads();
     }
     bound = bound + sb;
-  }
-  d3 wing = zero3();
-  for (int b = 0; b < d.nb; ++b) {
-    ChunkAcc acc(sumChunk);
-    for (int j = 0; j < d.ns; ++j)
-      for (int i = 0; i < d.nc; ++i) {
-        const int p = i + d.nc * j;
-        d3 c[4];
-        wing_ring(d, fr, b, p, c);
-        acc.add(vr_vind64(P, c, s.wRvc + 4 * ((size_t)b * d.npan + p)) * s.wGam[(size_t)b * d.npan + p]);
-      }
     wing = wing + acc.result();
   }
-  d3 v = ld3(s.velCP + 3 * (size_t)t);
-  v = v - bound;
-  v = v + wing;
-  st3(s.velCPTotal + 3 * (size_t)t, v);
+  if (threadIdx.x == 0) {
+    d3 v = ld3(s.velCP + 3 * (size_t)t);
+    v = v - bound;
+    v = v + wing;
+    st3(s.velCPTotal + 3 * (size_t)t, v);
+  }
 }
 
 // libMath.f90:293-426 (Doolittle inverse of lsq2's 3x3 normal matrix; its
@@ -1101,7 +1124,7 @@ void launch_solve(const Dims& d, const DevState& s, const double* frame, bool wi
 }
 void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st) {
   count_launch();
-  k_velcp_total<<<nblk(d.nbC * d.npan, 64), 64, 0, st>>>(d, s, frame, sumChunk);
+  k_velcp_total<<<d.nbC * d.npan, 128, 0, st>>>(d, s, frame, sumChunk);
   count_launch();
   k_loads<<<1, 256, 0, st>>>(d, s, frame, iter);
 }

@@ -34,21 +34,28 @@ constexpr int REC_SKIP = 2;
 //   [24..27] w_k |e_k|^2
 //   [28..31] (rvc_k |e_k|)^4, floored at 1e-36 so the kernel needs no clamp
 //   [32..35] near-field threshold on |r1 x r2|^2: (near_factor rvc_k |e_k|)^2, -1 if off
-//   [36..39] w_k for active edges, 0 for inactive / skipped
-//   [40..43] near-field slack along the filament: near_factor rvc_k |e_k|
+//   [36..39] lower near-field bound on (w_k e_k).r1
+//   [40..43] upper near-field bound on (w_k e_k).r1
 //   [44]     squared radius about corner 0 outside which no filament of the
 //            record can be near (-1 when the near-field path is off)
 //   [45..47] unused
 // A pair is near when the target lies within near_factor core radii of the
-// filament SEGMENT: |r1 x r2|^2 < [32+k] and -[40+k] < e.r1 < |e|^2 + [40+k]
-// (e recomputed from the corners).
+// filament SEGMENT: |r1 x r2|^2 < [32+k] and -s < e.r1 < |e|^2 + s with
+// s = near_factor rvc_k |e_k|; the second test is stored multiplied by w_k,
+// so [36+k] < (w_k e_k).r1 < [40+k] (bounds swapped when w_k < 0).
 constexpr int kRec32 = 48;
 
-// One near-field pair found by the FP32 kernel: target m, chunk q (partial
-// sum to correct), global record index, filament k.
+// One near-field filament-target pair found by the FP32 kernel: target m,
+// chunk q (partial sum to correct), global record index, filament k.
 struct NearPair {
   int32_t m, q, rec, k;
 };
+
+// Fixed-point scale of the near-field accumulators: FP64 near-field
+// velocities are added as integers (v * 2^44, |v| < 2^18) so that their sum
+// does not depend on the order in which the pairs are processed.
+constexpr double kNearScale = 17592186044416.0;  // 2^44
+constexpr double kNearMax = 262144.0;            // 2^18
 
 struct Group {
   int32_t rec_begin;    // first record (index into the record array)
@@ -69,17 +76,32 @@ struct Chunk {
 // Returns the number of chunks.
 int build_chunks(Group* groups, int ngroups, int chunk_size, Chunk* chunks, int cap);
 
+// Chunk plan for the FP32 kernel (whose summation order is free): picks the
+// number of chunks per group that minimises the modelled run time of a grid
+// of ceil(M / targets_per_block) x chunks blocks on `slots` resident block
+// slots, with chunks of balanced size inside each group.  Fills the groups'
+// chunk_begin/count like build_chunks; returns the number of chunks, or -1
+// if cap is too small.
+int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap);
+// Resident block slots of the FP32 kernel on the current device
+// (SMs x resident blocks per SM).
+int partial32_slots();
+// Targets one FP32 kernel block covers.
+constexpr int kTargetsPerBlock32 = 512;
+
 // FP64 reference-arithmetic partial sums: part[(q * M + m) * 3 + k].
 void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,
                       cudaStream_t s);
 // FP32 pairs with FP64 accumulation.  When near is non-null, pairs inside the
 // records' near-field thresholds are left out of the FP32 sums, listed in
-// near (capacity near_cap, count in ctl[1]) and then evaluated in FP64 from
-// rec64 and added to their partial sums by a second kernel.  ctl[0] receives
-// a nonzero code if a bounded wait on the tile pipeline expired or the near
-// list overflowed.  ctl must be zeroed before the call.
+// near (capacity near_cap, count in ctl[1]), evaluated in FP64 from rec64 by
+// a second kernel into the fixed-point accumulators nacc (M x nchunks x 3,
+// zero on entry and left zero on return) and added to their partial sums by
+// a third.  ctl[0] receives a nonzero code if a bounded wait on the tile
+// pipeline expired (1, 2), the near list overflowed (3) or a near-field
+// velocity left the fixed-point range (4).  ctl must be zeroed before the call.
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
-                      int M, double* part, int* ctl, NearPair* near, int near_cap, cudaStream_t s);
+                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s);
 // Converts FP64 records to FP32 records (near_factor <= 0 disables near-field).
 void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s);
 
@@ -90,6 +112,13 @@ void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec
 //   mode 2: out[m] = wing + wake            (point query)
 void launch_combine(const double* part, int M, const Group* groups, int ngroups, int mode, double* out,
                     cudaStream_t s);
+
+// As launch_combine, but each group's chunk partials are added as a fixed
+// tree (up to a warp per target, sized by max_chunks, the largest chunk count
+// of a group) instead of in chunk order: for the FP32 paths, whose chunking
+// is itself free.
+void launch_combine_unordered(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
+                              double* out, cudaStream_t s);
 
 // Isolated rings (vlm_biot_savart_rings): AoS corners (N x 4 x 3), rvc (N x 4), gam (N) -> FP64 records.
 void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,

@@ -78,6 +78,7 @@ struct DevState {
   double *rec64, *targets, *part, *outv;
   float* rec32;
   NearPair* near;
+  long long* nacc;  // fixed-point near-field accumulators, zero between evaluations
   int nearCap;
   int* err;  // [0] LU/inverse check, [2] FP32 pipeline or near-list error, [3] near-pair count
 };
