@@ -41,6 +41,43 @@ WORKLOAD = ("2-blade hover rotor R=1m c=0.08m theta0=8deg Omega=100rad/s 1x24 ri
 FULL_WAKE_STEP = 432
 RING_FLOP = 176.0  # flop per ring-target pair (4 filaments x 44)
 FIL_FLOP = 44.0
+PROFILES = Path(__file__).resolve().parent / "profiles"
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+    a kernel, from the committed ncu summary profiles/<name>.txt (its line
+    'traffic_bytes_per_launch: N'); None if there is none."""
+    f = PROFILES / f"{name}.txt"
+    try:
+        for line in f.read_text().splitlines():
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1].strip()))
+    except OSError:
+        return None
+    return None
+
+
+class nvtx_range:
+    """NVTX push/pop range (lets an ncu capture select the launches inside)."""
+
+    def __init__(self, name: str):
+        self.name = name
+        self.ok = False
+
+    def __enter__(self):
+        try:
+            import torch
+            torch.cuda.nvtx.range_push(self.name)
+            self.ok = True
+        except Exception:
+            pass
+        return self
+
+    def __exit__(self, *a):
+        if self.ok:
+            import torch
+            torch.cuda.nvtx.range_pop()
 
 
 def env_int(k, d):
@@ -256,7 +293,8 @@ def run_ours(args):
     except Exception:
         pass
     # roofline of the dominant kernel on the live steady-state state
-    ms_l, rp, fp = case.profile_eval(20)
+    with nvtx_range("profile_eval"):
+        ms_l, rp, fp = case.profile_eval(20)
     near_pairs = case.geti("nearPairs") if prec == lib.PREC_FP32_NEAR64 else 0
     node_chunks = case.geti("nodeChunks")
     flops = RING_FLOP * rp + FIL_FLOP * fp
@@ -286,7 +324,11 @@ def run_ours(args):
                 "h2d_bytes_per_step": 8 * frame_doubles if frame_doubles else None, "d2h_bytes_per_step": 80},
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp32-cuda-core", "achieved": round(achieved, 3), "peak": round(fp32_peak, 2),
-                     "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4), "traffic": None,
+                     "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4),
+                     "traffic": profiled_traffic(f"k_partial32_hover2_steady_{args.precision}"),
+                     "traffic_note": "DRAM bytes per launch from the ncu capture summarised in "
+                                     f"profiles/k_partial32_hover2_steady_{args.precision}.txt; the working set "
+                                     "(sources, targets, partials) stays in L2",
                      "kernel": "k_partial32" if prec != lib.PREC_FP64 else "k_partial64",
                      "ms_per_launch": round(ms_l, 4), "ring_pairs_per_launch": rp, "fil_pairs_per_launch": fp,
                      "near_pairs_per_launch": near_pairs, "chunks": node_chunks,
@@ -318,33 +360,93 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def helix_wake(nb: int, ns: int, nw: int, radius: float, rootcut: float, omega: float, dt: float,
+               core: float, seed: int = 0):
+    """Near-wake rings of a prescribed helical hover wake with the case's node
+    counts (nb blades x nw rows x ns rings): node (i, j) of blade b at radius
+    r_j, azimuth 2 pi b / nb - omega dt i, descending at the momentum-theory
+    induced velocity.  The FP64 filament kernel's cost does not depend on the
+    positions, so this stands in for the solver's wake in CPU timing."""
+    rng = np.random.default_rng(seed)
+    r = np.linspace(rootcut * radius, radius, ns + 1)
+    vi = omega * radius * np.sqrt(0.0035 / 2.0)
+    corners = []
+    for b in range(nb):
+        i = np.arange(nw + 1)[:, None]
+        psi = 2.0 * np.pi * b / nb - omega * dt * i
+        x, y = r[None, :] * np.cos(psi), r[None, :] * np.sin(psi)
+        z = np.broadcast_to(-vi * dt * i, x.shape)
+        nodes = np.stack([x, y, z], -1)  # [row][station]
+        c = np.stack([nodes[:-1, :-1], nodes[1:, :-1], nodes[1:, 1:], nodes[:-1, 1:]], 2)  # [row][ring][4][3]
+        corners.append(c.reshape(-1, 4, 3))
+    corners = np.concatenate(corners)
+    rvc = np.full((corners.shape[0], 4), core)
+    gam = rng.normal(0.0, 0.05, corners.shape[0])
+    nodes = corners[:, 1]
+    return corners, rvc, gam, nodes
+
+
+def oracle_pairs_per_step(sim):
+    """pairs_per_step from the oracle's case dimensions."""
+    g = sim.geti
+    nb, nc, ns, NW, NF, nbc = g("nb"), g("nc"), g("ns"), g("nNwake"), g("nFwake"), g("nbConvect")
+    m_nodes = nbc * (NW * (ns + 1) + NF)
+    src_wake = nb * NW * ns + nb * (ns + NF) / 4.0
+    src_all = nb * nc * ns + src_wake
+    return 2.0 * m_nodes * src_all + nbc * nc * ns * src_wake
+
+
 def run_reference(args):
-    """Reference arm: the reference algorithm (C++ restatement; the Fortran
-    reference has no compiler on this image) on the host cores, each "step" a
-    bounded sample of the steady-state workload scaled to timesteps/s."""
+    """Reference arm: the reference algorithm on the host cores, no GPU.  The
+    reference is Fortran and no Fortran compiler exists here, so this times
+    the oracle (the C++ FP64 restatement, OpenMP over targets like the
+    reference): each "step" is a bounded sample -- sampled wake-node targets x
+    every near-wake ring of a steady-state-sized helical wake -- converted to
+    timesteps/s by the ring pairs of one steady-state step of the case."""
     rank = env_int("RANK", 0)
     if rank != 0:
         return
+    import tempfile
     from oracle import oracle as O
-    from volcanor_gb300 import lib
     K, W = args.steps, args.warmup
     c = C.rotor_2blade_hover(nt=1440)
-    case = lib.Case(c.config, c.geom, precision=lib.PREC_FP32_NEAR64)
-    case.start()
-    case.step(FULL_WAKE_STEP + 1, with_ct=False)
-    eq = pairs_per_step(case)
+    with tempfile.TemporaryDirectory() as d:
+        c.write(d)
+        sim = O.Sim.from_case_dir(d)
+    eq = oracle_pairs_per_step(sim)
+    nb, ns, NW = sim.geti("nb"), sim.geti("ns"), sim.geti("nNwake")
+    corners, rvc, gam, nodes = helix_wake(nb, ns, NW, 1.0, 0.2, 100.0, 5.0 * np.pi / 180.0 / 100.0, 0.004)
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    rng = np.random.default_rng(0)
+    per_step = args.cpu_seconds / max(1, W + K)
+    # size the sample once: doubling target counts until one call takes a step's share
+    m = 64
+    while True:
+        P = nodes[rng.choice(len(nodes), size=min(m, len(nodes)), replace=False)]
+        t0 = time.perf_counter()
+        O.vind_rings(corners, rvc, gam, P)
+        t = time.perf_counter() - t0
+        if t > per_step / 2 or m >= 4096:
+            break
+        m *= 2
     rates = []
-    desc = ""
     for i in range(W + K):
-        rate, threads, desc = cpu_sample(case, seconds=args.cpu_seconds / max(1, (W + K) // 2))
+        P = nodes[rng.choice(len(nodes), size=P.shape[0], replace=False)]
+        t0 = time.perf_counter()
+        O.vind_rings(corners, rvc, gam, P)
+        t = time.perf_counter() - t0
         if i >= W:
-            rates.append(rate)
+            rates.append(P.shape[0] * corners.shape[0] / t)
     val = float(np.mean(rates)) / eq
+    desc = (f"{P.shape[0]} wake-node targets x {corners.shape[0]} near-wake rings of a helical wake with the case's "
+            f"node counts, {K} timed samples after {W} warm-up; oracle (C++ FP64 restatement, not the Fortran "
+            f"reference: no Fortran compiler); converted at {eq:.4g} ring pairs per step")
     out = {"impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "timesteps/s", "n_gpus": 1,
-           "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic", "config": {"workload": WORKLOAD},
-           "cpu_baseline": {"value": round(val, 4), "unit": "timesteps/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": desc + f"; converted at {eq:.4g} ring pairs per step"},
+           "steps": K, "warmup": W, "ms_per_step": round(1e3 / val, 3), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD},
+           "cpu_baseline": {"value": round(val, 4), "unit": "timesteps/s", "cores": threads, "kind": "port",
+                            "sample": desc},
            "e2e": {"value": round(val, 4), "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

@@ -5,7 +5,7 @@
  * Boundary: the reference has no plugin layer; its hot path is the set of
  * type-bound procedures src/main.f90 calls between OpenMP regions.  Each entry
  * below names the reference call site it replaces.  A Fortran caller binds
- * these through ISO_C_BINDING; Python binds them through
+ * these through ISO_C_BINDING interface blocks; Python binds them through
  * ctypes (volcanor_gb300/lib.py).
  *
  * Conventions
@@ -51,6 +51,12 @@ typedef struct vlm_options {
   double near_factor;  /* near-field radius in core radii for VLM_PREC_FP32_NEAR64 (default 4) */
   int device;          /* CUDA device ordinal (default 0) */
   int use_graph;       /* capture multi-step runs in a CUDA graph (default 1) */
+  int solve_mode;      /* circulation solve: 0 = FP64 explicit inverse (the reference's inv2 +
+                          matmulAX), 1 = FP32 LU with partial pivoting + FP64 iterative
+                          refinement (3 passes; lu_residual reports max|b-Ax|/max|b|),
+                          -1 = 1 for the FP32 precisions, 0 for FP64 (default) */
+  int nbody_slots;     /* resident block slots the FP32 chunk planner plans for (0 = the whole
+                          device; a batch gives each of its cases a share) */
 } vlm_options;
 
 /* ---- library ------------------------------------------------------------ */
@@ -92,7 +98,7 @@ int64_t vlm_biot_savart_rings_sum_chunk(int64_t N, int64_t M, int precision);
  * device memory when they call it (a host solver that reserves its device
  * memory once at start-up, a process under a hard device-memory cap, or a
  * caller that must not trigger the device-wide synchronisation an allocation
- * may cause): its scratch is one fixed 8 MiB array compiled into the library,
+ * may cause): its scratch is one fixed 9.25 MiB array compiled into the library,
  * held on every device that loads the library until the process exits.
  * Limits: N <= 16384 rings, M <= 65536 points, at most 65536 near-field
  * pairs (VLM_PREC_FP32_NEAR64); larger sizes return VLM_ERR_INVALID with a
@@ -129,8 +135,21 @@ int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows);
  * last FP32 evaluation) and nodeChunks (chunks of the next step's wake-node
  * evaluation) describe this library's kernels. */
 int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
-/* Copy a named array (see the design doc for the list and layouts) into out.
- * Returns the element count, or -1 for an unknown name. */
+/* Copy a named array into out (at most cap doubles); blade is 1-based where
+ * the array is per blade.  Returns the element count, or -1 for an unknown
+ * name.  Names and layouts (Fortran column-major, xyz fastest):
+ *   dt, nonDimDenom, lu_residual    scalars (lu_residual: last refined solve, 0 without refinement)
+ *   ct_hist                         (10, iter+1) CT rows so far
+ *   AIC, AIC_inv                    (n, n); gamVec (n)
+ *   gam (blade)                     (nc, ns) wing circulation
+ *   CP, nCap, velCP, velCPTotal     (3, nc, ns) per blade
+ *   vr (blade)                      (3, 4, nc, ns) wing ring corners
+ *   waN (blade)                     (3, 4, nNwake, ns) near-wake ring corners
+ *   waN_gam, waN_rvc (blade)        (nNwake, ns), (4, nNwake, ns)
+ *   waF (blade)                     (3, 2, nFwake) far-wake filament nodes
+ *   waF_gam, waF_rvc (blade)        (nFwake)
+ *   velN, velF (blade)              (3, nNwake, ns+1), (3, nFwake) node velocities
+ *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section */
 int64_t vlm_case_get(vlm_case* c, const char* name, int blade, double* out, int64_t cap);
 /* Induced velocity of the current wing + wake at M points (probes / gridgen:
  * src/libPostprocess.f90:333-361, src/gridgen.f90:115-140). */
@@ -143,6 +162,100 @@ int vlm_case_last_step_ms(vlm_case* c, double* ms);
  * its mean launch time and the ring-target and filament-target pair counts of
  * one launch (roofline accounting). */
 int vlm_case_profile_eval(vlm_case* c, int reps, double* ms_per_launch, double* ring_pairs, double* fil_pairs);
+
+/* ---- many independent cases in one launch per step -------------------------
+ * The reference has no batch mode (nr > 1 couples rotors aerodynamically);
+ * this runs ncases independent cases (each its own case files, precision
+ * and options from opt) on one GPU.  A batch step enqueues every case's step
+ * on the case's own stream, so their kernels run concurrently; once every
+ * case is in its steady state (same near/far rows step after step), one
+ * batch step is captured as one CUDA graph and replayed with one launch per
+ * step.  Each case's FP32 chunk plan is made for its share of the device
+ * (opt->nbody_slots, default all slots / ncases). */
+typedef struct vlm_batch vlm_batch;
+int vlm_batch_create(int ncases, const char* const* configs, const char* const* geoms, const char* const* base_dirs,
+                     const vlm_options* opt, vlm_batch** out);
+int vlm_batch_destroy(vlm_batch* b);
+/* Borrowed handle of case i (getters; do not destroy or step it alone). */
+int vlm_batch_case(vlm_batch* b, int i, vlm_case** out);
+int vlm_batch_start(vlm_batch* b);
+/* Every case advances nsteps; ct_rows (if not NULL) receives ncases x nsteps x 10. */
+int vlm_batch_step(vlm_batch* b, int nsteps, double* ct_rows);
+/* Device time of the last vlm_batch_step call (all cases), milliseconds. */
+int vlm_batch_last_step_ms(vlm_batch* b, double* ms);
+
+/* ---- learned far-wake surrogate of a case -----------------------------------
+ * No counterpart in the reference (it sums the far wake directly).  With the
+ * FP32 precisions, the OLD far wake -- the rolled-up tip filaments behind the
+ * near-wake sheet past the young_far youngest of each blade -- is the
+ * surrogate's domain.  Once it holds min_far filaments per blade, the case
+ * collects training pairs for collect_steps steps -- features of the
+ * collocation points and every sample_stride-th near-wake node: position
+ * about the hub over the rotor radius, rotor-azimuth harmonics, old-wake fill
+ * -> their direct old-far-wake velocity -- and trains an MLP (layers linear
+ * layers of width hidden, tanh) for train_iters Adam steps on the GPU.  From
+ * then on the network replaces the old-far-wake sum at the collocation
+ * points and near-wake nodes (far-wake nodes, next to the old wake along the
+ * tip vortex, keep the direct sum).  Before every step an audit compares it
+ * with the direct FP64 old-far-wake sum at the collocation points and
+ * audit_samples near-wake nodes; when the relative rms error exceeds
+ * audit_tol that step sums the old far wake directly and data collection and
+ * training start again. */
+#define VLM_SURR_OFF -1
+#define VLM_SURR_WAIT 0
+#define VLM_SURR_COLLECT 1
+#define VLM_SURR_ACTIVE 2
+typedef struct vlm_surrogate_options {
+  int enable;          /* default 1 */
+  int young_far;       /* youngest far-wake filaments per blade kept in the direct sum (216) */
+  int min_far;         /* old far-wake filaments per blade before collecting (72) */
+  int collect_steps;   /* steps of training data (72) */
+  int sample_stride;   /* every k-th near-wake node is a training sample (4) */
+  int train_iters;     /* Adam steps per training (3000) */
+  int batch;           /* samples per Adam step (1024) */
+  float lr;            /* learning rate (1e-3; the last third at a fifth) */
+  int audit_samples;   /* near-wake nodes audited per step (256) */
+  double audit_tol;    /* relative rms error of the old-far-wake velocity that reverts (0.1) */
+  int hidden;          /* width (128) */
+  int layers;          /* linear layers (4) */
+  uint64_t seed;       /* weights and shuffles (1) */
+} vlm_surrogate_options;
+typedef struct vlm_surrogate_stats {
+  int phase;           /* VLM_SURR_* */
+  int trainings;
+  int audits;
+  int reverts;
+  int active_steps;    /* steps that used the network */
+  int64_t samples;     /* training pairs of the current data set */
+  double last_audit_err, max_audit_err;
+  float last_loss;     /* training loss (targets in units of their rms) */
+} vlm_surrogate_stats;
+void vlm_default_surrogate_options(vlm_surrogate_options* o);
+/* Before vlm_case_start. */
+int vlm_case_set_surrogate(vlm_case* c, const vlm_surrogate_options* o);
+int vlm_case_surrogate_stats(vlm_case* c, vlm_surrogate_stats* out);
+
+/* ---- multilayer perceptron of the learned far-wake surrogate ---------------
+ * No counterpart in the reference (its far wake is always summed directly).
+ * An FP32 MLP with tanh hidden layers and a linear output layer; sizes[0]
+ * inputs, sizes[nsizes-1] outputs, row-major W_l (out x in) then b_l per
+ * layer in the parameter vector; MSE loss over all outputs of a batch; Adam.
+ * Forward, backward and update run as this library's CUDA kernels; every
+ * reduction has a fixed order, so results are reproducible.  Buffers are
+ * host memory, row major (n x in, n x out). */
+typedef struct vlm_mlp vlm_mlp;
+int vlm_mlp_create(const int* sizes, int nsizes, uint64_t seed, vlm_mlp** out);
+int vlm_mlp_destroy(vlm_mlp* m);
+int64_t vlm_mlp_param_count(const vlm_mlp* m);
+int vlm_mlp_get_params(vlm_mlp* m, float* out);
+int vlm_mlp_set_params(vlm_mlp* m, const float* in);
+int vlm_mlp_forward(vlm_mlp* m, const float* X, int64_t n, float* Y);
+/* Gradient of the batch MSE with respect to every parameter, and the loss. */
+int vlm_mlp_gradient(vlm_mlp* m, const float* X, const float* T, int64_t n, float* grad, float* loss);
+/* iters Adam steps (learning rate lr) over consecutive batches of the
+ * n samples (shuffle them beforehand); final_loss = loss of the last batch. */
+int vlm_mlp_train(vlm_mlp* m, const float* X, const float* T, int64_t n, int batch, int iters, float lr,
+                  float* final_loss);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,7 @@ def test_version_and_defaults_without_gpu():
     assert b"sm_103a" in L.vlm_version()
     o = lib.options()
     assert o.precision == lib.PREC_FP64 and o.sum_chunk == 256 and o.near_factor == 4.0
+    assert o.solve_mode == -1
 
 
 def test_error_paths_without_gpu():

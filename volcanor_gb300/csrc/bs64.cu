@@ -153,6 +153,7 @@ __global__ void k_rings_to_rec64(const double* __restrict__ corners, const doubl
 
 static std::atomic<long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(); }
 
 int build_chunks(Group* groups, int ngroups, int chunk_size, Chunk* chunks, int cap) {

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/vlm.h"
+#include "mlp.h"
 #include "vlm_bs.h"
 #include "vlm_solver.h"
 #include "wing.h"
@@ -76,6 +77,8 @@ struct Case {
   int iter = 0;
   bool started = false;
   int chunk64 = 0;
+  int surrYoung = 0;  // youngest far-wake filaments per blade the surrogate leaves to the direct sum
+  bool refine = false;  // FP32 LU + FP64 iterative refinement instead of the FP64 inverse
   int slots32 = 0;  // resident FP32-kernel blocks on the device (chunk planner input)
   double lastMs = 0;
   int maxTargets = 0, maxRecords = 0, maxChunks = 0;
@@ -84,6 +87,11 @@ struct Case {
   ~Case() {
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : owned) cudaFree(p);
+    for (void* p : scratchOwned) cudaFree(p);
+    for (void* p : surrOwned) cudaFree(p);
+    surr.net.destroy();
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (hIter) cudaFreeHost(hIter);
     if (hFrames) cudaFreeHost(hFrames);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -98,9 +106,13 @@ struct Case {
   }
 
   // groups of one evaluation: wing sums (kind 0) for every blade when
-  // withWing, then wake sums (kind 1) for every blade
-  void addEval(EvalPlan& e, bool withWing, int rowNear, int rowFar, int M) {
+  // withWing, then wake sums (kind 1) for every blade.  farMode 0: the whole
+  // wake; 1: without the old far-wake filaments (all far-wake filaments but
+  // the surrYoung youngest of each blade); 2: the old far-wake filaments alone.
+  // force64: FP64 summation blocks whatever the case's precision.
+  void addEval(EvalPlan& e, bool withWing, int rowNear, int rowFar, int M, int farMode = 0, bool force64 = false) {
     const int NW = d.NW, NF = d.NF, ns = d.ns;
+    e = EvalPlan();
     e.goff = (int)hGroups.size();
     int rec = 0;
     if (withWing)
@@ -118,10 +130,13 @@ struct Case {
       const int nNear = (NW - (rowNear - 1)) * ns;
       const int hs = rowFar <= NF ? ns : 0;
       const int nFar = rowFar <= NF ? NF - rowFar + 1 : 0;
+      const int nYoung = std::min(nFar, surrYoung);
       g.rec_begin = rec;
-      g.rec_count = nNear + hs + nFar;
+      g.rec_count = farMode == 0 ? nNear + hs + nFar : (farMode == 1 ? nNear + hs + nYoung : nFar - nYoung);
       g.kind = 1;
       g.blade = b;
+      g.pad[0] = farMode == 2 ? 1 : 0;
+      g.pad[1] = farMode == 2 ? nYoung : 0;
       rec += g.rec_count;
       hGroups.push_back(g);
     }
@@ -129,20 +144,24 @@ struct Case {
     e.nrec = rec;
     e.coff = (int)hChunks.size();
     std::vector<Chunk> tmp(rec + e.ngroups + 1);
-    const int nq = chunkTable(hGroups.data() + e.goff, e.ngroups, M, tmp.data(), (int)tmp.size());
+    const int nq = force64 ? build_chunks(hGroups.data() + e.goff, e.ngroups, chunk64, tmp.data(), (int)tmp.size())
+                           : chunkTable(hGroups.data() + e.goff, e.ngroups, M, tmp.data(), (int)tmp.size());
     if (nq < 0) throw std::runtime_error("chunk table overflow");
     hChunks.insert(hChunks.end(), tmp.begin(), tmp.begin() + nq);
     e.nchunks = nq;
     for (int g = e.goff; g < e.goff + e.ngroups; ++g) e.maxq = std::max(e.maxq, hGroups[g].chunk_count);
     maxRecords = std::max(maxRecords, rec);
     maxChunks = std::max(maxChunks, nq);
-    maxPart = std::max(maxPart, (int64_t)nq * M);
+    maxPart = std::max(maxPart, (int64_t)std::max(nq, 1) * M);
+    maxTargets = std::max(maxTargets, M);
   }
 
   void create(const std::string& cfg, const std::string& geo, const std::string& base, const vlm_options* o) {
     vlm_default_options(&opt);
     if (o) opt = *o;
     if (opt.precision < 0 || opt.precision > 2) throw StatusError(VLM_ERR_INVALID, "precision must be 0, 1 or 2");
+    if (opt.solve_mode < -1 || opt.solve_mode > 1) throw StatusError(VLM_ERR_INVALID, "solve_mode must be -1, 0 or 1");
+    refine = opt.solve_mode == 1 || (opt.solve_mode == -1 && opt.precision != VLM_PREC_FP64);
     chunk64 = opt.sum_chunk;
     W.load(cfg, geo, base);
     const RotorParams& P = W.P;
@@ -172,7 +191,7 @@ struct Case {
     const int nt = W.nt;
 
     VLM_CUDA(cudaSetDevice(opt.device));
-    slots32 = partial32_slots();
+    slots32 = opt.nbody_slots > 0 ? opt.nbody_slots : partial32_slots();
     VLM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     VLM_CUDA(cudaEventCreate(&ev0));
     VLM_CUDA(cudaEventCreate(&ev1));
@@ -280,6 +299,17 @@ struct Case {
     s.rotorLift = dalloc<double>(3, owned);
     s.ctHist = dalloc<double>((size_t)(nt + 1) * 10, owned);
     s.err = dalloc<int>(4, owned);
+    s.devIter = dalloc<int>(1, owned);
+    s.curFrame = dalloc<double>(d.fl.size, owned);
+    VLM_CUDA(cudaMallocHost(&hIter, sizeof(int)));
+    if (refine) {
+      s.LU32 = dalloc<float>((size_t)d.n * d.n, owned);
+      s.AICinv32 = dalloc<float>((size_t)d.n * d.n, owned);
+      s.piv32 = dalloc<int>(d.n, owned);
+      s.refX = dalloc<double>(d.n, owned);
+      s.refR = dalloc<double>(d.n, owned);
+      s.luRes = dalloc<double>(1, owned);
+    }
     // initial wake cores (classdef.f90:3864-3891)
     if (NW > 0) {
       std::vector<double> nr(nring * 4), fr(nfar, P.streamwiseCoreVec[ns]);
@@ -296,19 +326,26 @@ struct Case {
       VLM_CUDA(cudaMemcpy(s.fRvc, fr.data(), fr.size() * sizeof(double), cudaMemcpyHostToDevice));
       VLM_CUDA(cudaMemcpy(s.fRvc0, fr.data(), fr.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    // N-body scratch
     maxRecords = std::max(maxRecords, d.n);
-    s.rec64 = dalloc<double>((size_t)maxRecords * kRec64, owned);
-    s.rec32 = dalloc<float>((size_t)maxRecords * kRec32, owned);
-    s.targets = dalloc<double>((size_t)maxTargets * 3, owned);
-    s.outv = dalloc<double>((size_t)maxTargets * 3, owned);
-    s.part = dalloc<double>((size_t)maxPart * 3, owned);
+    allocScratch();
+  }
+
+  // N-body scratch and plan tables (again after the surrogate adds plans)
+  std::vector<void*> scratchOwned;
+  void allocScratch() {
+    for (void* p : scratchOwned) cudaFree(p);
+    scratchOwned.clear();
+    s.rec64 = dalloc<double>((size_t)maxRecords * kRec64, scratchOwned);
+    s.rec32 = dalloc<float>((size_t)maxRecords * kRec32, scratchOwned);
+    s.targets = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
+    s.outv = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
+    s.part = dalloc<double>((size_t)maxPart * 3, scratchOwned);
     s.nearCap = opt.precision == VLM_PREC_FP32_NEAR64 ? 256 * maxTargets : 1;
-    s.near = dalloc<NearPair>((size_t)s.nearCap, owned);
+    s.near = dalloc<NearPair>((size_t)s.nearCap, scratchOwned);
     // zero here; every near-field evaluation leaves them zero
-    s.nacc = dalloc<long long>(opt.precision == VLM_PREC_FP32_NEAR64 ? (size_t)maxPart * 3 : 1, owned);
-    dGroups = dalloc<Group>(std::max<size_t>(hGroups.size(), 1), owned);
-    dChunks = dalloc<Chunk>(std::max<size_t>(hChunks.size(), 1), owned);
+    s.nacc = dalloc<long long>(opt.precision == VLM_PREC_FP32_NEAR64 ? (size_t)maxPart * 3 : 1, scratchOwned);
+    dGroups = dalloc<Group>(std::max<size_t>(hGroups.size(), 1), scratchOwned);
+    dChunks = dalloc<Chunk>(std::max<size_t>(hChunks.size(), 1), scratchOwned);
     if (!hGroups.empty())
       VLM_CUDA(cudaMemcpy(dGroups, hGroups.data(), hGroups.size() * sizeof(Group), cudaMemcpyHostToDevice));
     if (!hChunks.empty())
@@ -316,32 +353,332 @@ struct Case {
   }
 
   const double* frame(int k) const { return s.frames + (size_t)k * d.fl.size; }
+  // the frame a step's kernels read: while a step is captured for replay, the
+  // device-side current frame that launch_step_begin fills
+  const double* stepFrame(int k) const { return replaying ? s.curFrame : frame(k); }
 
-  // one Biot-Savart evaluation of plan e into s.outv (targets already in s.targets)
-  void evaluate(const EvalPlan& e, int M, int mode) {
+  // ---- CUDA-graph replay of steady-state steps ------------------------------
+  // A step whose plan (near/far rows, chunk tables) and host-side branches
+  // equal its predecessor's is captured once and replayed: the graph starts
+  // with launch_step_begin (device step counter + 1, current frame copied in)
+  // and its loads write the CT row of the device counter.
+  bool replaying = false;
+  cudaGraphExec_t gexec = nullptr;
+  int graphRN = -1, graphRF = -1;
+  long graphKernels = 0;
+  int* hIter = nullptr;  // pinned source of the device step counter
+  bool iterSynced = false;
+
+  bool steadyStep(int k) const {
+    if (!opt.use_graph || surr.on || k <= 3 || k <= W.sw.initWakeVelNt || W.sw.rotorForcePlot > 1) return false;
+    return plans[k].rowNear == plans[k - 1].rowNear && plans[k].rowFar == plans[k - 1].rowFar;
+  }
+
+  void captureStep(int k) {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    cudaGraph_t g = nullptr;
+    const long l0 = launch_count();
+    VLM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    replaying = true;
+    try {
+      launch_step_begin(d, s, stream);
+      enqueueStep(k);
+    } catch (...) {
+      replaying = false;
+      cudaStreamEndCapture(stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    replaying = false;
+    VLM_CUDA(cudaStreamEndCapture(stream, &g));
+    const cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+    cudaGraphDestroy(g);
+    VLM_CUDA(e);
+    graphKernels = launch_count() - l0;
+    count_launches(-graphKernels);  // counted when replayed
+    graphRN = plans[k].rowNear;
+    graphRF = plans[k].rowFar;
+  }
+
+  void replayStep(int k) {
+    if (!gexec || graphRN != plans[k].rowNear || graphRF != plans[k].rowFar) captureStep(k);
+    if (!iterSynced) {
+      *hIter = k - 1;
+      VLM_CUDA(cudaMemcpyAsync(s.devIter, hIter, sizeof(int), cudaMemcpyHostToDevice, stream));
+      iterSynced = true;
+    }
+    VLM_CUDA(cudaGraphLaunch(gexec, stream));
+    count_launches(graphKernels);
+  }
+
+  // one Biot-Savart evaluation of plan e (its records already gathered) at the
+  // M targets P into out; prec -1 = the case's precision
+  void evaluate(const EvalPlan& e, int M, int mode, const double* P = nullptr, double* out = nullptr, int prec = -1) {
+    if (!P) P = s.targets;
+    if (!out) out = s.outv;
+    if (prec < 0) prec = opt.precision;
     const Chunk* ch = dChunks + e.coff;
-    if (opt.precision == VLM_PREC_FP64) {
-      launch_partial64(s.rec64, ch, e.nchunks, s.targets, M, s.part, stream);
+    if (prec == VLM_PREC_FP64) {
+      launch_partial64(s.rec64, ch, e.nchunks, P, M, s.part, stream);
     } else {
-      const bool nearOn = opt.precision == VLM_PREC_FP32_NEAR64;
+      const bool nearOn = prec == VLM_PREC_FP32_NEAR64;
       launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream);
       VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
-      launch_partial32(s.rec32, s.rec64, ch, e.nchunks, s.targets, M, s.part, s.err + 2, nearOn ? s.near : nullptr,
+      launch_partial32(s.rec32, s.rec64, ch, e.nchunks, P, M, s.part, s.err + 2, nearOn ? s.near : nullptr,
                        s.nearCap, s.nacc, stream);
     }
-    if (opt.precision == VLM_PREC_FP64) launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, s.outv, stream);
-    else launch_combine_unordered(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, s.outv, stream);
+    if (e.nchunks == 0) {
+      VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M, stream));
+      return;
+    }
+    if (prec == VLM_PREC_FP64) launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, out, stream);
+    else launch_combine_unordered(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, out, stream);
+  }
+
+  // ---- learned far-wake surrogate ----------------------------------------
+  struct SurrPlans {
+    EvalPlan rhsNoFar, nodeNoFar, farFar, farCollect, farAudit;
+    int collectNodes = 0, collectStride = 1, auditNodes = 0, auditStride = 1;
+  };
+  struct Surrogate {
+    vlm_surrogate_options o{};
+    bool on = false;
+    int phase = 0;  // VLM_SURR_WAIT / COLLECT / ACTIVE
+    int collected = 0, startStep = 0;
+    int64_t nsamp = 0, cap = 0;
+    Mlp net;
+    float *X = nullptr, *T = nullptr, *fX = nullptr, *fY = nullptr;
+    double *sP = nullptr, *sV = nullptr, *outFar = nullptr, *farP = nullptr, *scale = nullptr, *audit = nullptr;
+    double invR = 1.0;
+    bool useNow = false;
+    vlm_surrogate_stats st{};
+  };
+  Surrogate surr;
+  std::vector<SurrPlans> splans;
+  std::vector<void*> surrOwned;
+
+  int nearNodeCount(int rowNear) const { return d.nbC * (d.NW - (rowNear - 1)) * (d.ns + 1); }
+  int farRows(int rowFar) const { return std::max(d.NF - (rowFar - 1), 0); }
+
+  void setSurrogate(const vlm_surrogate_options& o) {
+    if (started) throw StatusError(VLM_ERR_STATE, "set the surrogate before vlm_case_start");
+    if (!o.enable) {
+      surr.on = false;
+      return;
+    }
+    if (opt.precision == VLM_PREC_FP64) throw StatusError(VLM_ERR_INVALID, "the surrogate runs with the FP32 precisions only");
+    if (d.NW == 0 || d.NF == 0) throw StatusError(VLM_ERR_UNSUPPORTED, "the surrogate needs a far wake");
+    if (o.collect_steps <= 0 || o.sample_stride <= 0 || o.train_iters < 0 || o.batch <= 0 || o.audit_samples <= 0 ||
+        o.hidden <= 0 || o.hidden > 1024 || o.layers < 2 || o.layers > kMlpMaxLayers || !(o.audit_tol > 0.0) ||
+        !(o.lr > 0.f))
+      throw StatusError(VLM_ERR_INVALID, "invalid surrogate options");
+    if (surr.on) throw StatusError(VLM_ERR_STATE, "the surrogate is already set");
+    if (o.young_far < 0 || o.min_far <= 0) throw StatusError(VLM_ERR_INVALID, "invalid surrogate options");
+    surr.o = o;
+    surr.on = true;
+    surrYoung = o.young_far;
+    // per-step plans: the same evaluations without the far wake, the far
+    // wake alone on the far-wake nodes, on the collection sample (FP32) and
+    // on the audit sample (FP64, the judge)
+    splans.assign(W.nt + 1, SurrPlans());
+    for (int k = 1; k <= W.nt; ++k) {
+      const StepPlan& pl = plans[k];
+      SurrPlans& sp = splans[k];
+      const int rN = pl.rowNear, rF = pl.rowFar;
+      const int rNprev = std::max(plans[k - 1].rowNear, 1);
+      addEval(sp.rhsNoFar, false, rN, rF, d.nbC * d.npan, 1);
+      addEval(sp.nodeNoFar, true, rN, rF, node_target_count(d, rN, rF), 1);
+      addEval(sp.farFar, false, rN, rF, d.nbC * farRows(rF), 2);
+      const int nodes = plans[k - 1].rowNear <= d.NW ? nearNodeCount(rNprev) : 0;
+      sp.collectStride = o.sample_stride;
+      sp.collectNodes = nodes / o.sample_stride;
+      sp.auditStride = std::max(1, nodes / o.audit_samples);
+      sp.auditNodes = nodes > 0 ? std::min(o.audit_samples, nodes) : 0;
+      addEval(sp.farCollect, false, rN, rF, d.nbC * d.npan + sp.collectNodes, 2);
+      addEval(sp.farAudit, false, rN, rF, d.nbC * d.npan + sp.auditNodes, 2, true);
+    }
+    allocScratch();
+    // surrogate buffers
+    int maxSample = 0, maxFar = 0;
+    for (int k = 1; k <= W.nt; ++k) {
+      maxSample = std::max(maxSample, d.nbC * d.npan + std::max(splans[k].collectNodes, splans[k].auditNodes));
+      maxFar = std::max(maxFar, d.nbC * farRows(plans[k].rowFar));
+    }
+    int64_t perStep = d.nbC * d.npan;
+    for (int k = 1; k <= W.nt; ++k) perStep = std::max<int64_t>(perStep, d.nbC * d.npan + splans[k].collectNodes);
+    surr.cap = perStep * o.collect_steps;
+    surr.X = dalloc<float>((size_t)surr.cap * 8, surrOwned);
+    surr.T = dalloc<float>((size_t)surr.cap * 3, surrOwned);
+    surr.fX = dalloc<float>((size_t)std::max(maxTargets, maxSample) * 8, surrOwned);
+    surr.fY = dalloc<float>((size_t)std::max(maxTargets, maxSample) * 3, surrOwned);
+    surr.sP = dalloc<double>((size_t)maxSample * 3, surrOwned);
+    surr.sV = dalloc<double>((size_t)maxSample * 3, surrOwned);
+    surr.outFar = dalloc<double>((size_t)std::max(maxFar, 1) * 3, surrOwned);
+    surr.farP = dalloc<double>((size_t)std::max(maxFar, 1) * 3, surrOwned);
+    surr.scale = dalloc<double>(1, surrOwned);
+    surr.audit = dalloc<double>(2, surrOwned);
+    std::vector<int> sizes(o.layers + 1, o.hidden);
+    sizes.front() = 8;
+    sizes.back() = 3;
+    surr.net.create(sizes, o.seed, stream);
+    surr.net.reserve(std::max(o.batch, 1 << 14));
+    // length scale of the features: the farthest collocation point from the hub
+    const double* f0 = hFrames;
+    double r2 = 0.0;
+    for (int b = 0; b < d.nb; ++b)
+      for (int p = 0; p < d.npan; ++p) {
+        const double* c = f0 + d.fl.pan + ((size_t)b * d.npan + p) * kPan + 12;
+        const double* h = f0 + d.fl.rot + 3;
+        const double dx = c[0] - h[0], dy = c[1] - h[1], dz = c[2] - h[2];
+        r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+      }
+    surr.invR = r2 > 0.0 ? 1.0 / std::sqrt(r2) : 1.0;
+    surr.phase = VLM_SURR_WAIT;
+    surr.st = vlm_surrogate_stats{};
+  }
+
+  // old far-wake filaments per blade over their most
+  double farFill(int rowFar) const {
+    const int most = d.NF - surrYoung;
+    return most > 0 ? (double)std::max(farRows(rowFar) - surrYoung, 0) / most : 0.0;
+  }
+  int youngAt(int k) const { return std::min(surrYoung, farRows(plans[k].rowFar)); }
+
+  // direct far-wake velocity at the sample targets of step k's start state
+  // (CPs at frame k-1 and every stride-th near-wake node from offset)
+  int surrSample(int k, const EvalPlan& e, int nodes, int stride, int offset, int prec) {
+    const int M = d.nbC * d.npan + nodes;
+    const int rNprev = plans[k - 1].rowNear;
+    launch_surr_targets(d, s, frame(k - 1), rNprev, plans[k].rowFar, 0, stride, offset, nodes, surr.sP, stream);
+    launch_gather(d, s, frame(k - 1), dGroups + e.goff, e.ngroups, e.nrec, plans[k].rowNear, plans[k].rowFar, false,
+                  stream);
+    evaluate(e, M, 2, surr.sP, surr.sV, prec);
+    launch_surr_features(d, frame(k - 1), surr.sP, M, surr.invR, farFill(plans[k].rowFar), surr.fX, stream);
+    return M;
+  }
+
+  void surrTrain() {
+    Surrogate& S = surr;
+    const int64_t n = S.nsamp;
+    std::vector<float> hX((size_t)n * 8), hT((size_t)n * 3);
+    VLM_CUDA(cudaMemcpyAsync(hX.data(), S.X, sizeof(float) * hX.size(), cudaMemcpyDeviceToHost, stream));
+    VLM_CUDA(cudaMemcpyAsync(hT.data(), S.T, sizeof(float) * hT.size(), cudaMemcpyDeviceToHost, stream));
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    double ss = 0.0;
+    for (float t : hT) ss += (double)t * t;
+    const double scale = std::sqrt(ss / std::max<size_t>(hT.size(), 1)) + 1e-30;
+    // a seeded shuffle, then targets in units of the rms velocity
+    std::vector<int64_t> idx((size_t)n);
+    for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
+    uint64_t r = S.o.seed * 0x9E3779B97F4A7C15ull + (uint64_t)S.st.trainings + 1;
+    for (int64_t i = n - 1; i > 0; --i) {
+      r ^= r << 13;
+      r ^= r >> 7;
+      r ^= r << 17;
+      std::swap(idx[(size_t)i], idx[(size_t)(r % (uint64_t)(i + 1))]);
+    }
+    std::vector<float> sX((size_t)n * 8), sT((size_t)n * 3);
+    for (int64_t i = 0; i < n; ++i) {
+      std::memcpy(&sX[(size_t)i * 8], &hX[(size_t)idx[(size_t)i] * 8], 8 * sizeof(float));
+      for (int c = 0; c < 3; ++c) sT[(size_t)i * 3 + c] = (float)(hT[(size_t)idx[(size_t)i] * 3 + c] / scale);
+    }
+    VLM_CUDA(cudaMemcpyAsync(S.X, sX.data(), sizeof(float) * sX.size(), cudaMemcpyHostToDevice, stream));
+    VLM_CUDA(cudaMemcpyAsync(S.T, sT.data(), sizeof(float) * sT.size(), cudaMemcpyHostToDevice, stream));
+    VLM_CUDA(cudaMemcpyAsync(S.scale, &scale, sizeof(double), cudaMemcpyHostToDevice, stream));
+    const int b = (int)std::min<int64_t>(S.o.batch, n);
+    const int64_t nb = std::max<int64_t>(n / b, 1);
+    for (int it = 0; it < S.o.train_iters; ++it) {
+      const int64_t q = it % nb;
+      S.net.grad(S.X + (size_t)q * b * 8, S.T + (size_t)q * b * 3, b);
+      // the last third of the iterations at a fifth of the rate
+      S.net.adam(it < (2 * S.o.train_iters) / 3 ? S.o.lr : 0.2f * S.o.lr);
+    }
+    VLM_CUDA(cudaGetLastError());
+    float loss = 0.f;
+    VLM_CUDA(cudaMemcpyAsync(&loss, S.net.loss, sizeof(float), cudaMemcpyDeviceToHost, stream));
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    S.st.last_loss = loss;
+    S.st.trainings += 1;
+  }
+
+  // the surrogate's work before step k: collect samples, train, or audit
+  void surrPreStep(int k) {
+    Surrogate& S = surr;
+    S.useNow = false;
+    const SurrPlans& sp = splans[k];
+    const int rowsF = farRows(plans[k].rowFar);
+    const int rowsOld = rowsF - youngAt(k);
+    if (S.phase == VLM_SURR_WAIT && rowsOld >= S.o.min_far && sp.collectNodes > 0) {
+      S.phase = VLM_SURR_COLLECT;
+      S.collected = 0;
+      S.nsamp = 0;
+    }
+    if (S.phase == VLM_SURR_COLLECT) {
+      const int off = (int)((uint64_t)k * 2654435761ull % (uint64_t)sp.collectStride);
+      const int M = surrSample(k, sp.farCollect, sp.collectNodes, sp.collectStride, off, opt.precision);
+      const int n = (int)std::min<int64_t>(M, S.cap - S.nsamp);
+      launch_surr_append(n, S.fX, S.sV, S.X + (size_t)S.nsamp * 8, S.T + (size_t)S.nsamp * 3, stream);
+      S.nsamp += n;
+      if (++S.collected >= S.o.collect_steps) {
+        surrTrain();
+        S.phase = VLM_SURR_ACTIVE;
+      }
+      S.st.samples = S.nsamp;
+      return;
+    }
+    if (S.phase != VLM_SURR_ACTIVE || rowsOld <= 0) return;
+    // audit: the network against the direct FP64 far-wake sum on a random sample
+    const int off = (int)((uint64_t)k * 2246822519ull % (uint64_t)sp.auditStride);
+    const int M = surrSample(k, sp.farAudit, sp.auditNodes, sp.auditStride, off, VLM_PREC_FP64);
+    S.net.forward(S.fX, M, S.fY);
+    launch_surr_audit(M, S.fY, S.scale, S.sV, S.audit, stream);
+    double a[2] = {0.0, 0.0};
+    VLM_CUDA(cudaMemcpyAsync(a, S.audit, sizeof(a), cudaMemcpyDeviceToHost, stream));
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    const double e = std::sqrt(a[0] / std::max(a[1], 1e-300));
+    S.st.audits += 1;
+    S.st.last_audit_err = e;
+    S.st.max_audit_err = std::max(S.st.max_audit_err, e);
+    if (e <= S.o.audit_tol) {
+      S.useNow = true;
+      S.st.active_steps += 1;
+    } else {
+      // revert: this step sums the far wake directly; collect fresh data
+      S.st.reverts += 1;
+      S.phase = VLM_SURR_COLLECT;
+      S.collected = 0;
+      S.nsamp = 0;
+    }
   }
 
   void evalNodes(int k, bool pred) {
     const StepPlan& pl = plans[k];
     const int M = node_target_count(d, pl.rowNear, pl.rowFar);
     launch_node_targets(d, s, pl.rowNear, pl.rowFar, pred, s.targets, stream);
-    launch_gather(d, s, frame(k), dGroups + pl.node.goff, pl.node.ngroups, pl.node.nrec, pl.rowNear, pl.rowFar, pred,
-                  stream);
-    evaluate(pl.node, M, 0);
+    if (surr.on && surr.useNow) {
+      // near-wake nodes: direct without the far wake + the network's far-wake
+      // velocity; far-wake nodes: + the direct far-wake sum
+      const SurrPlans& sp = splans[k];
+      launch_gather(d, s, stepFrame(k), dGroups + sp.nodeNoFar.goff, sp.nodeNoFar.ngroups, sp.nodeNoFar.nrec, pl.rowNear,
+                    pl.rowFar, pred, stream);
+      evaluate(sp.nodeNoFar, M, 0);
+      // every far-wake node, young or old, sums the old far wake directly
+      const int Mf = d.nbC * farRows(pl.rowFar);
+      launch_surr_far_targets(d, s, pl.rowFar, 0, pred, surr.farP, stream);
+      launch_gather(d, s, stepFrame(k), dGroups + sp.farFar.goff, sp.farFar.ngroups, sp.farFar.nrec, pl.rowNear, pl.rowFar,
+                    pred, stream);
+      evaluate(sp.farFar, Mf, 2, surr.farP, surr.outFar);
+      launch_surr_features(d, frame(pred ? k : k - 1), s.targets, M, surr.invR, farFill(pl.rowFar), surr.fX, stream);
+      surr.net.forward(surr.fX, M, surr.fY);
+      launch_surr_merge_nodes(d, pl.rowNear, pl.rowFar, 0, M, surr.fY, surr.scale, surr.outFar, s.outv, stream);
+    } else {
+      launch_gather(d, s, stepFrame(k), dGroups + pl.node.goff, pl.node.ngroups, pl.node.nrec, pl.rowNear, pl.rowFar,
+                    pred, stream);
+      evaluate(pl.node, M, 0);
+    }
     const double iwv = k < W.sw.initWakeVelNt ? W.P.initWakeVel : 0.0;
-    launch_scatter_nodes(d, s, frame(k), pl.rowNear, pl.rowFar, pred, iwv, stream);
+    launch_scatter_nodes(d, s, stepFrame(k), pl.rowNear, pl.rowFar, pred, iwv, stream);
   }
 
   void start() {
@@ -354,6 +691,7 @@ struct Case {
     VLM_CUDA(cudaStreamSynchronize(stream));
     if (err == 10) throw StatusError(VLM_ERR_SINGULAR, "Matrix is numerically singular!");
     if (err == 11) throw StatusError(VLM_ERR_SINGULAR, "Computed AIC_inv does not seem to be correct within given tolerance");
+    if (refine) launch_lu32(d, s, stream);
     launch_solve(d, s, frame(0), false, stream);
     if (d.NW > 0) launch_shed(d, s, frame(0), d.NW + 1, false, stream);
     if (W.sw.rotorForcePlot != 0) launch_loads(d, s, frame(0), chunk64, 0, stream);
@@ -366,7 +704,7 @@ struct Case {
   void enqueueStep(int k) {
     const StepPlan& pl = plans[k];
     const int rN = pl.rowNear, rF = pl.rowFar;
-    const double* fr = frame(k);
+    const double* fr = stepFrame(k);
     const bool wake = d.NW > 0 && W.sw.wakeSuppress == 0;
     if (wake) {
       launch_shed(d, s, fr, rN, true, stream);
@@ -374,14 +712,25 @@ struct Case {
       if (W.sw.wakeDissipation == 1) launch_dissipate(d, s, rN, rF, stream);
     }
     if (d.NW > 0) {
+      const int Mcp = d.nbC * d.npan;
       launch_cp_targets(d, fr, s.targets, stream);
-      launch_gather(d, s, fr, dGroups + pl.rhs.goff, pl.rhs.ngroups, pl.rhs.nrec, rN, rF, false, stream);
-      evaluate(pl.rhs, d.nbC * d.npan, 1);
+      if (surr.on && surr.useNow) {
+        const EvalPlan& e = splans[k].rhsNoFar;
+        launch_gather(d, s, fr, dGroups + e.goff, e.ngroups, e.nrec, rN, rF, false, stream);
+        evaluate(e, Mcp, 1);
+        launch_surr_features(d, frame(k - 1), s.targets, Mcp, surr.invR, farFill(rF), surr.fX, stream);
+        surr.net.forward(surr.fX, Mcp, surr.fY);
+        launch_surr_add(Mcp, surr.fY, surr.scale, s.outv, stream);
+      } else {
+        launch_gather(d, s, fr, dGroups + pl.rhs.goff, pl.rhs.ngroups, pl.rhs.nrec, rN, rF, false, stream);
+        evaluate(pl.rhs, Mcp, 1);
+      }
       launch_solve(d, s, fr, true, stream);
     } else {
       launch_solve(d, s, fr, false, stream);
     }
-    if (W.sw.rotorForcePlot != 0 && k % W.sw.rotorForcePlot == 0) launch_loads(d, s, fr, chunk64, k, stream);
+    if (W.sw.rotorForcePlot != 0 && k % W.sw.rotorForcePlot == 0)
+      launch_loads(d, s, fr, chunk64, replaying ? -1 : k, stream);
     if (!wake) return;
     evalNodes(k, false);
     switch (W.sw.fdScheme) {
@@ -453,35 +802,58 @@ struct Case {
     launch_shed(d, s, fr, rN, false, stream);
   }
 
-  void step(int nsteps, double* ctRows) {
+  // ---- the time loop: inputs in, steps enqueued, results out ---------------
+  void checkSteps(int nsteps) const {
     if (!started) throw StatusError(VLM_ERR_STATE, "vlm_case_start must be called before vlm_case_step");
     if (nsteps < 0 || iter + nsteps > W.nt)
       throw StatusError(VLM_ERR_INVALID, "nsteps runs past the case's nt timesteps");
-    // this call's inputs: the wing frames of its steps (host -> device)
+  }
+  // this call's inputs: the wing frames of its steps (host -> device)
+  void uploadFrames(int nsteps) {
     if (nsteps > 0)
       VLM_CUDA(cudaMemcpyAsync(s.frames + (size_t)(iter + 1) * d.fl.size, hFrames + (size_t)(iter + 1) * d.fl.size,
                                sizeof(double) * d.fl.size * nsteps, cudaMemcpyHostToDevice, stream));
-    VLM_CUDA(cudaEventRecord(ev0, stream));
-    for (int k = iter + 1; k <= iter + nsteps; ++k) enqueueStep(k);
-    VLM_CUDA(cudaEventRecord(ev1, stream));
-    VLM_CUDA(cudaGetLastError());
+  }
+  void enqueueOne(int k) {
+    if (steadyStep(k)) {
+      replayStep(k);
+      return;
+    }
+    iterSynced = false;
+    if (surr.on) surrPreStep(k);
+    enqueueStep(k);
+  }
+  // after the stream has run the steps: CT rows out, device error flags
+  void finishSteps(int nsteps, double* ctRows) {
     if (ctRows && nsteps > 0)
       VLM_CUDA(cudaMemcpyAsync(ctRows, s.ctHist + (size_t)(iter + 1) * 10, sizeof(double) * 10 * nsteps,
                                cudaMemcpyDeviceToHost, stream));
     int errs[4] = {0, 0, 0, 0};
     VLM_CUDA(cudaMemcpyAsync(errs, s.err, sizeof(errs), cudaMemcpyDeviceToHost, stream));
     VLM_CUDA(cudaStreamSynchronize(stream));
-    const int err = errs[2];
-    float ms = 0.f;
-    VLM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-    lastMs = ms;
     iter += nsteps;
+    const int err = errs[2];
     if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
     if (err == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
     if (err) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
+    if (errs[1]) throw StatusError(VLM_ERR_SINGULAR, "FP32 LU iterative refinement left a relative residual above 1e-9");
     if (ctRows)
       for (int k = 0; k < 10 * nsteps; ++k)
         if (!std::isfinite(ctRows[k])) throw StatusError(VLM_ERR_NONFINITE, "non-finite load in the CT history");
+  }
+
+  void step(int nsteps, double* ctRows) {
+    checkSteps(nsteps);
+    uploadFrames(nsteps);
+    VLM_CUDA(cudaEventRecord(ev0, stream));
+    for (int k = iter + 1; k <= iter + nsteps; ++k) enqueueOne(k);
+    VLM_CUDA(cudaEventRecord(ev1, stream));
+    VLM_CUDA(cudaGetLastError());
+    VLM_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    VLM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    lastMs = ms;
+    finishSteps(nsteps, ctRows);
   }
 
   // Times the partial-sum kernel of the next step's wake-node evaluation on
@@ -538,6 +910,7 @@ struct Case {
     const bool bok = b >= 0 && b < d.nb;
     const size_t npan = d.npan, NW = d.NW, NF = d.NF, ns = d.ns;
     if (k == "dt") v = {W.dt};
+    else if (k == "lu_residual") v = refine ? dget(s.luRes, 1) : std::vector<double>{0.0};
     else if (k == "nonDimDenom") v = {W.nonDimDenom};
     else if (k == "ct_hist") v = dget(s.ctHist, (size_t)(iter + 1) * 10);
     else if (k == "gamVec") v = dget(s.gamVec, d.n);
@@ -835,6 +1208,8 @@ void vlm_default_options(vlm_options* o) {
   o->near_factor = 4.0;
   o->device = 0;
   o->use_graph = 1;
+  o->solve_mode = -1;
+  o->nbody_slots = 0;
 }
 
 int vlm_device_info(int device, int* sm_count, int* cc_major, int* cc_minor) {
@@ -887,6 +1262,194 @@ int vlm_biot_savart_rings(const double* corners, const double* rvc, const double
     }
     cleanup();
   });
+}
+
+// ---------------------------------------------------------------------------
+// Batch: many independent cases advanced together.  Each case keeps its own
+// stream; a step of the batch enqueues every case's step on its stream, so
+// the cases' kernels run concurrently.  Once every case is in its steady
+// state, one step of the whole batch is captured as ONE CUDA graph (a fork
+// from the batch stream into every case stream and a join back) and
+// replayed with a single graph launch per step.  Each case's FP32 chunk plan
+// is made for its share of the device's block slots.
+struct vlm_batch {
+  std::vector<vlm_case*> cases;
+  cudaStream_t origin = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<std::pair<int, int>> gsig;  // (rowNear, rowFar) per case of the captured step
+  long graphKernels = 0;
+  double lastMs = 0.0;
+
+  ~vlm_batch() {
+    if (origin) cudaStreamSynchronize(origin);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (cudaEvent_t e : joins) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ev0, ev1, fork})
+      if (e) cudaEventDestroy(e);
+    if (origin) cudaStreamDestroy(origin);
+    for (vlm_case* c : cases) delete c;
+  }
+
+  // all case streams wait for the batch stream's work so far
+  void forkAll() {
+    VLM_CUDA(cudaEventRecord(fork, origin));
+    for (vlm_case* c : cases) VLM_CUDA(cudaStreamWaitEvent(c->c.stream, fork, 0));
+  }
+  // the batch stream waits for every case stream's work so far
+  void joinAll() {
+    for (size_t i = 0; i < cases.size(); ++i) {
+      VLM_CUDA(cudaEventRecord(joins[i], cases[i]->c.stream));
+      VLM_CUDA(cudaStreamWaitEvent(origin, joins[i], 0));
+    }
+  }
+
+  bool allSteady(int k) const {
+    for (vlm_case* c : cases)
+      if (!c->c.steadyStep(k)) return false;
+    return true;
+  }
+
+  void capture(int k) {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    cudaGraph_t g = nullptr;
+    const long l0 = launch_count();
+    VLM_CUDA(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal));
+    try {
+      forkAll();
+      for (vlm_case* c : cases) {
+        Case& C = c->c;
+        C.replaying = true;
+        launch_step_begin(C.d, C.s, C.stream);
+        C.enqueueStep(k);
+        C.replaying = false;
+      }
+      joinAll();
+    } catch (...) {
+      for (vlm_case* c : cases) c->c.replaying = false;
+      cudaStreamEndCapture(origin, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    VLM_CUDA(cudaStreamEndCapture(origin, &g));
+    const cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+    cudaGraphDestroy(g);
+    VLM_CUDA(e);
+    graphKernels = launch_count() - l0;
+    count_launches(-graphKernels);
+    gsig.clear();
+    for (vlm_case* c : cases) gsig.emplace_back(c->c.plans[k].rowNear, c->c.plans[k].rowFar);
+  }
+
+  bool sigMatches(int k) const {
+    if (!gexec || gsig.size() != cases.size()) return false;
+    for (size_t i = 0; i < cases.size(); ++i)
+      if (gsig[i] != std::make_pair(cases[i]->c.plans[k].rowNear, cases[i]->c.plans[k].rowFar)) return false;
+    return true;
+  }
+
+  void step(int nsteps, double* ctRows) {
+    if (cases.empty()) return;
+    const int it0 = cases[0]->c.iter;
+    for (vlm_case* c : cases) {
+      if (c->c.iter != it0) throw StatusError(VLM_ERR_STATE, "the batch's cases are at different steps");
+      c->c.checkSteps(nsteps);
+    }
+    for (vlm_case* c : cases) c->c.uploadFrames(nsteps);
+    VLM_CUDA(cudaEventRecord(ev0, origin));
+    joinAll();  // the frames are in
+    for (int k = it0 + 1; k <= it0 + nsteps; ++k) {
+      if (allSteady(k)) {
+        if (!sigMatches(k)) capture(k);
+        // device step counters for replay (the graph advances them)
+        for (vlm_case* c : cases) {
+          Case& C = c->c;
+          if (!C.iterSynced) {
+            *C.hIter = k - 1;
+            VLM_CUDA(cudaMemcpyAsync(C.s.devIter, C.hIter, sizeof(int), cudaMemcpyHostToDevice, origin));
+            C.iterSynced = true;
+          }
+        }
+        VLM_CUDA(cudaGraphLaunch(gexec, origin));
+        count_launches(graphKernels);
+      } else {
+        forkAll();
+        for (vlm_case* c : cases) c->c.enqueueOne(k);
+        joinAll();
+      }
+    }
+    forkAll();  // later work on the case streams follows the batch's steps
+    VLM_CUDA(cudaEventRecord(ev1, origin));
+    VLM_CUDA(cudaGetLastError());
+    VLM_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    VLM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    lastMs = ms;
+    for (size_t i = 0; i < cases.size(); ++i)
+      cases[i]->c.finishSteps(nsteps, ctRows ? ctRows + (size_t)i * nsteps * 10 : nullptr);
+  }
+};
+
+int vlm_batch_create(int ncases, const char* const* configs, const char* const* geoms, const char* const* base_dirs,
+                     const vlm_options* opt, vlm_batch** out) {
+  if (!out || ncases <= 0 || !configs || !geoms) {
+    g_err = "invalid batch arguments";
+    return VLM_ERR_INVALID;
+  }
+  *out = nullptr;
+  auto b = std::make_unique<vlm_batch>();
+  const int rc = guard([&]() {
+    vlm_options o;
+    vlm_default_options(&o);
+    if (opt) o = *opt;
+    VLM_CUDA(cudaSetDevice(o.device));
+    if (o.nbody_slots <= 0) o.nbody_slots = std::max(1, partial32_slots() / ncases);
+    for (int i = 0; i < ncases; ++i) {
+      if (!configs[i] || !geoms[i]) throw StatusError(VLM_ERR_INVALID, "null case text");
+      auto c = std::make_unique<vlm_case>();
+      c->c.create(configs[i], geoms[i], base_dirs && base_dirs[i] ? base_dirs[i] : "", &o);
+      b->cases.push_back(c.release());
+    }
+    VLM_CUDA(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+    VLM_CUDA(cudaEventCreate(&b->ev0));
+    VLM_CUDA(cudaEventCreate(&b->ev1));
+    VLM_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->joins.resize(ncases);
+    for (int i = 0; i < ncases; ++i) VLM_CUDA(cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming));
+  });
+  if (rc == VLM_OK) *out = b.release();
+  return rc;
+}
+
+int vlm_batch_destroy(vlm_batch* b) {
+  delete b;
+  return VLM_OK;
+}
+
+int vlm_batch_case(vlm_batch* b, int i, vlm_case** out) {
+  if (!b || !out || i < 0 || i >= (int)b->cases.size()) return VLM_ERR_INVALID;
+  *out = b->cases[i];
+  return VLM_OK;
+}
+
+int vlm_batch_start(vlm_batch* b) {
+  if (!b) return VLM_ERR_INVALID;
+  return guard([&]() {
+    for (vlm_case* c : b->cases) c->c.start();
+  });
+}
+
+int vlm_batch_step(vlm_batch* b, int nsteps, double* ct_rows) {
+  if (!b) return VLM_ERR_INVALID;
+  return guard([&]() { b->step(nsteps, ct_rows); });
+}
+
+int vlm_batch_last_step_ms(vlm_batch* b, double* ms) {
+  if (!b || !ms) return VLM_ERR_INVALID;
+  *ms = b->lastMs;
+  return VLM_OK;
 }
 
 int vlm_case_create(const char* config_text, const char* geom_text, const char* base_dir, const vlm_options* opt,
@@ -986,6 +1549,35 @@ int64_t vlm_case_get(vlm_case* c, const char* name, int blade, double* out, int6
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V) {
   if (!c || (M > 0 && (!P || !V))) return VLM_ERR_INVALID;
   return guard([&]() { c->c.vindPoints(P, M, V); });
+}
+
+void vlm_default_surrogate_options(vlm_surrogate_options* o) {
+  if (!o) return;
+  o->enable = 1;
+  o->young_far = 216;
+  o->min_far = 72;
+  o->collect_steps = 72;
+  o->sample_stride = 4;
+  o->train_iters = 3000;
+  o->batch = 1024;
+  o->lr = 1e-3f;
+  o->audit_samples = 256;
+  o->audit_tol = 0.1;
+  o->hidden = 128;
+  o->layers = 4;
+  o->seed = 1;
+}
+
+int vlm_case_set_surrogate(vlm_case* c, const vlm_surrogate_options* o) {
+  if (!c || !o) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.setSurrogate(*o); });
+}
+
+int vlm_case_surrogate_stats(vlm_case* c, vlm_surrogate_stats* out) {
+  if (!c || !out) return VLM_ERR_INVALID;
+  *out = c->c.surr.st;
+  out->phase = c->c.surr.on ? c->c.surr.phase : VLM_SURR_OFF;
+  return VLM_OK;
 }
 
 int vlm_case_profile_eval(vlm_case* c, int reps, double* ms_per_launch, double* ring_pairs, double* fil_pairs) {

@@ -494,11 +494,11 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
   int g = 0;
   while (g + 1 < ngroups && t >= groups[g + 1].rec_begin) ++g;
   const Group G = groups[g];
-  const int l = t - G.rec_begin;
+  const int l0 = t - G.rec_begin;
   const int b = G.blade;
   double* R = s.rec64 + (size_t)t * kRec64;
   if (G.kind == 0) {
-    const int j = l / d.nc, i = l % d.nc;
+    const int j = l0 / d.nc, i = l0 % d.nc;
     const int p = i + d.nc * j;
     const double* w = panRec(d, fr, b, p);
     for (int k = 0; k < 12; ++k) R[k] = w[k];
@@ -511,6 +511,9 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
   const int nNear = rowsN * d.ns;
   const int hs = rowFar <= d.NF ? d.ns : 0;
   const double* nc = pred ? s.nCP : s.nC;
+  // a far-only group (pad[0] = 1) lists the far filaments alone, from the
+  // pad[1]-th active one
+  const int l = G.pad[0] ? l0 + nNear + hs + G.pad[1] : l0;
   if (l < nNear) {
     const int j = l / rowsN, i = rowNear - 1 + l % rowsN;
     const size_t r = ringI(d, b, i, j);
@@ -635,6 +638,163 @@ __global__ void k_inv_cols(Dims d, DevState s) {
   }
 }
 
+// ---- FP32 LU + FP64 iterative refinement ---------------------------------------
+// The AIC (FP64, assembled once like the reference) is factored in FP32 with
+// partial pivoting and inverted in FP32 (one unit column per thread); every
+// solve then refines in FP64: x <- x + inv32 (b - A x), the residual b - A x
+// in FP64.  ||I - inv32 A|| ~ cond(A) x 2^-24 << 1 for vortex-lattice AICs,
+// so each pass gains ~7 digits.
+__global__ void k_lu32(Dims d, DevState s) {
+  const int n = d.n;
+  float* A = s.LU32;
+  __shared__ float redv[1024];
+  __shared__ int redi[1024];
+  __shared__ int pk;
+  for (long e = threadIdx.x; e < (long)n * n; e += blockDim.x) A[e] = (float)s.AIC[e];
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    float bv = -1.f;
+    int bi = n;
+    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+      const float v = fabsf(A[i + (size_t)n * k]);
+      if (v > bv || (v == bv && i < bi)) {
+        bv = v;
+        bi = i;
+      }
+    }
+    redv[threadIdx.x] = bv;
+    redi[threadIdx.x] = bi;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        const float v = redv[threadIdx.x + w];
+        const int i = redi[threadIdx.x + w];
+        if (v > redv[threadIdx.x] || (v == redv[threadIdx.x] && i < redi[threadIdx.x])) {
+          redv[threadIdx.x] = v;
+          redi[threadIdx.x] = i;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      pk = redi[0];
+      s.piv32[k] = pk;
+      if (A[pk + (size_t)n * k] == 0.f) atomicExch(s.err, 10);
+    }
+    __syncthreads();
+    const int p = pk;
+    if (p != k)
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const float t = A[k + (size_t)n * j];
+        A[k + (size_t)n * j] = A[p + (size_t)n * j];
+        A[p + (size_t)n * j] = t;
+      }
+    __syncthreads();
+    const float akk = A[k + (size_t)n * k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)n * k] = A[i + (size_t)n * k] / akk;
+    __syncthreads();
+    const long m = n - k - 1;
+    for (long e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + (int)(e % m), j = k + 1 + (int)(e / m);
+      A[i + (size_t)n * j] = fmaf(-A[i + (size_t)n * k], A[k + (size_t)n * j], A[i + (size_t)n * j]);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_inv32_cols(Dims d, DevState s) {
+  const int n = d.n;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const float* A = s.LU32;
+  float* X = s.AICinv32 + (size_t)n * c;
+  int pos = c;
+  for (int k = 0; k < n; ++k) {
+    const int pk = s.piv32[k];
+    if (pos == k) pos = pk;
+    else if (pos == pk) pos = k;
+  }
+  for (int i = 0; i < n; ++i) {
+    float sum = i == pos ? 1.f : 0.f;
+    for (int k = 0; k < i; ++k) sum = fmaf(-A[i + (size_t)n * k], X[k], sum);
+    X[i] = sum;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    float sum = X[i];
+    for (int k = i + 1; k < n; ++k) sum = fmaf(-A[i + (size_t)n * k], X[k], sum);
+    X[i] = sum / A[i + (size_t)n * i];
+  }
+}
+
+// Solve AIC gamVec = -RHS by refinement (one block); records the final
+// relative residual max|b - A x| / max|b| in s.luRes[0] and flags err[1]
+// when it stays above 1e-9.
+constexpr int kRefinePasses = 3;
+__global__ void k_solve_refine(Dims d, DevState s) {
+  const int n = d.n;
+  __shared__ double red[1024];
+  double* b = s.RHS;
+  double* x = s.refX;
+  double* r = s.refR;
+  if (d.axisym)
+    for (int i = d.npan + threadIdx.x; i < n; i += blockDim.x) b[i] = b[i % d.npan];
+  __syncthreads();
+  double bmax = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    b[i] = -1.0 * b[i];
+    x[i] = 0.0;
+    r[i] = b[i];
+    bmax = fmax(bmax, fabs(b[i]));
+  }
+  red[threadIdx.x] = bmax;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  bmax = red[0];
+  __syncthreads();
+  double rmax = 0.0;
+  for (int pass = 0; pass < kRefinePasses; ++pass) {
+    // x += inv32 r  (FP32 products of the FP32-rounded residual, FP64 update)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      float z = 0.f;
+      for (int j = 0; j < n; ++j) z = fmaf(s.AICinv32[i + (size_t)n * j], (float)r[j], z);
+      x[i] += (double)z;
+    }
+    __syncthreads();
+    // r = b - A x in FP64
+    rmax = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double ax = 0.0;
+      for (int j = 0; j < n; ++j) ax = fma(s.AIC[i + (size_t)n * j], x[j], ax);
+      r[i] = b[i] - ax;
+      rmax = fmax(rmax, fabs(r[i]));
+    }
+    __syncthreads();
+  }
+  red[threadIdx.x] = rmax;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  const double rel = bmax > 0.0 ? red[0] / bmax : red[0];
+  if (threadIdx.x == 0) {
+    s.luRes[0] = rel;
+    if (!(rel <= 1e-9)) atomicExch(s.err + 1, 12);
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s.gamVecPrev[i] = s.gamVec[i];
+    s.gamVec[i] = x[i];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < d.nbC * d.npan; t += blockDim.x) s.wGam[t] = s.gamVec[t];
+  __syncthreads();
+  if (d.axisym)
+    for (int t = d.npan + threadIdx.x; t < d.nb * d.npan; t += blockDim.x) s.wGam[t] = s.wGam[t % d.npan];
+}
+
 // libMath.f90:428-458 (tolerance 1E-04 single precision)
 __global__ void k_is_inverse(Dims d, DevState s) {
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -697,14 +857,6 @@ struct ChunkAcc {
   }
   __device__ d3 result() const { return (C > 0 && cnt > 0) ? tot + part : tot; }
 };
-
-__device__ __forceinline__ void wing_ring(const Dims& d, const double* fr, int b, int p, d3* c) {
-  const double* w = panRec(d, fr, b, p);
-  c[0] = ld3(w);
-  c[1] = ld3(w + 3);
-  c[2] = ld3(w + 6);
-  c[3] = ld3(w + 9);
-}
 
 // Velocity at collocation point t including the wing's own induced velocity
 // minus its bound vortices (src/classdef.f90 calc_force's velCPTotal): one
@@ -837,7 +989,16 @@ __device__ double lsq2_dev(double xq, const double* xd, const double* yd, int n)
 
 constexpr int kMaxNc = 64;
 
+__global__ void k_step_begin(Dims d, DevState s) {
+  const int it = s.devIter[0] + 1;
+  const double* src = s.frames + (size_t)it * d.fl.size;
+  for (int i = threadIdx.x; i < d.fl.size; i += blockDim.x) s.curFrame[i] = src[i];
+  __syncthreads();
+  if (threadIdx.x == 0) s.devIter[0] = it;
+}
+
 __global__ void k_loads(Dims d, DevState s, const double* fr, int iter) {
+  if (iter < 0) iter = s.devIter[0];
   const int nsec = d.nbC * d.ns;
   const double iGS = -1.0 * fsign1(d.omega);
   // phase A: sectional resultant velocity and lift/drag directions
@@ -1120,7 +1281,18 @@ void launch_solve(const Dims& d, const DevState& s, const double* frame, bool wi
   count_launch();
   k_rhs<<<nblk(d.nbC * d.npan, 128), 128, 0, st>>>(d, s, frame, withWake ? 1 : 0);
   count_launch();
-  k_solve<<<1, 1024, 0, st>>>(d, s);
+  if (s.LU32) k_solve_refine<<<1, 1024, 0, st>>>(d, s);
+  else k_solve<<<1, 1024, 0, st>>>(d, s);
+}
+void launch_lu32(const Dims& d, const DevState& s, cudaStream_t st) {
+  count_launch();
+  k_lu32<<<1, 1024, 0, st>>>(d, s);
+  count_launch();
+  k_inv32_cols<<<nblk(d.n, 64), 64, 0, st>>>(d, s);
+}
+void launch_step_begin(const Dims& d, const DevState& s, cudaStream_t st) {
+  count_launch();
+  k_step_begin<<<1, 256, 0, st>>>(d, s);
 }
 void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st) {
   count_launch();

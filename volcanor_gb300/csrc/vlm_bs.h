@@ -17,6 +17,7 @@ namespace vlm {
 
 // Number of kernels this library has launched (all threads, all cases).
 void count_launch();
+void count_launches(long n);  // kernels of a replayed graph (negative: undo a capture's count)
 long launch_count();
 
 // FP64 source record, 18 doubles:
@@ -64,7 +65,7 @@ struct Group {
   int32_t chunk_count;
   int32_t kind;         // 0 = wing sum, 1 = wake sum
   int32_t blade;        // blade whose wing or wake the group sums
-  int32_t pad[2];
+  int32_t pad[2];       // pad[0] = 1: a wake group of the far-wake filaments alone, from the pad[1]-th
 };
 
 struct Chunk {

@@ -61,6 +61,10 @@ struct DevState {
   double *wGam, *gamPrev, *gamVec, *gamVecPrev, *RHS, *velCP, *velCPTotal;
   double *AIC, *AICinv, *LU;
   int* piv;
+  // FP32 LU + FP64 refinement (null when the solve uses the FP64 inverse)
+  float *LU32, *AICinv32;
+  int* piv32;
+  double *refX, *refR, *luRes;
   // near wake
   double *nC, *nCP, *nGam, *nRvc, *nAge, *nTmp;
   // far wake
@@ -80,7 +84,11 @@ struct DevState {
   NearPair* near;
   long long* nacc;  // fixed-point near-field accumulators, zero between evaluations
   int nearCap;
-  int* err;  // [0] LU/inverse check, [2] FP32 pipeline or near-list error, [3] near-pair count
+  // step replay by a CUDA graph: the step counter on the device and the
+  // frame of the step being computed (filled by launch_step_begin)
+  int* devIter;
+  double* curFrame;
+  int* err;  // [0] LU/inverse check, [1] refinement residual, [2] FP32 pipeline or near-list error, [3] near-pair count
 };
 
 // ---- wake bookkeeping (src/classdef.f90:4297-4605, 1515-1702, 4786-4830) ----
@@ -130,9 +138,34 @@ void launch_scatter_nodes(const Dims& d, const DevState& s, const double* frame,
 void launch_aic(const Dims& d, const DevState& s, const double* frame, cudaStream_t st);
 void launch_lu_inverse(const Dims& d, const DevState& s, cudaStream_t st);
 void launch_is_inverse(const Dims& d, const DevState& s, cudaStream_t st);
+// FP32 LU with partial pivoting of the AIC and its FP32 inverse (solves then
+// refine in FP64: launch_solve uses them when s.LU32 is set)
+void launch_lu32(const Dims& d, const DevState& s, cudaStream_t st);
 // velCP = velKin (+ wake velocity in outv if withWake); RHS; gamVec = AICinv RHS; map to wing gam
 void launch_solve(const Dims& d, const DevState& s, const double* frame, bool withWake, cudaStream_t st);
+// start of a replayed step: devIter += 1, curFrame = frame[devIter]
+void launch_step_begin(const Dims& d, const DevState& s, cudaStream_t st);
 // velCPTotal, sectional resultant velocity, lift direction, forces, CT row
+// (iter < 0: the row of the device step counter)
 void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st);
+
+// ---- learned far-wake surrogate (surrogate.cu) ------------------------------
+// targets: the convecting blades' CPs, then nNodes inner-wake nodes (every
+// stride-th from offset; per blade the near-wake nodes of rows rowNear..NW
+// and the `young` youngest far-wake nodes)
+void launch_surr_targets(const Dims& d, const DevState& s, const double* fr, int rowNear, int rowFar, int young,
+                         int stride, int offset, int nNodes, double* P, cudaStream_t st);
+// old far-wake nodes (all but the `young` youngest) of the convecting blades
+void launch_surr_far_targets(const Dims& d, const DevState& s, int rowFar, int young, bool pred, double* P,
+                             cudaStream_t st);
+// 8 FP32 features per target (position about the hub / R, rotor azimuth
+// harmonics, far-wake fill fraction)
+void launch_surr_features(const Dims& d, const double* fr, const double* P, int M, double invR, double fill, float* X,
+                          cudaStream_t st);
+void launch_surr_add(int M, const float* Y, const double* scale, double* outv, cudaStream_t st);
+void launch_surr_merge_nodes(const Dims& d, int rowNear, int rowFar, int young, int M, const float* Y,
+                             const double* scale, const double* outFar, double* outv, cudaStream_t st);
+void launch_surr_append(int n, const float* Xs, const double* V, float* X, float* T, cudaStream_t st);
+void launch_surr_audit(int n, const float* Y, const double* scale, const double* V, double* out, cudaStream_t st);
 
 }  // namespace vlm

@@ -35,11 +35,27 @@ class VlmError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("sum_chunk", ctypes.c_int), ("near_factor", ctypes.c_double),
-                ("device", ctypes.c_int), ("use_graph", ctypes.c_int)]
+                ("device", ctypes.c_int), ("use_graph", ctypes.c_int), ("solve_mode", ctypes.c_int),
+                ("nbody_slots", ctypes.c_int)]
+
+
+class SurrogateOptions(ctypes.Structure):
+    _fields_ = [("enable", ctypes.c_int), ("young_far", ctypes.c_int), ("min_far", ctypes.c_int),
+                ("collect_steps", ctypes.c_int),
+                ("sample_stride", ctypes.c_int), ("train_iters", ctypes.c_int), ("batch", ctypes.c_int),
+                ("lr", ctypes.c_float), ("audit_samples", ctypes.c_int), ("audit_tol", ctypes.c_double),
+                ("hidden", ctypes.c_int), ("layers", ctypes.c_int), ("seed", ctypes.c_uint64)]
+
+
+class SurrogateStats(ctypes.Structure):
+    _fields_ = [("phase", ctypes.c_int), ("trainings", ctypes.c_int), ("audits", ctypes.c_int),
+                ("reverts", ctypes.c_int), ("active_steps", ctypes.c_int), ("samples", ctypes.c_int64),
+                ("last_audit_err", ctypes.c_double), ("max_audit_err", ctypes.c_double), ("last_loss", ctypes.c_float)]
 
 
 # exported symbols and their signatures (include/vlm.h)
 _dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
 _i64 = ctypes.c_int64
 _vp = ctypes.c_void_p
 SIGNATURES = {
@@ -65,6 +81,24 @@ SIGNATURES = {
     "vlm_case_vind_points": (ctypes.c_int, [_vp, _dp, _i64, _dp]),
     "vlm_case_last_step_ms": (ctypes.c_int, [_vp, _dp]),
     "vlm_case_profile_eval": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "vlm_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
+                                        ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
+    "vlm_batch_destroy": (ctypes.c_int, [_vp]),
+    "vlm_batch_case": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "vlm_batch_start": (ctypes.c_int, [_vp]),
+    "vlm_batch_step": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "vlm_batch_last_step_ms": (ctypes.c_int, [_vp, _dp]),
+    "vlm_default_surrogate_options": (None, [ctypes.POINTER(SurrogateOptions)]),
+    "vlm_case_set_surrogate": (ctypes.c_int, [_vp, ctypes.POINTER(SurrogateOptions)]),
+    "vlm_case_surrogate_stats": (ctypes.c_int, [_vp, ctypes.POINTER(SurrogateStats)]),
+    "vlm_mlp_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_vp)]),
+    "vlm_mlp_destroy": (ctypes.c_int, [_vp]),
+    "vlm_mlp_param_count": (_i64, [_vp]),
+    "vlm_mlp_get_params": (ctypes.c_int, [_vp, _fp]),
+    "vlm_mlp_set_params": (ctypes.c_int, [_vp, _fp]),
+    "vlm_mlp_forward": (ctypes.c_int, [_vp, _fp, _i64, _fp]),
+    "vlm_mlp_gradient": (ctypes.c_int, [_vp, _fp, _fp, _i64, _fp, _fp]),
+    "vlm_mlp_train": (ctypes.c_int, [_vp, _fp, _fp, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_float, _fp]),
 }
 
 _lib = None
@@ -107,7 +141,7 @@ def _c64(a) -> np.ndarray:
 
 
 def options(precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
-            device: int = 0, use_graph: bool = True) -> Options:
+            device: int = 0, use_graph: bool = True, solve_mode: Optional[int] = None) -> Options:
     o = Options()
     load().vlm_default_options(ctypes.byref(o))
     o.precision = precision
@@ -117,6 +151,8 @@ def options(precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_fa
         o.near_factor = near_factor
     o.device = device
     o.use_graph = int(use_graph)
+    if solve_mode is not None:
+        o.solve_mode = solve_mode
     return o
 
 
@@ -170,10 +206,12 @@ class Case:
     """One rotor case on the GPU: the reference's rotor object + time loop."""
 
     def __init__(self, config_text: str, geom_text: str, base_dir: str | os.PathLike = "",
-                 precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None):
+                 precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
+                 solve_mode: Optional[int] = None, use_graph: bool = True, nbody_slots: int = 0):
         L = load()
         self._h = _vp()
-        self.opt = options(precision, sum_chunk, near_factor)
+        self.opt = options(precision, sum_chunk, near_factor, use_graph=use_graph, solve_mode=solve_mode)
+        self.opt.nbody_slots = nbody_slots
         _err(L.vlm_case_create(config_text.encode(), geom_text.encode(), str(base_dir).encode(),
                                ctypes.byref(self.opt), ctypes.byref(self._h)))
 
@@ -215,6 +253,20 @@ class Case:
         L.vlm_case_get(self._h, name.encode(), blade, _ptr(out), n)
         return out[:n]
 
+    def set_surrogate(self, **kw) -> None:
+        """Enable the learned far-wake surrogate (before start); keywords
+        override the defaults of vlm_surrogate_options."""
+        o = SurrogateOptions()
+        load().vlm_default_surrogate_options(ctypes.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        _err(load().vlm_case_set_surrogate(self._h, ctypes.byref(o)))
+
+    def surrogate_stats(self) -> dict:
+        st = SurrogateStats()
+        _err(load().vlm_case_surrogate_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
     def ct_hist(self) -> np.ndarray:
         return self.get("ct_hist").reshape(-1, 10)
 
@@ -234,3 +286,124 @@ class Case:
         ms = ctypes.c_double()
         _err(load().vlm_case_last_step_ms(self._h, ctypes.byref(ms)))
         return ms.value
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(_fp)
+
+
+class Mlp:
+    """The surrogate's FP32 MLP (tanh hidden layers, linear output) on the GPU:
+    forward, MSE gradient and Adam training by the library's own kernels."""
+
+    def __init__(self, sizes, seed: int = 0):
+        arr = (ctypes.c_int * len(sizes))(*sizes)
+        self.sizes = list(sizes)
+        self._h = _vp()
+        _err(load().vlm_mlp_create(arr, len(sizes), seed, ctypes.byref(self._h)))
+
+    @property
+    def nparam(self) -> int:
+        return int(load().vlm_mlp_param_count(self._h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.nparam, dtype=np.float32)
+        _err(load().vlm_mlp_get_params(self._h, _fptr(out)))
+        return out
+
+    def set_params(self, p) -> None:
+        p = _f32(p)
+        assert p.size == self.nparam
+        _err(load().vlm_mlp_set_params(self._h, _fptr(p)))
+
+    def forward(self, X) -> np.ndarray:
+        X = _f32(X).reshape(-1, self.sizes[0])
+        Y = np.zeros((X.shape[0], self.sizes[-1]), dtype=np.float32)
+        _err(load().vlm_mlp_forward(self._h, _fptr(X), X.shape[0], _fptr(Y)))
+        return Y
+
+    def gradient(self, X, T):
+        X = _f32(X).reshape(-1, self.sizes[0])
+        T = _f32(T).reshape(-1, self.sizes[-1])
+        g = np.zeros(self.nparam, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _err(load().vlm_mlp_gradient(self._h, _fptr(X), _fptr(T), X.shape[0], _fptr(g), _fptr(loss)))
+        return g, float(loss[0])
+
+    def train(self, X, T, batch: int, iters: int, lr: float) -> float:
+        X = _f32(X).reshape(-1, self.sizes[0])
+        T = _f32(T).reshape(-1, self.sizes[-1])
+        loss = np.zeros(1, dtype=np.float32)
+        _err(load().vlm_mlp_train(self._h, _fptr(X), _fptr(T), X.shape[0], batch, iters, lr, _fptr(loss)))
+        return float(loss[0])
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().vlm_mlp_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _BorrowedCase(Case):
+    """A case owned by a batch (getters only)."""
+
+    def __init__(self, handle, batch):
+        self._h = handle
+        self._batch = batch  # keeps the batch alive
+
+    def close(self):
+        self._h = _vp()
+
+
+class Batch:
+    """Many independent cases advanced together (one graph launch per step in
+    steady state); cases = [(config_text, geom_text, base_dir), ...]."""
+
+    def __init__(self, cases, precision: int = PREC_FP64, sum_chunk: Optional[int] = None,
+                 nbody_slots: int = 0, use_graph: bool = True):
+        n = len(cases)
+        enc = lambda i: (ctypes.c_char_p * n)(*[str(c[i]).encode() for c in cases])
+        self._cfg, self._geo, self._dir = enc(0), enc(1), enc(2)
+        self.opt = options(precision, sum_chunk, use_graph=use_graph)
+        self.opt.nbody_slots = nbody_slots
+        self.n = n
+        self._h = _vp()
+        _err(load().vlm_batch_create(n, self._cfg, self._geo, self._dir, ctypes.byref(self.opt), ctypes.byref(self._h)))
+
+    def case(self, i: int) -> Case:
+        h = _vp()
+        _err(load().vlm_batch_case(self._h, i, ctypes.byref(h)))
+        return _BorrowedCase(h, self)
+
+    def start(self):
+        _err(load().vlm_batch_start(self._h))
+
+    def step(self, n: int = 1, with_ct: bool = True) -> Optional[np.ndarray]:
+        rows = np.zeros((self.n, n, 10)) if with_ct else None
+        _err(load().vlm_batch_step(self._h, n, _ptr(rows) if with_ct else None))
+        return rows
+
+    def last_step_ms(self) -> float:
+        ms = ctypes.c_double()
+        _err(load().vlm_batch_last_step_ms(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().vlm_batch_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
