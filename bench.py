@@ -339,11 +339,15 @@ def run_ours(args):
     }
     out["pairs_per_s"] = round(rp / (ms_l / 1e3), 1)
     if not args.no_kernel:
-        kp = {"fp32near": lib.PREC_FP32_NEAR64, "fp32": lib.PREC_FP32, "fp64": lib.PREC_FP32_NEAR64}[args.precision]
-        k3 = run_kernel_cfg3(kp, reps=args.kernel_reps)
-        k3["frac_of_fp32_peak"] = round(k3["tflops"] / fp32_peak, 4)
-        k3["workload"] = "isolated kernel: 2^20 targets x 2^18 rings (U[0,1]^3, edges U(0.005,0.05), core 0.002)"
-        out["kernel_rings"] = k3
+        # the isolated N-body kernel in both FP32 forms (the FP64 form runs
+        # ~60x slower on this part: see the bench's fp64 precision)
+        for key, kp in (("kernel_rings", lib.PREC_FP32), ("kernel_rings_near64", lib.PREC_FP32_NEAR64)):
+            k3 = run_kernel_cfg3(kp, reps=args.kernel_reps)
+            k3["frac_of_fp32_peak"] = round(k3["tflops"] / fp32_peak, 4)
+            k3["precision"] = "fp32" if kp == lib.PREC_FP32 else "fp32near"
+            k3["workload"] = ("isolated kernel: 2^20 targets x 2^18 rings (U[0,1]^3, edges U(0.005,0.05), "
+                              "core 0.002)")
+            out[key] = k3
     if rank == 0 and not args.no_cpu:
         try:
             rate, threads, desc = cpu_sample(case, seconds=args.cpu_seconds)
@@ -451,6 +455,122 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_batch(args):
+    """Batched sweep: 256 independent uneven rotor cases (volcanor_gb300/cases.py
+    batch_sweep) advanced together; after every case reached its steady state
+    each batch step is one CUDA-graph launch.  Reports case-timesteps/s."""
+    from volcanor_gb300 import lib
+    prec = {"fp32near": lib.PREC_FP32_NEAR64, "fp32": lib.PREC_FP32, "fp64": lib.PREC_FP64}[args.precision]
+    K, W = args.steps, args.warmup
+    n = args.batch_cases
+    steady = 8 * 72 + 2
+    cases = C.batch_sweep(n, seed=0, nt=steady + W + 2 * K)
+    t0 = time.perf_counter()
+    b = lib.Batch([(c.config, c.geom, "") for c in cases], precision=prec)
+    b.start()
+    done = 0
+    while done < steady + W:
+        m = min(50, steady + W - done)
+        b.step(m, with_ct=False)
+        done += m
+    warm_s = time.perf_counter() - t0
+    l0 = lib.launch_count()
+    with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
+        rows = b.step(K)
+        ms = b.last_step_ms()
+    launches = lib.launch_count() - l0
+    value = n * K / (ms / 1e3)
+    # e2e: single batch steps through the public API (frames in, CT rows out)
+    t1 = time.perf_counter()
+    for _ in range(K):
+        b.step(1)
+    e2e = n * K / (time.perf_counter() - t1)
+    out = {"metric": "batched free-wake case-timesteps/s", "value": round(value, 2), "unit": "case-timesteps/s",
+           "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+           "data": "synthetic (256 seeded uneven rotor cases, volcanor_gb300/cases.py batch_sweep)",
+           "config": {"workload": f"{n} independent rotor cases: 2-4 blades, 24-400 rings, collective 2-12 deg, "
+                                  "advance ratio 0-0.3, wakes of 1-8 revolutions (5k-120k filaments), steady state, "
+                                  "one CUDA-graph launch per batch step", "precision": args.precision},
+           "e2e": {"value": round(e2e, 2), "unit": "case-timesteps/s",
+                   "h2d_bytes_per_step": None, "d2h_bytes_per_step": n * 80},
+           "gpu_launches": int(launches), "graph_launches_per_step": 1,
+           "warmup_wall_s": round(warm_s, 1), "clocks": clk.summary(),
+           "ct_finite": bool(np.all(np.isfinite(rows)))}
+    print(json.dumps(out))
+
+
+def run_forward4(args):
+    """4-blade rotor in forward flight (R = 2 m, c = 0.12 m, -8 deg twist,
+    theta0 = 10 deg, mu = 0.1, shaft tilt -4 deg, 1 x 32 rings per blade,
+    dt = 5 deg, 1 rev of near wake, untruncated far wake): timesteps/s of the
+    plain FP64 form and of the FP32 forms (with the learned surrogate of the
+    far wake older than 4 revs, and batched as 8 copies) over the same step
+    window, after the same number of steps from the start."""
+    import tempfile
+    from volcanor_gb300 import lib
+    K, W = args.steps, args.warmup
+    S = args.forward_step
+    nt = S + W + K
+
+    def make(prec, surr=None):
+        c = C.rotor_4blade_forward(nt=nt)
+        with tempfile.TemporaryDirectory() as d:
+            c.write(d)
+            g = lib.Case.from_case_dir(d, precision=prec)
+        if surr is not None:
+            g.set_surrogate(**surr)
+        g.start()
+        return g
+
+    def advance(g, n):
+        done = 0
+        while done < n:
+            m = min(100, n - done)
+            g.step(m, with_ct=False)
+            done += m
+
+    res = {}
+    for name, prec, surr in (("fp64", lib.PREC_FP64, None), ("fp32near", lib.PREC_FP32_NEAR64, None),
+                             ("fp32near_surrogate", lib.PREC_FP32_NEAR64, {})):
+        g = make(prec, surr)
+        advance(g, S + W)
+        rows = g.step(K)
+        ms = g.last_step_ms()
+        res[name] = {"timesteps_per_s": round(K / (ms / 1e3), 3), "ms_per_step": round(ms / K, 3),
+                     "ct_last": float(rows[-1, 1])}
+        if surr is not None:
+            res[name]["surrogate"] = g.surrogate_stats()
+        g.close()
+    # batched: 8 copies in one batch (one launch per step is for steady wakes;
+    # this wake grows every step, so each batch step enqueues every case)
+    c = C.rotor_4blade_forward(nt=nt)
+    with tempfile.TemporaryDirectory() as d:
+        c.write(d)
+        b = lib.Batch([(c.config, c.geom, d)] * 8, precision=lib.PREC_FP32_NEAR64)
+        b.start()
+    done = 0
+    while done < S + W:
+        m = min(100, S + W - done)
+        b.step(m, with_ct=False)
+        done += m
+    b.step(K, with_ct=False)
+    ms = b.last_step_ms()
+    res["fp32near_batched_x8"] = {"case_timesteps_per_s": round(8 * K / (ms / 1e3), 3)}
+    base = res["fp64"]["timesteps_per_s"]
+    out = {"metric": "free-wake timesteps/s, 4-blade forward-flight rotor", "unit": "timesteps/s",
+           "value": res["fp32near_surrogate"]["timesteps_per_s"], "n_gpus": 1, "steps": K, "warmup": W,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32near",
+           "data": "synthetic (case files generated by volcanor_gb300/cases.py rotor_4blade_forward)",
+           "config": {"workload": f"4-blade forward flight, steps {S + W + 1}..{S + W + K} of an untruncated wake",
+                      "surrogate": "far wake older than 4 revs (young_far 216) by a 4 x 128 tanh MLP, audited "
+                                   "every step against the direct FP64 sum (tolerance 0.1 rms)"},
+           "forms": res,
+           "speedup_vs_fp64": {k: round((v.get("timesteps_per_s") or v.get("case_timesteps_per_s")) / base, 1)
+                               for k, v in res.items()}}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -465,6 +585,10 @@ def main():
     ap.add_argument("--kernel-only", action="store_true",
                     help="only the isolated ring kernel (for profiling); prints its JSON")
     ap.add_argument("--kernel-m", type=int, default=1 << 20)
+    ap.add_argument("--forward-step", type=int, default=720)
+    ap.add_argument("--workload", default="hover2", choices=["hover2", "batch", "forward4"],
+                    help="hover2: the headline 2-blade hover case; batch: 256 uneven cases in one graph launch")
+    ap.add_argument("--batch-cases", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -475,6 +599,10 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "forward4":
+        run_forward4(args)
     else:
         run_ours(args)
 

@@ -187,3 +187,35 @@ def rotor_4blade_forward(nt: int = 2880, n_nwake: int = 72, omega: float = 100.0
                     wakeTruncateNt=truncate_nt, symmetricTau=0, pivotLE=0.25)
     return Case("rotor_4blade_forward", cfg, geo,
                 files={"blade.xyz": plot3d_twisted_blade(nc, ns, radius, chord, 0.2, -8.0)})
+
+
+def batch_sweep(n: int = 256, seed: int = 0, nt: Optional[int] = None) -> list:
+    """Independent uneven rotor cases for the batched launch: per case (seeded)
+    2-4 blades with 24-400 rings in all (1 chordwise row), R = 1-2 m,
+    c = 0.08 R, collective U(2, 12) deg, advance ratio U(0, 0.3), Omega =
+    100 rad/s, dt = 5 deg, one revolution of near-wake sheet and a far wake
+    truncated after 1-8 revolutions (uneven filament counts of about 5k to
+    120k), viscous core growth on.  Returns [Case, ...]; nt defaults to
+    8 revolutions plus 36 steps (every case then in its steady state)."""
+    import random
+
+    rng = random.Random(seed)
+    nt = nt if nt is not None else 8 * 72 + 36
+    out = []
+    for i in range(n):
+        nb = rng.choice((2, 3, 4))
+        rings = rng.randint(24, 400)
+        ns = max(8, min(100, round(rings / nb)))
+        radius = rng.uniform(1.0, 2.0)
+        revs = rng.randint(1, 8)
+        theta0 = rng.uniform(2.0, 12.0)
+        mu = rng.uniform(0.0, 0.3)
+        omega = 100.0
+        cfg = config_text(nt=nt, dt=0.0, density=1.2, kinematicVisc=1.5e-5, fdScheme=3, wakeDissipation=1)
+        geo = geom_text(nb=nb, nc=1, ns=ns, nNwake=72, span=radius, rootcut=0.2, chord=0.08 * radius,
+                        Omega=omega, shaftAxis=(0.0, 0.0, 1.0), theta0=theta0,
+                        velBody=(-mu * omega * radius, 0.0, 0.0), spanSpacing=1, chordSpacing=1,
+                        spanwiseCore=0.05, streamwiseCoreVec=0.05, apparentViscCoeff=5.0,
+                        wakeTruncateNt=72 * revs + (72 if revs == 1 else 0), symmetricTau=0, pivotLE=0.25)
+        out.append(Case(f"sweep_{i:03d}", cfg, geo))
+    return out

@@ -79,10 +79,32 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// Appends one list entry per near filament (bits of msk) of this warp's
-// lanes: a warp prefix sum of the bit counts, one atomic per warp.
+// Near-list entries are staged per warp in shared memory and written to the
+// global list in batches, one atomic per batch (a single global counter
+// shared by every warp would otherwise put its latency on every append).
+constexpr int kNearStage = 128;  // entries staged per warp
+
+// Writes the warp's staged entries to the global list.
+__device__ __forceinline__ void near_flush(NearPair* __restrict__ stage, int& staged, int lane, int* __restrict__ ctl,
+                                           NearPair* __restrict__ near, int near_cap) {
+  if (staged == 0) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(ctl + 1, staged);
+  base = __shfl_sync(kFull, base, 0);
+  __syncwarp();
+  for (int i = lane; i < staged; i += 32) {
+    if (base + i < near_cap) near[base + i] = stage[i];
+    else atomicExch(ctl, 3);
+  }
+  __syncwarp();
+  staged = 0;
+}
+
+// Appends one entry per near filament (bits of msk) of this warp's lanes:
+// a warp prefix sum of the bit counts places them in the warp's stage.
 __device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec, int lane, int* __restrict__ ctl,
-                                            NearPair* __restrict__ near, int near_cap) {
+                                            NearPair* __restrict__ near, int near_cap, NearPair* __restrict__ stage,
+                                            int& staged) {
   const int cnt = __popc(msk);
   int incl = cnt;
 #pragma unroll
@@ -92,22 +114,38 @@ __device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec,
   }
   const int total = __shfl_sync(kFull, incl, 31);
   if (total == 0) return;
-  int base = 0;
-  if (lane == 0) base = atomicAdd(ctl + 1, total);
-  base = __shfl_sync(kFull, base, 0);
-  int slot = base + incl - cnt;
-  for (unsigned b = msk; b; b &= b - 1u, ++slot) {
-    if (slot < near_cap) {
-      NearPair np;
-      np.m = m;
-      np.q = q;
-      np.rec = rec;
-      np.k = __ffs(b) - 1;
-      near[slot] = np;
-    } else {
-      atomicExch(ctl, 3);
+  if (staged + total > kNearStage) near_flush(stage, staged, lane, ctl, near, near_cap);
+  if (total > kNearStage) {
+    // more than a stage holds (at most 32 lanes x 4 filaments): straight out
+    int base = 0;
+    if (lane == 0) base = atomicAdd(ctl + 1, total);
+    base = __shfl_sync(kFull, base, 0);
+    int slot = base + incl - cnt;
+    for (unsigned b = msk; b; b &= b - 1u, ++slot) {
+      if (slot < near_cap) {
+        NearPair np;
+        np.m = m;
+        np.q = q;
+        np.rec = rec;
+        np.k = __ffs(b) - 1;
+        near[slot] = np;
+      } else {
+        atomicExch(ctl, 3);
+      }
     }
+    return;
   }
+  int slot = staged + incl - cnt;
+  for (unsigned b = msk; b; b &= b - 1u, ++slot) {
+    NearPair np;
+    np.m = m;
+    np.q = q;
+    np.rec = rec;
+    np.k = __ffs(b) - 1;
+    stage[slot] = np;
+  }
+  __syncwarp();
+  staged += total;
 }
 
 // Adds the FP32 velocity of one record at one target (corner vectors r_k and
@@ -208,13 +246,18 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   }
 
   // ---- consumers ----
+  __shared__ NearPair nstage_all[NEAR ? kConsumerWarps * kNearStage : 1];
+  NearPair* nstage = nstage_all + (NEAR ? warp * kNearStage : 0);
+  int staged = 0;
   int mt[kTPT];
   bool valid[kTPT];
   float px[kTPT], py[kTPT], pz[kTPT];
   double acc64[kTPT][3];
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
-    mt[u] = (blockIdx.x * kTPT + u) * kThreads32 + tid;
+    // a warp's targets are 64 consecutive ones (two runs of 32), so that a
+    // spatially ordered target list gives each warp a compact patch
+    mt[u] = blockIdx.x * kTargetsPerBlock32 + warp * (32 * kTPT) + u * 32 + lane;
     valid[u] = mt[u] < M;
     const int mm = valid[u] ? mt[u] : M - 1;
     px[u] = (float)P[3 * (size_t)mm];
@@ -264,7 +307,7 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) {
             unsigned msk = ring_fp32<true>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
-            near_append(valid[u] ? msk : 0u, mt[u], q, rec, lane, ctl, near, near_cap);
+            near_append(valid[u] ? msk : 0u, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
           }
         } else {
 #pragma unroll
@@ -281,6 +324,7 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
+  if (NEAR) near_flush(nstage, staged, lane, ctl, near, near_cap);
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
     if (valid[u]) {

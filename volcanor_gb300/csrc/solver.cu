@@ -434,6 +434,7 @@ __global__ void k_order2(Dims d, DevState s, int rowNear, int rowFar, int phase)
 }
 
 // ---- targets ----------------------------------------------------------------
+constexpr int kTileRows = 16, kTileCols = 4;
 __device__ __forceinline__ void decode_node(const Dims& d, int rowNear, int rowFar, int m, int& b, int& far, int& i,
                                             int& j) {
   const int rowsN = d.NW - (rowNear - 1);
@@ -442,12 +443,17 @@ __device__ __forceinline__ void decode_node(const Dims& d, int rowNear, int rowF
   b = m / per;
   const int l = m % per;
   if (l < rowsN * (d.ns + 1)) {
-    // span station fastest: a warp's consecutive targets are a compact strip
-    // of the wake sheet (a few rows across the span), not a helix turn of one
-    // station, so few source rings come near any of them
+    // tiles of kTileRows rows x kTileCols span stations, tile by tile: the 64
+    // consecutive targets of a warp of the FP32 kernel are a compact patch of
+    // the wake sheet, so few source rings come near any of them
     far = 0;
-    j = l % (d.ns + 1);
-    i = rowNear - 1 + l / (d.ns + 1);
+    const int band = l / (kTileRows * (d.ns + 1));
+    const int br = min(kTileRows, rowsN - band * kTileRows);
+    const int o = l - band * kTileRows * (d.ns + 1);
+    const int tc = o / (br * kTileCols);
+    const int q = o - tc * br * kTileCols;
+    i = rowNear - 1 + band * kTileRows + q % br;
+    j = tc * kTileCols + q / br;
   } else {
     far = 1;
     j = 0;
