@@ -100,52 +100,52 @@ __device__ __forceinline__ void near_flush(NearPair* __restrict__ stage, int& st
   staged = 0;
 }
 
-// Appends one entry per near filament (bits of msk) of this warp's lanes:
-// a warp prefix sum of the bit counts places them in the warp's stage.
+// Appends one entry per near filament (bits of msk, at most 4) of this
+// warp's lanes.  Slots come from one ballot per filament index, no shuffles:
+// filament k of lane l goes to P_k + popc(ballot_k & lanes below l), P_k the
+// entries of the filament indices below k.
 __device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec, int lane, int* __restrict__ ctl,
                                             NearPair* __restrict__ near, int near_cap, NearPair* __restrict__ stage,
                                             int& staged) {
-  const int cnt = __popc(msk);
-  int incl = cnt;
+  if (!__ballot_sync(kFull, msk != 0u)) return;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned bk[4];
+  int pk[4], total = 0;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int v = __shfl_up_sync(kFull, incl, o);
-    if (lane >= o) incl += v;
+  for (int k = 0; k < 4; ++k) {
+    bk[k] = __ballot_sync(kFull, (msk >> k) & 1u);
+    pk[k] = total;
+    total += __popc(bk[k]);
   }
-  const int total = __shfl_sync(kFull, incl, 31);
-  if (total == 0) return;
-  if (staged + total > kNearStage) near_flush(stage, staged, lane, ctl, near, near_cap);
-  if (total > kNearStage) {
-    // more than a stage holds (at most 32 lanes x 4 filaments): straight out
-    int base = 0;
-    if (lane == 0) base = atomicAdd(ctl + 1, total);
-    base = __shfl_sync(kFull, base, 0);
-    int slot = base + incl - cnt;
-    for (unsigned b = msk; b; b &= b - 1u, ++slot) {
-      if (slot < near_cap) {
-        NearPair np;
-        np.m = m;
-        np.q = q;
-        np.rec = rec;
-        np.k = __ffs(b) - 1;
-        near[slot] = np;
-      } else {
-        atomicExch(ctl, 3);
-      }
+  int base;
+  NearPair* dst;
+  if (total <= kNearStage) {
+    if (staged + total > kNearStage) near_flush(stage, staged, lane, ctl, near, near_cap);
+    base = staged;
+    dst = stage;
+  } else {
+    // more than a stage holds (up to 32 lanes x 4 filaments): straight out
+    int b0 = 0;
+    if (lane == 0) b0 = atomicAdd(ctl + 1, total);
+    base = __shfl_sync(kFull, b0, 0);
+    dst = nullptr;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if ((msk >> k) & 1u) {
+      const int slot = base + pk[k] + __popc(bk[k] & lt);
+      NearPair np;
+      np.m = m;
+      np.q = q;
+      np.rec = rec;
+      np.k = k;
+      if (dst) dst[slot] = np;
+      else if (slot < near_cap) near[slot] = np;
+      else atomicExch(ctl, 3);
     }
-    return;
-  }
-  int slot = staged + incl - cnt;
-  for (unsigned b = msk; b; b &= b - 1u, ++slot) {
-    NearPair np;
-    np.m = m;
-    np.q = q;
-    np.rec = rec;
-    np.k = __ffs(b) - 1;
-    stage[slot] = np;
   }
   __syncwarp();
-  staged += total;
+  if (dst) staged += total;
 }
 
 // Adds the FP32 velocity of one record at one target (corner vectors r_k and
