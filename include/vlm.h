@@ -154,6 +154,16 @@ int64_t vlm_case_get(vlm_case* c, const char* name, int blade, double* out, int6
 /* Induced velocity of the current wing + wake at M points (probes / gridgen:
  * src/libPostprocess.f90:333-361, src/gridgen.f90:115-140). */
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V);
+/* Checkpoint / resume: replaces the reference's restart files
+ * (Restart/restartNNNNN.dat written every restartWriteNt steps and read for
+ * restartFromNt, src/main.f90:389-397,1443-1450).  save writes the case's
+ * whole solver state (step counter, circulations, wake, loads history, AIC
+ * factors) to a binary file; load restores it into a case created from the
+ * same case files and options (started or not), which then continues
+ * bit-identically.  A different case, options or format -> VLM_ERR_INVALID.
+ * Not available with the surrogate (VLM_ERR_UNSUPPORTED). */
+int vlm_case_checkpoint_save(vlm_case* c, const char* path);
+int vlm_case_checkpoint_load(vlm_case* c, const char* path);
 /* Device time of the kernels of the last vlm_case_step call, milliseconds
  * (CUDA events after the call's input upload). */
 int vlm_case_last_step_ms(vlm_case* c, double* ms);

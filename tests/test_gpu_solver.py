@@ -155,3 +155,27 @@ def test_errors_and_state_checks():
         g.step(100)  # past nt
     with pytest.raises(lib.VlmError):
         lib.Case(cfg.replace("fdScheme = 3", "fdScheme = 9"), geo)
+
+
+@pytest.mark.parametrize("prec", [lib.PREC_FP64, lib.PREC_FP32_NEAR64])
+def test_checkpoint_resume_is_bit_identical(prec, tmp_path):
+    """Save after 25 steps, continue 30; a fresh case loaded from the file
+    continues the same 30 steps bit for bit (the reference's restart files)."""
+    c = C.rotor_2blade_hover(nt=60, n_nwake=20, truncate_nt=30)
+    a = lib.Case(c.config, c.geom, precision=prec)
+    a.start()
+    a.step(25)
+    ck = tmp_path / "ck.bin"
+    a.checkpoint_save(ck)
+    ra = a.step(30)
+    b = lib.Case(c.config, c.geom, precision=prec)
+    b.checkpoint_load(ck)
+    assert b.geti("iter") == 25
+    rb = b.step(30)
+    assert np.array_equal(ra, rb)
+    assert np.array_equal(a.get("waN", 2), b.get("waN", 2))
+    # a checkpoint of another case is refused
+    other = C.rotor_2blade_hover(nt=60, n_nwake=21, truncate_nt=30)
+    o = lib.Case(other.config, other.geom, precision=prec)
+    with pytest.raises(lib.VlmError):
+        o.checkpoint_load(ck)

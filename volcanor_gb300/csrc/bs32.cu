@@ -37,7 +37,6 @@ namespace vlm {
 
 namespace {
 
-constexpr int kThreads32 = 256;
 constexpr int kTPT = 2;         // targets per thread
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr float kS2Min = 1e-30f;
@@ -379,6 +378,9 @@ __global__ void k_near_apply(double* __restrict__ part, long long* __restrict__ 
   }
 }
 
+// FP64 record -> FP32 record.  The edge vectors are differenced in FP64
+// (nearby corners cancel) and rounded once; everything else is FP32 (the
+// record is FP32; GB300's FP64 rate would make this kernel latency-bound).
 __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near_factor, float* __restrict__ rec32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrec) return;
@@ -387,56 +389,57 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
   const int flags = (int)R[17];
   const double g = R[16];
   const bool skipped = (flags & REC_SKIP) && !(fabs(g) > kEps);
-  d3 c[4];
-  double rv[4];
-  bool act[4];
-  if (flags & REC_FIL) {
-    c[0] = mk3(R[0], R[1], R[2]);
-    c[1] = mk3(R[3], R[4], R[5]);
-    c[2] = c[1];
-    c[3] = c[0];
-    rv[0] = R[12];
-    rv[1] = rv[2] = rv[3] = 0.0;
-    act[0] = true;
-    act[1] = act[2] = act[3] = false;
-  } else {
-    for (int k = 0; k < 4; ++k) {
-      c[k] = mk3(R[3 * k], R[3 * k + 1], R[3 * k + 2]);
-      rv[k] = R[12 + k];
-      act[k] = true;
-    }
+  const bool fil = flags & REC_FIL;
+  // corner k (FP64) and core radius of filament k
+  double cx[4], cy[4], cz[4];
+  float rv[4];
+  for (int k = 0; k < 4; ++k) {
+    const int src = fil ? (k == 1 || k == 2 ? 1 : 0) : k;
+    cx[k] = R[3 * src];
+    cy[k] = R[3 * src + 1];
+    cz[k] = R[3 * src + 2];
+    rv[k] = fil ? (k == 0 ? (float)R[12] : 0.f) : (float)R[12 + k];
   }
-  const double w = g * kInv4Pi;
-  double reach = 0.0;
+  const float nf = (float)near_factor;
+  const float w = (float)(g * kInv4Pi);
+  float reach = 0.f;
   bool anyNear = false;
   for (int k = 0; k < 4; ++k) {
-    const d3 e = c[(k + 1) & 3] - c[k];
-    const double ee = dot3(e, e);
-    const double s = rv[k] * sqrt(ee);
-    o[3 * k] = (float)c[k].x;
-    o[3 * k + 1] = (float)c[k].y;
-    o[3 * k + 2] = (float)c[k].z;
-    const double wk = (act[k] && !skipped) ? w : 0.0;
-    o[12 + 3 * k] = (float)(wk * e.x);
-    o[12 + 3 * k + 1] = (float)(wk * e.y);
-    o[12 + 3 * k + 2] = (float)(wk * e.z);
-    o[24 + k] = (float)(wk * ee);
-    o[28 + k] = (float)fmax(pow4(s), 1e-36);
-    const bool on = act[k] && !skipped && near_factor > 0.0;
-    const double nfs = near_factor * s;
-    o[32 + k] = on ? (float)(nfs * nfs) : -1.f;
+    const int j = (k + 1) & 3;
+    const bool act = (!fil || k == 0) && !skipped;
+    const float ex = (float)(cx[j] - cx[k]), ey = (float)(cy[j] - cy[k]), ez = (float)(cz[j] - cz[k]);
+    const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    const float sk = rv[k] * sqrtf(ee);
+    const float s2 = sk * sk;
+    o[3 * k] = (float)cx[k];
+    o[3 * k + 1] = (float)cy[k];
+    o[3 * k + 2] = (float)cz[k];
+    const float wk = act ? w : 0.f;
+    o[12 + 3 * k] = wk * ex;
+    o[12 + 3 * k + 1] = wk * ey;
+    o[12 + 3 * k + 2] = wk * ez;
+    o[24 + k] = wk * ee;
+    o[28 + k] = fmaxf(s2 * s2, 1e-36f);
+    const bool on = act && nf > 0.f;
+    const float nfs = nf * sk;
+    o[32 + k] = on ? nfs * nfs : -1.f;
     // -s < e.r1 < |e|^2 + s, multiplied by w_k
-    const double blo = -nfs * wk, bhi = (ee + nfs) * wk;
-    o[36 + k] = on ? (float)fmin(blo, bhi) : 0.f;
-    o[40 + k] = on ? (float)fmax(blo, bhi) : 0.f;
+    const float blo = -nfs * wk, bhi = (ee + nfs) * wk;
+    o[36 + k] = on ? fminf(blo, bhi) : 0.f;
+    o[40 + k] = on ? fmaxf(blo, bhi) : 0.f;
     if (on) {
       anyNear = true;
       // farthest point of this filament's near zone from corner 0
-      reach = fmax(reach, fmax(norm3(c[k] - c[0]), norm3(c[(k + 1) & 3] - c[0])) + near_factor * rv[k]);
+      const float ax = (float)(cx[k] - cx[0]), ay = (float)(cy[k] - cy[0]), az = (float)(cz[k] - cz[0]);
+      const float bx = (float)(cx[j] - cx[0]), by = (float)(cy[j] - cy[0]), bz = (float)(cz[j] - cz[0]);
+      const float da = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+      const float db = sqrtf(fmaf(bx, bx, fmaf(by, by, bz * bz)));
+      reach = fmaxf(reach, fmaxf(da, db) + nf * rv[k]);
     }
   }
-  const double r = reach * 1.0001 + 1e-6;
-  o[44] = anyNear ? (float)(r * r) : -1.f;
+  // margin for the FP32 rounding of corners and of this sum
+  const float r = reach * 1.0001f + 1e-6f;
+  o[44] = anyNear ? r * r : -1.f;
   o[45] = o[46] = o[47] = 0.f;
 }
 

@@ -856,6 +856,100 @@ struct Case {
     finishSteps(nsteps, ctRows);
   }
 
+  // ---- checkpoint / resume (the reference's Restart/restartNNNNN.dat:
+  // src/main.f90:389-397 reads t and the rotor object, :1443-1450 writes
+  // them every restartWriteNt steps) -------------------------------------------
+  std::vector<std::pair<void*, size_t>> stateArrays() {
+    const size_t nb = d.nb, npan = d.npan, n = d.n, ns = d.ns;
+    const size_t nring = nb * std::max(d.NW, 1) * ns, nfar = nb * std::max(d.NF, 1), nsec = nb * ns;
+    const size_t D = sizeof(double);
+    std::vector<std::pair<void*, size_t>> v = {
+        {s.wGam, nb * npan * D},   {s.gamPrev, nb * npan * D},     {s.gamVec, n * D},
+        {s.gamVecPrev, n * D},     {s.RHS, n * D},                 {s.velCP, 3 * nb * npan * D},
+        {s.velCPTotal, 3 * nb * npan * D}, {s.AIC, n * n * D},     {s.AICinv, n * n * D},
+        {s.LU, n * n * D},         {s.piv, n * sizeof(int)},       {s.nC, nring * 12 * D},
+        {s.nCP, nring * 12 * D},   {s.nGam, nring * D},            {s.nRvc, nring * 4 * D},
+        {s.nAge, nring * D},       {s.fC, nfar * 6 * D},           {s.fCP, nfar * 6 * D},
+        {s.fGam, nfar * D},        {s.fRvc, nfar * D},             {s.fRvc0, nfar * D},
+        {s.fL0, nfar * D},         {s.fLc, nfar * D},              {s.fAge, nfar * D},
+        {s.secResVel, 3 * nsec * D}, {s.secLiftDir, 3 * nsec * D}, {s.secDragDir, 3 * nsec * D},
+        {s.secLift, 3 * nsec * D}, {s.secForceInertial, 3 * nsec * D}, {s.secLiftUnsteady, 3 * nsec * D},
+        {s.secLiftInPlane, 3 * nsec * D}, {s.secLiftOutPlane, 3 * nsec * D}, {s.secCL, nsec * D},
+        {s.secCD, nsec * D},       {s.secCLu, nsec * D},           {s.bladeForce, nb * 12 * D},
+        {s.rotorLift, 3 * D},      {s.ctHist, (size_t)(W.nt + 1) * 10 * D}};
+    for (int k = 0; k < 7; ++k) {
+      v.push_back({s.vN[k], nb * std::max(d.NW, 1) * (ns + 1) * 3 * D});
+      v.push_back({s.vF[k], nfar * 3 * D});
+    }
+    if (refine) {
+      v.push_back({s.LU32, n * n * sizeof(float)});
+      v.push_back({s.AICinv32, n * n * sizeof(float)});
+      v.push_back({s.piv32, n * sizeof(int)});
+      v.push_back({s.luRes, D});
+    }
+    return v;
+  }
+  static constexpr uint64_t kCkptMagic = 0x3154504b434d4c56ull;  // "VLMCKPT1"
+  std::vector<int64_t> ckptHeader() const {
+    return {(int64_t)kCkptMagic, iter, d.nb, d.nc, d.ns, d.NW, d.NF, W.nt, opt.precision, opt.sum_chunk,
+            refine ? 1 : 0};
+  }
+
+  void checkpointSave(const std::string& path) {
+    if (!started) throw StatusError(VLM_ERR_STATE, "checkpoint before vlm_case_start");
+    if (surr.on) throw StatusError(VLM_ERR_UNSUPPORTED, "checkpoints of a case with the surrogate");
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw StatusError(VLM_ERR_IO, "cannot open " + path);
+    const auto h = ckptHeader();
+    const int64_t nh = (int64_t)h.size();
+    f.write(reinterpret_cast<const char*>(&nh), sizeof(nh));
+    f.write(reinterpret_cast<const char*>(h.data()), sizeof(int64_t) * h.size());
+    std::vector<char> buf;
+    for (auto& a : stateArrays()) {
+      buf.resize(a.second);
+      VLM_CUDA(cudaMemcpy(buf.data(), a.first, a.second, cudaMemcpyDeviceToHost));
+      const int64_t nb = (int64_t)a.second;
+      f.write(reinterpret_cast<const char*>(&nb), sizeof(nb));
+      f.write(buf.data(), (std::streamsize)buf.size());
+    }
+    if (!f) throw StatusError(VLM_ERR_IO, "write failed: " + path);
+  }
+
+  void checkpointLoad(const std::string& path) {
+    if (surr.on) throw StatusError(VLM_ERR_UNSUPPORTED, "checkpoints of a case with the surrogate");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw StatusError(VLM_ERR_IO, "cannot open " + path);
+    int64_t nh = 0;
+    f.read(reinterpret_cast<char*>(&nh), sizeof(nh));
+    auto mine = ckptHeader();
+    if (!f || nh != (int64_t)mine.size()) throw StatusError(VLM_ERR_INVALID, "not a checkpoint of this format: " + path);
+    std::vector<int64_t> h((size_t)nh);
+    f.read(reinterpret_cast<char*>(h.data()), sizeof(int64_t) * nh);
+    if (!f || h[0] != (int64_t)kCkptMagic) throw StatusError(VLM_ERR_INVALID, "not a checkpoint: " + path);
+    for (size_t i = 2; i < h.size(); ++i)
+      if (h[i] != mine[i])
+        throw StatusError(VLM_ERR_INVALID, "checkpoint of a different case or options: " + path);
+    if (h[1] < 0 || h[1] > W.nt) throw StatusError(VLM_ERR_INVALID, "checkpoint step out of range");
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    std::vector<char> buf;
+    for (auto& a : stateArrays()) {
+      int64_t nb = 0;
+      f.read(reinterpret_cast<char*>(&nb), sizeof(nb));
+      if (!f || nb != (int64_t)a.second) throw StatusError(VLM_ERR_INVALID, "checkpoint arrays do not match: " + path);
+      buf.resize(a.second);
+      f.read(buf.data(), (std::streamsize)buf.size());
+      if (!f) throw StatusError(VLM_ERR_IO, "truncated checkpoint: " + path);
+      VLM_CUDA(cudaMemcpy(a.first, buf.data(), a.second, cudaMemcpyHostToDevice));
+    }
+    // the frame of the restored step (later steps upload their own)
+    iter = (int)h[1];
+    VLM_CUDA(cudaMemcpy(s.frames + (size_t)iter * d.fl.size, hFrames + (size_t)iter * d.fl.size,
+                        sizeof(double) * d.fl.size, cudaMemcpyHostToDevice));
+    started = true;
+    iterSynced = false;
+  }
+
   // Times the partial-sum kernel of the next step's wake-node evaluation on
   // the current state (reps launches between CUDA events); reports the mean
   // launch time and the ring / single-filament pair counts of one launch.
@@ -1578,6 +1672,16 @@ int vlm_case_surrogate_stats(vlm_case* c, vlm_surrogate_stats* out) {
   *out = c->c.surr.st;
   out->phase = c->c.surr.on ? c->c.surr.phase : VLM_SURR_OFF;
   return VLM_OK;
+}
+
+int vlm_case_checkpoint_save(vlm_case* c, const char* path) {
+  if (!c || !path) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.checkpointSave(path); });
+}
+
+int vlm_case_checkpoint_load(vlm_case* c, const char* path) {
+  if (!c || !path) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.checkpointLoad(path); });
 }
 
 int vlm_case_profile_eval(vlm_case* c, int reps, double* ms_per_launch, double* ring_pairs, double* fil_pairs) {

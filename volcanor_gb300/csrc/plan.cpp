@@ -32,7 +32,7 @@ constexpr int kMinChunk = 16;
 constexpr int64_t kMaxPartials = 1 << 24;  // (chunks x targets) bound: 384 MB of FP64 partial sums
 }  // namespace
 
-int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap) {
+int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap, int targets_per_block) {
   int64_t total = 0;
   int maxRec = 0;
   for (int g = 0; g < ngroups; ++g) {
@@ -44,7 +44,7 @@ int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, i
     return 0;
   }
   slots = std::max(1, slots);
-  const int64_t bx = (M + kTargetsPerBlock32 - 1) / kTargetsPerBlock32;
+  const int64_t bx = (M + targets_per_block - 1) / targets_per_block;
   const int nmax = std::max(1, std::min(maxRec / kMinChunk, 4 * slots));
   int bestN = 1;
   double bestT = 0.0;

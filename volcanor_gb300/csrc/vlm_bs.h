@@ -77,18 +77,21 @@ struct Chunk {
 // Returns the number of chunks.
 int build_chunks(Group* groups, int ngroups, int chunk_size, Chunk* chunks, int cap);
 
+// Targets one FP32 kernel block covers.
+constexpr int kTargetsPerBlock32 = 512;
+
 // Chunk plan for the FP32 kernel (whose summation order is free): picks the
 // number of chunks per group that minimises the modelled run time of a grid
 // of ceil(M / targets_per_block) x chunks blocks on `slots` resident block
 // slots, with chunks of balanced size inside each group.  Fills the groups'
 // chunk_begin/count like build_chunks; returns the number of chunks, or -1
 // if cap is too small.
-int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap);
+int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap,
+                  int targets_per_block = kTargetsPerBlock32);
 // Resident block slots of the FP32 kernel on the current device
 // (SMs x resident blocks per SM).
 int partial32_slots();
-// Targets one FP32 kernel block covers.
-constexpr int kTargetsPerBlock32 = 512;
+
 
 // FP64 reference-arithmetic partial sums: part[(q * M + m) * 3 + k].
 void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,

@@ -81,6 +81,8 @@ SIGNATURES = {
     "vlm_case_vind_points": (ctypes.c_int, [_vp, _dp, _i64, _dp]),
     "vlm_case_last_step_ms": (ctypes.c_int, [_vp, _dp]),
     "vlm_case_profile_eval": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "vlm_case_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "vlm_case_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "vlm_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
                                         ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
     "vlm_batch_destroy": (ctypes.c_int, [_vp]),
@@ -252,6 +254,12 @@ class Case:
         out = np.zeros(max(n, 1))
         L.vlm_case_get(self._h, name.encode(), blade, _ptr(out), n)
         return out[:n]
+
+    def checkpoint_save(self, path) -> None:
+        _err(load().vlm_case_checkpoint_save(self._h, str(path).encode()))
+
+    def checkpoint_load(self, path) -> None:
+        _err(load().vlm_case_checkpoint_load(self._h, str(path).encode()))
 
     def set_surrogate(self, **kw) -> None:
         """Enable the learned far-wake surrogate (before start); keywords
