@@ -335,9 +335,23 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   }
 }
 
-// FP64 evaluation of the listed near-field filament-target pairs (reference
-// arithmetic: filament velocity times the circulation), added in fixed point
-// to the accumulators of their (chunk, target).
+// FP64 filament velocity (src/classdef.f90:476-503: the Vatistas n=2 kernel
+// with the eps^2 cut-off) written for speed on a part whose FP64 divide and
+// square root are slow: three reciprocal square roots, no division.  Equal
+// to the reference arithmetic to a few FP64 ulps.
+__device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
+  const d3 r1 = p - a, r2 = p - b, r0 = r1 - r2;
+  const d3 c = cross3(r1, r2);
+  const double c2 = dot3(c, c);
+  if (!(c2 > kEps * kEps)) return zero3();
+  const double d = dot3(r0, r1) * rsqrt(dot3(r1, r1)) - dot3(r0, r2) * rsqrt(dot3(r2, r2));
+  const double s2 = (rvc * rvc) * dot3(r0, r0);
+  return c * (d * rsqrt(s2 * s2 + c2 * c2) * kInv4Pi);
+}
+
+// FP64 evaluation of the listed near-field filament-target pairs (filament
+// velocity times the circulation), added in fixed point to the accumulators
+// of their (chunk, target).
 __global__ void k_near64(const NearPair* __restrict__ near, int* __restrict__ ctl, int near_cap,
                          const double* __restrict__ rec64, const double* __restrict__ P, int M,
                          unsigned long long* __restrict__ nacc) {
@@ -348,11 +362,11 @@ __global__ void k_near64(const NearPair* __restrict__ near, int* __restrict__ ct
     const d3 p = mk3(P[3 * (size_t)np.m], P[3 * (size_t)np.m + 1], P[3 * (size_t)np.m + 2]);
     d3 v;
     if ((int)R[17] & REC_FIL) {
-      v = fil_vind64(p, mk3(R[0], R[1], R[2]), mk3(R[3], R[4], R[5]), R[12]);
+      v = fil_near64(p, mk3(R[0], R[1], R[2]), mk3(R[3], R[4], R[5]), R[12]);
     } else {
       const int k = np.k, j = (k + 1) & 3;
-      v = vf_vind64(make_corner64(p, mk3(R[3 * k], R[3 * k + 1], R[3 * k + 2])),
-                    make_corner64(p, mk3(R[3 * j], R[3 * j + 1], R[3 * j + 2])), R[12 + k]);
+      v = fil_near64(p, mk3(R[3 * k], R[3 * k + 1], R[3 * k + 2]), mk3(R[3 * j], R[3 * j + 1], R[3 * j + 2]),
+                     R[12 + k]);
     }
     v = v * R[16];
     unsigned long long* o = nacc + ((size_t)np.q * M + np.m) * 3;

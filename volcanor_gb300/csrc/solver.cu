@@ -760,22 +760,29 @@ __global__ void k_solve_refine(Dims d, DevState s) {
   }
   bmax = red[0];
   __syncthreads();
+  // one warp per row for both products, lanes over the columns, then a
+  // butterfly: latency of n/32 multiply-adds instead of n
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   double rmax = 0.0;
   for (int pass = 0; pass < kRefinePasses; ++pass) {
     // x += inv32 r  (FP32 products of the FP32-rounded residual, FP64 update)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = warp; i < n; i += nwarps) {
       float z = 0.f;
-      for (int j = 0; j < n; ++j) z = fmaf(s.AICinv32[i + (size_t)n * j], (float)r[j], z);
-      x[i] += (double)z;
+      for (int j = lane; j < n; j += 32) z = fmaf(s.AICinv32[i + (size_t)n * j], (float)r[j], z);
+      for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+      if (lane == 0) x[i] += (double)z;
     }
     __syncthreads();
     // r = b - A x in FP64
     rmax = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = warp; i < n; i += nwarps) {
       double ax = 0.0;
-      for (int j = 0; j < n; ++j) ax = fma(s.AIC[i + (size_t)n * j], x[j], ax);
-      r[i] = b[i] - ax;
-      rmax = fmax(rmax, fabs(r[i]));
+      for (int j = lane; j < n; j += 32) ax = fma(s.AIC[i + (size_t)n * j], x[j], ax);
+      for (int o = 16; o > 0; o >>= 1) ax += __shfl_xor_sync(0xffffffffu, ax, o);
+      if (lane == 0) {
+        r[i] = b[i] - ax;
+        rmax = fmax(rmax, fabs(r[i]));
+      }
     }
     __syncthreads();
   }
@@ -866,57 +873,69 @@ struct ChunkAcc {
 
 // Velocity at collocation point t including the wing's own induced velocity
 // minus its bound vortices (src/classdef.f90 calc_force's velCPTotal): one
-// block per collocation point.  The threads evaluate the four filament
-// velocities of a batch of panels in parallel (one filament each) into shared
+// block per collocation point.  The block's threads evaluate, batch by
+// batch, one stream of items over all blades -- per blade the four filament
+// velocities of every panel, then the trailing-edge filament of every
+// section (times its circulation), padded to a multiple of 4 -- into shared
 // memory, and thread 0 forms the terms and adds them in the reference's
 // order: the ring term ((f1 + f2) + f3) + f4 is vr_vind's sum, the bound pair
 // f2 + f4 and the trailing-edge f2 are the single-filament calls, all of
 // which evaluate the same filament function on the same corners.
-constexpr int kVcPanels = 32;  // panels per batch (4 filaments each, 128 threads)
-__global__ void __launch_bounds__(128) k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk) {
-  __shared__ double F[kVcPanels * 4 * 3];
+constexpr int kVcItems = 256;  // items per batch (a multiple of 4)
+__global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk) {
+  __shared__ double F[kVcItems * 3];
   const int t = blockIdx.x;
   if (t >= d.nbC * d.npan) return;
   const d3 P = ld3(panRec(d, fr, t / d.npan, t % d.npan) + 12);
+  const int nf = 4 * d.npan, nte = (d.ns + 3) & ~3, per = nf + nte;
+  const int total = d.nb * per;
   d3 bound = zero3(), wing = zero3();
-  for (int b = 0; b < d.nb; ++b) {
-    d3 sb = zero3();
-    ChunkAcc acc(sumChunk);
-    for (int p0 = 0; p0 < d.npan; p0 += kVcPanels) {
-      const int n = min(kVcPanels, d.npan - p0);
-      for (int i = threadIdx.x; i < 4 * n; i += blockDim.x) {
-        const int p = p0 + (i >> 2), k = i & 3;
+  d3 sb = zero3();
+  ChunkAcc acc(sumChunk);
+  for (int i0 = 0; i0 < total; i0 += kVcItems) {
+    const int n = min(kVcItems, total - i0);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int it = i0 + i, b = it / per, o = it % per;
+      d3 v = zero3();
+      if (o < nf) {
+        const int p = o >> 2, k = o & 3;
         const double* w = panRec(d, fr, b, p);
-        const corner64 ka = make_corner64(P, ld3(w + 3 * k)), kb = make_corner64(P, ld3(w + 3 * ((k + 1) & 3)));
-        st3(F + 3 * i, vf_vind64(ka, kb, s.wRvc[4 * ((size_t)b * d.npan + p) + k]));
+        v = vf_vind64(make_corner64(P, ld3(w + 3 * k)), make_corner64(P, ld3(w + 3 * ((k + 1) & 3))),
+                      s.wRvc[4 * ((size_t)b * d.npan + p) + k]);
+      } else if (o - nf < d.ns) {
+        const int p = (d.nc - 1) + d.nc * (o - nf);
+        const double* w = panRec(d, fr, b, p);
+        v = vf_vind64(make_corner64(P, ld3(w + 3)), make_corner64(P, ld3(w + 6)),
+                      s.wRvc[4 * ((size_t)b * d.npan + p) + 1]) *
+            s.wGam[(size_t)b * d.npan + p];
       }
-      __syncthreads();
-      if (threadIdx.x == 0)
-        for (int i = 0; i < n; ++i) {
-          const int p = p0 + i;
+      st3(F + 3 * i, v);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < n;) {
+        const int it = i0 + i, b = it / per, o = it % per;
+        if (o < nf) {
+          const int p = o >> 2;
           const double g = s.wGam[(size_t)b * d.npan + p];
-          const d3 f0 = ld3(F + 12 * i), f1 = ld3(F + 12 * i + 3), f2 = ld3(F + 12 * i + 6), f3 = ld3(F + 12 * i + 9);
+          const d3 f0 = ld3(F + 3 * i), f1 = ld3(F + 3 * i + 3), f2 = ld3(F + 3 * i + 6), f3 = ld3(F + 3 * i + 9);
           sb = sb + (f1 + f3) * g;
           acc.add((((f0 + f1) + f2) + f3) * g);
+          i += 4;
+        } else {
+          if (o - nf < d.ns) sb = sb - ld3(F + 3 * i);
+          if (o == per - 1) {
+            // the blade's sums are complete
+            bound = bound + sb;
+            wing = wing + acc.result();
+            sb = zero3();
+            acc = ChunkAcc(sumChunk);
+          }
+          i += 1;
         }
-      __syncthreads();
-    }
-    // trailing-edge panels (i = nc - 1) of every section j, in order of j
-    for (int j0 = 0; j0 < d.ns; j0 += 4 * kVcPanels) {
-      const int n = min(4 * kVcPanels, d.ns - j0);
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int p = (d.nc - 1) + d.nc * (j0 + i);
-        const double* w = panRec(d, fr, b, p);
-        const corner64 ka = make_corner64(P, ld3(w + 3)), kb = make_corner64(P, ld3(w + 6));
-        st3(F + 3 * i, vf_vind64(ka, kb, s.wRvc[4 * ((size_t)b * d.npan + p) + 1]) * s.wGam[(size_t)b * d.npan + p]);
       }
-      __syncthreads();
-      if (threadIdx.x == 0)
-        for (int i = 0; i < n; ++i) sb = sb - ld3(F + 3 * i);
-      __syncthreads();
     }
-    bound = bound + sb;
-    wing = wing + acc.result();
+    __syncthreads();
   }
   if (threadIdx.x == 0) {
     d3 v = ld3(s.velCP + 3 * (size_t)t);
@@ -1302,7 +1321,7 @@ void launch_step_begin(const Dims& d, const DevState& s, cudaStream_t st) {
 }
 void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st) {
   count_launch();
-  k_velcp_total<<<d.nbC * d.npan, 128, 0, st>>>(d, s, frame, sumChunk);
+  k_velcp_total<<<d.nbC * d.npan, 256, 0, st>>>(d, s, frame, sumChunk);
   count_launch();
   k_loads<<<1, 256, 0, st>>>(d, s, frame, iter);
 }
