@@ -147,6 +147,20 @@ __device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec,
   if (dst) staged += total;
 }
 
+// Corner vectors r_k = P - c_k and 1/|r_k| (|r|^2 + 1e-30: a target on a
+// corner gets a finite 1/|r|, times r = 0).
+__device__ __forceinline__ void corner_vectors(float px, float py, float pz, const float (&cx)[4], const float (&cy)[4],
+                                               const float (&cz)[4], float (&rx)[4], float (&ry)[4], float (&rz)[4],
+                                               float (&inv)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    rx[k] = px - cx[k];
+    ry[k] = py - cy[k];
+    rz[k] = pz - cz[k];
+    inv[k] = rsqrtf(fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], fmaf(rz[k], rz[k], kS2Min))));
+  }
+}
+
 // Adds the FP32 velocity of one record at one target (corner vectors r_k and
 // rsqrt norms given).  CHECK: also tests every filament against its near
 // zone, leaves the near ones out and returns their bit mask.
@@ -285,30 +299,42 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
         const float cx[4] = {q0.x, q0.w, q1.z, q2.y};
         const float cy[4] = {q0.y, q1.x, q1.w, q2.z};
         const float cz[4] = {q0.z, q1.y, q2.x, q2.w};
-        float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
-        bool cand = false;
-#pragma unroll
-        for (int u = 0; u < kTPT; ++u) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            rx[u][k] = px[u] - cx[k];
-            ry[u][k] = py[u] - cy[k];
-            rz[u][k] = pz[u] - cz[k];
-            // |r|^2 + 1e-30: a target on a corner gets a finite 1/|r| (times r = 0)
-            const float s2 = fmaf(rx[u][k], rx[u][k], fmaf(ry[u][k], ry[u][k], fmaf(rz[u][k], rz[u][k], kS2Min)));
-            inv[u][k] = rsqrtf(s2);
-            if (NEAR && k == 0) cand |= valid[u] && s2 < tile[r * kRec32 + 44];
-          }
-        }
-        if (NEAR && __any_sync(kFull, cand)) {
-          // some lane of the warp is within reach of this record
-          const int rec = ch.rec_begin + t * kTileW + r;
+        if (NEAR) {
+          // candidate test first (distance to corner 0 against the record's
+          // reach), so that only one target's corner vectors are live in
+          // either path below
+          const float reach2 = tile[r * kRec32 + 44];
+          bool cand = false;
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) {
-            unsigned msk = ring_fp32<true>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
-            near_append(valid[u] ? msk : 0u, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
+            const float dx = px[u] - cx[0], dy = py[u] - cy[0], dz = pz[u] - cz[0];
+            cand |= valid[u] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < reach2;
+          }
+          if (__any_sync(kFull, cand)) {
+            // some lane of the warp is within reach of this record
+            const int rec = ch.rec_begin + t * kTileW + r;
+#pragma unroll
+            for (int u = 0; u < kTPT; ++u) {
+              float rx[4], ry[4], rz[4], inv[4];
+              corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
+              const unsigned msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
+              near_append(valid[u] ? msk : 0u, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
+            }
+            continue;
+          }
+        }
+        if (NEAR) {
+#pragma unroll
+          for (int u = 0; u < kTPT; ++u) {
+            float rx[4], ry[4], rz[4], inv[4];
+            corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
+            ring_fp32<false>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
           }
         } else {
+          // both targets' corner vectors first: more independent work in flight
+          float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
+#pragma unroll
+          for (int u = 0; u < kTPT; ++u) corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx[u], ry[u], rz[u], inv[u]);
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) ring_fp32<false>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
         }
