@@ -852,11 +852,12 @@ __global__ void k_solve(Dims d, DevState s) {
 }
 
 // ---- loads (main.f90:623-690, classdef.f90:1704-1896, 2196-2232, 4607-4671) ---
-struct ChunkAcc {
+// Chunked (sum_chunk) accumulation of one component, as the oracle's ChunkSum
+struct ChunkAcc1 {
   int C, cnt;
-  d3 tot, part;
-  __device__ ChunkAcc(int c) : C(c), cnt(0), tot(zero3()), part(zero3()) {}
-  __device__ void add(d3 x) {
+  double tot, part;
+  __device__ ChunkAcc1(int c) : C(c), cnt(0), tot(0.0), part(0.0) {}
+  __device__ void add(double x) {
     if (C <= 0) {
       tot = tot + x;
       return;
@@ -864,12 +865,13 @@ struct ChunkAcc {
     part = part + x;
     if (++cnt == C) {
       tot = tot + part;
-      part = zero3();
+      part = 0.0;
       cnt = 0;
     }
   }
-  __device__ d3 result() const { return (C > 0 && cnt > 0) ? tot + part : tot; }
+  __device__ double result() const { return (C > 0 && cnt > 0) ? tot + part : tot; }
 };
+
 
 // Velocity at collocation point t including the wing's own induced velocity
 // minus its bound vortices (src/classdef.f90 calc_force's velCPTotal): one
@@ -877,10 +879,11 @@ struct ChunkAcc {
 // batch, one stream of items over all blades -- per blade the four filament
 // velocities of every panel, then the trailing-edge filament of every
 // section (times its circulation), padded to a multiple of 4 -- into shared
-// memory, and thread 0 forms the terms and adds them in the reference's
+// memory, and the terms are formed and added in the reference's
 // order: the ring term ((f1 + f2) + f3) + f4 is vr_vind's sum, the bound pair
 // f2 + f4 and the trailing-edge f2 are the single-filament calls, all of
-// which evaluate the same filament function on the same corners.
+// which evaluate the same filament function on the same corners.  Threads
+// 0..2 do the ordered sums of the x, y, z components.
 constexpr int kVcItems = 256;  // items per batch (a multiple of 4)
 __global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk) {
   __shared__ double F[kVcItems * 3];
@@ -889,9 +892,11 @@ __global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const d
   const d3 P = ld3(panRec(d, fr, t / d.npan, t % d.npan) + 12);
   const int nf = 4 * d.npan, nte = (d.ns + 3) & ~3, per = nf + nte;
   const int total = d.nb * per;
-  d3 bound = zero3(), wing = zero3();
-  d3 sb = zero3();
-  ChunkAcc acc(sumChunk);
+  // threads 0..2 each sum one component (the d3 sums are component-wise, so
+  // the bits equal those of one thread summing d3 values)
+  const int c = threadIdx.x;
+  double bound = 0.0, wing = 0.0, sb = 0.0;
+  ChunkAcc1 acc(sumChunk);
   for (int i0 = 0; i0 < total; i0 += kVcItems) {
     const int n = min(kVcItems, total - i0);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -912,24 +917,24 @@ __global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const d
       st3(F + 3 * i, v);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (c < 3) {
       for (int i = 0; i < n;) {
         const int it = i0 + i, b = it / per, o = it % per;
         if (o < nf) {
           const int p = o >> 2;
           const double g = s.wGam[(size_t)b * d.npan + p];
-          const d3 f0 = ld3(F + 3 * i), f1 = ld3(F + 3 * i + 3), f2 = ld3(F + 3 * i + 6), f3 = ld3(F + 3 * i + 9);
+          const double f0 = F[3 * i + c], f1 = F[3 * i + 3 + c], f2 = F[3 * i + 6 + c], f3 = F[3 * i + 9 + c];
           sb = sb + (f1 + f3) * g;
           acc.add((((f0 + f1) + f2) + f3) * g);
           i += 4;
         } else {
-          if (o - nf < d.ns) sb = sb - ld3(F + 3 * i);
+          if (o - nf < d.ns) sb = sb - F[3 * i + c];
           if (o == per - 1) {
             // the blade's sums are complete
             bound = bound + sb;
             wing = wing + acc.result();
-            sb = zero3();
-            acc = ChunkAcc(sumChunk);
+            sb = 0.0;
+            acc = ChunkAcc1(sumChunk);
           }
           i += 1;
         }
@@ -937,11 +942,11 @@ __global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const d
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    d3 v = ld3(s.velCP + 3 * (size_t)t);
+  if (c < 3) {
+    double v = s.velCP[3 * (size_t)t + c];
     v = v - bound;
     v = v + wing;
-    st3(s.velCPTotal + 3 * (size_t)t, v);
+    s.velCPTotal[3 * (size_t)t + c] = v;
   }
 }
 
