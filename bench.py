@@ -241,6 +241,23 @@ def run_kernel_cfg3(prec: int, reps: int, M: int = 1 << 20, N: int = 1 << 18):
             "tflops": pairs * RING_FLOP / (ms / 1e3) / 1e12}
 
 
+def max_over_ranks(x: float, dist=None, device: str = "cuda") -> float:
+    """The maximum of x over the ranks of the process group (x itself when
+    there is none): the contract's max-over-ranks timing."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput of `world` independent replicas that each did
+    units_per_rank units, the slowest in `seconds`."""
+    return world * units_per_rank / seconds
+
+
 def run_ours(args):
     from volcanor_gb300 import lib
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
@@ -255,8 +272,7 @@ def run_ours(args):
     K, W = args.steps, args.warmup
     nt = FULL_WAKE_STEP + W + 2 * K + 2
     c = C.rotor_2blade_hover(nt=max(nt, 1440))
-    case = lib.Case(c.config, c.geom, precision=prec)
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    case = lib.Case(c.config, c.geom, precision=prec, device=local)
     case.start()
     # reach the steady state, then W warm-up steps
     done = 0
@@ -274,18 +290,16 @@ def run_ours(args):
         wall = time.perf_counter() - t0
         dev_ms = case.last_step_ms()
     if dist:
-        import torch
-        t = torch.tensor([dev_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
-    value = world * K / (dev_ms / 1e3)
+        dist.barrier()
+    dev_ms = max_over_ranks(dev_ms, dist)
+    value = replica_rate(K, world, dev_ms / 1e3)
     # e2e: one public-API call per step with host buffers
     e2e_steps = K
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         case.step(1)
-    e2e_wall = time.perf_counter() - t0
-    e2e = world * e2e_steps / e2e_wall
+    e2e_wall = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = replica_rate(e2e_steps, world, e2e_wall)
     frame_doubles = None
     try:
         nb, nc, ns = case.geti("nb"), case.geti("nc"), case.geti("ns")

@@ -480,7 +480,7 @@ struct Case {
     surrYoung = o.young_far;
     // per-step plans: the same evaluations without the far wake, the far
     // wake alone on the far-wake nodes, on the collection sample (FP32) and
-    // on the audit sample (FP64, the judge)
+    // on the audit sample (FP64, which decides the audit)
     splans.assign(W.nt + 1, SurrPlans());
     for (int k = 1; k <= W.nt; ++k) {
       const StepPlan& pl = plans[k];

@@ -209,10 +209,12 @@ class Case:
 
     def __init__(self, config_text: str, geom_text: str, base_dir: str | os.PathLike = "",
                  precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
-                 solve_mode: Optional[int] = None, use_graph: bool = True, nbody_slots: int = 0):
+                 solve_mode: Optional[int] = None, use_graph: bool = True, nbody_slots: int = 0,
+                 device: int = 0):
         L = load()
         self._h = _vp()
-        self.opt = options(precision, sum_chunk, near_factor, use_graph=use_graph, solve_mode=solve_mode)
+        self.opt = options(precision, sum_chunk, near_factor, device=device, use_graph=use_graph,
+                           solve_mode=solve_mode)
         self.opt.nbody_slots = nbody_slots
         _err(L.vlm_case_create(config_text.encode(), geom_text.encode(), str(base_dir).encode(),
                                ctypes.byref(self.opt), ctypes.byref(self._h)))
