@@ -18,14 +18,15 @@
 // zero; the reference's eps^2 cut-off needs no separate test.  FP32 partial sums are promoted to
 // the FP64 accumulator after every tile.
 //
-// Near field: one compare per target and ring (distance to corner 0 against
-// the record's reach) and a warp vote select the records some lane of the
-// warp may be near; for those the warp evaluates the record with a per-
+// Near field: one compare per target and ring (distance to the record's
+// centre against its reach) and a warp vote select the records some lane of
+// the warp may be near; for those the warp evaluates the record with a per-
 // filament near-zone test that leaves near filaments out of the FP32 sum and
-// appends one (target, record, filament) entry per near filament to a list.  k_near64 evaluates
-// the list coherently in FP64 into order-independent fixed-point
-// accumulators, and k_near_apply adds them to the chunk partial sums, so the
-// result does not depend on the order of the list.
+// appends one (target, record, filament) entry per near filament to a list
+// (staged per warp in shared memory).  k_near64 evaluates the list
+// coherently in FP64 into order-independent fixed-point accumulators, and
+// k_near_apply adds them to the chunk partial sums, so the result does not
+// depend on the order of the list.
 #include <stdint.h>
 
 #include <algorithm>
@@ -300,15 +301,15 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
         const float cy[4] = {q0.y, q1.x, q1.w, q2.z};
         const float cz[4] = {q0.z, q1.y, q2.x, q2.w};
         if (NEAR) {
-          // candidate test first (distance to corner 0 against the record's
-          // reach), so that only one target's corner vectors are live in
+          // candidate test first (distance to the record's centre against
+          // its reach), so that only one target's corner vectors are live in
           // either path below
-          const float reach2 = tile[r * kRec32 + 44];
+          const float4 zone = R4[11];  // reach^2, centre of the near zones
           bool cand = false;
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) {
-            const float dx = px[u] - cx[0], dy = py[u] - cy[0], dz = pz[u] - cz[0];
-            cand |= valid[u] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < reach2;
+            const float dx = px[u] - zone.y, dy = py[u] - zone.z, dz = pz[u] - zone.w;
+            cand |= valid[u] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < zone.x;
           }
           if (__any_sync(kFull, cand)) {
             // some lane of the warp is within reach of this record
@@ -442,6 +443,16 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
   }
   const float nf = (float)near_factor;
   const float w = (float)(g * kInv4Pi);
+  // centre of the near zones: mean of the active filaments' end points
+  double mx = 0.0, my = 0.0, mz = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    mx += cx[k];
+    my += cy[k];
+    mz += cz[k];
+  }
+  mx *= 0.25;
+  my *= 0.25;
+  mz *= 0.25;
   float reach = 0.f;
   bool anyNear = false;
   for (int k = 0; k < 4; ++k) {
@@ -469,9 +480,9 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
     o[40 + k] = on ? fmaxf(blo, bhi) : 0.f;
     if (on) {
       anyNear = true;
-      // farthest point of this filament's near zone from corner 0
-      const float ax = (float)(cx[k] - cx[0]), ay = (float)(cy[k] - cy[0]), az = (float)(cz[k] - cz[0]);
-      const float bx = (float)(cx[j] - cx[0]), by = (float)(cy[j] - cy[0]), bz = (float)(cz[j] - cz[0]);
+      // farthest point of this filament's near zone from the centre
+      const float ax = (float)(cx[k] - mx), ay = (float)(cy[k] - my), az = (float)(cz[k] - mz);
+      const float bx = (float)(cx[j] - mx), by = (float)(cy[j] - my), bz = (float)(cz[j] - mz);
       const float da = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
       const float db = sqrtf(fmaf(bx, bx, fmaf(by, by, bz * bz)));
       reach = fmaxf(reach, fmaxf(da, db) + nf * rv[k]);
@@ -480,7 +491,9 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
   // margin for the FP32 rounding of corners and of this sum
   const float r = reach * 1.0001f + 1e-6f;
   o[44] = anyNear ? r * r : -1.f;
-  o[45] = o[46] = o[47] = 0.f;
+  o[45] = (float)mx;
+  o[46] = (float)my;
+  o[47] = (float)mz;
 }
 
 }  // namespace

@@ -37,9 +37,9 @@ constexpr int REC_SKIP = 2;
 //   [32..35] near-field threshold on |r1 x r2|^2: (near_factor rvc_k |e_k|)^2, -1 if off
 //   [36..39] lower near-field bound on (w_k e_k).r1
 //   [40..43] upper near-field bound on (w_k e_k).r1
-//   [44]     squared radius about corner 0 outside which no filament of the
+//   [44]     squared radius about [45..47] outside which no filament of the
 //            record can be near (-1 when the near-field path is off)
-//   [45..47] unused
+//   [45..47] centre of the near zones (mean of the four corners)
 // A pair is near when the target lies within near_factor core radii of the
 // filament SEGMENT: |r1 x r2|^2 < [32+k] and -s < e.r1 < |e|^2 + s with
 // s = near_factor rvc_k |e_k|; the second test is stored multiplied by w_k,
