@@ -269,9 +269,11 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   double acc64[kTPT][3];
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
-    // a warp's targets are 64 consecutive ones (two runs of 32), so that a
-    // spatially ordered target list gives each warp a compact patch
-    mt[u] = blockIdx.x * kTargetsPerBlock32 + warp * (32 * kTPT) + u * 32 + lane;
+    // near-field variant: a warp's targets are 64 consecutive ones (two runs
+    // of 32), so that a spatially ordered target list gives each warp a
+    // compact patch; plain variant: runs of 256 per u (measured ~2 % faster)
+    mt[u] = NEAR ? blockIdx.x * kTargetsPerBlock32 + warp * (32 * kTPT) + u * 32 + lane
+                 : blockIdx.x * kTargetsPerBlock32 + u * (32 * kConsumerWarps) + tid;
     valid[u] = mt[u] < M;
     const int mm = valid[u] ? mt[u] : M - 1;
     px[u] = (float)P[3 * (size_t)mm];
