@@ -168,7 +168,7 @@ __device__ __forceinline__ void corner_vectors(float px, float py, float pz, con
 template <bool CHECK>
 __device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, const float (&rx)[4], const float (&ry)[4],
                                               const float (&rz)[4], const float (&inv)[4], float& ax, float& ay,
-                                              float& az) {
+                                              float& az, bool mine = false) {
   const float4 q3 = R4[3], q4 = R4[4], q5 = R4[5];  // weighted edges
   const float4 ee = R4[6], a4 = R4[7];
   const float ex[4] = {q3.x, q3.w, q4.z, q5.y};
@@ -197,7 +197,9 @@ __device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, con
     float f = d * rsqrtf(fmaf(c2, c2, a4v[k]));
     if (CHECK) {
       // exact zeros (target on the filament line) stay in the FP32 sum
-      const bool nr = c2 < thr[k] && c2 > kS2Min && tt > lo[k] && tt < hi[k];
+      // only a target inside the record's sphere can flag (so that which
+      // pairs are near does not depend on the other lanes of its warp)
+      const bool nr = mine && c2 < thr[k] && c2 > kS2Min && tt > lo[k] && tt < hi[k];
       f = nr ? 0.f : f;
       msk |= nr ? (1u << k) : 0u;
     }
@@ -269,11 +271,9 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   double acc64[kTPT][3];
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
-    // near-field variant: a warp's targets are 64 consecutive ones (two runs
-    // of 32), so that a spatially ordered target list gives each warp a
-    // compact patch; plain variant: runs of 256 per u (measured ~2 % faster)
-    mt[u] = NEAR ? blockIdx.x * kTargetsPerBlock32 + warp * (32 * kTPT) + u * 32 + lane
-                 : blockIdx.x * kTargetsPerBlock32 + u * (32 * kConsumerWarps) + tid;
+    // runs of 256 targets per u: a warp's targets are two runs of 32
+    // consecutive ones (measured 1-2 % faster than one run of 64)
+    mt[u] = blockIdx.x * kTargetsPerBlock32 + u * (32 * kConsumerWarps) + tid;
     valid[u] = mt[u] < M;
     const int mm = valid[u] ? mt[u] : M - 1;
     px[u] = (float)P[3 * (size_t)mm];
@@ -307,11 +307,12 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
           // its reach), so that only one target's corner vectors are live in
           // either path below
           const float4 zone = R4[11];  // reach^2, centre of the near zones
-          bool cand = false;
+          bool candu[kTPT], cand = false;
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) {
             const float dx = px[u] - zone.y, dy = py[u] - zone.z, dz = pz[u] - zone.w;
-            cand |= valid[u] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < zone.x;
+            candu[u] = valid[u] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < zone.x;
+            cand |= candu[u];
           }
           if (__any_sync(kFull, cand)) {
             // some lane of the warp is within reach of this record
@@ -320,8 +321,8 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
             for (int u = 0; u < kTPT; ++u) {
               float rx[4], ry[4], rz[4], inv[4];
               corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-              const unsigned msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
-              near_append(valid[u] ? msk : 0u, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
+              const unsigned msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u], candu[u]);
+              near_append(msk, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
             }
             continue;
           }
