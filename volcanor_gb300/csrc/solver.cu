@@ -443,9 +443,10 @@ __device__ __forceinline__ void decode_node(const Dims& d, int rowNear, int rowF
   b = m / per;
   const int l = m % per;
   if (l < rowsN * (d.ns + 1)) {
-    // tiles of kTileRows rows x kTileCols span stations, tile by tile: the 64
-    // consecutive targets of a warp of the FP32 kernel are a compact patch of
-    // the wake sheet, so few source rings come near any of them
+    // tiles of kTileRows rows x kTileCols span stations, tile by tile: a run
+    // of 32 consecutive targets (one warp's lanes in the FP32 kernel) is a
+    // compact patch of the wake sheet, so few source rings come near any of
+    // them
     far = 0;
     const int band = l / (kTileRows * (d.ns + 1));
     const int br = min(kTileRows, rowsN - band * kTileRows);
