@@ -352,6 +352,19 @@ def run_ours(args):
         "ct_last": float(rows[-1, 1]),
     }
     out["pairs_per_s"] = round(rp / (ms_l / 1e3), 1)
+    if rank == 0 and not args.no_accuracy and prec != lib.PREC_FP64:
+        # this precision's CT error against the FP64 GPU form over the first
+        # revolution (the free wake's pre-chaotic horizon; see the accuracy module)
+        ref = lib.Case(c.config, c.geom, precision=lib.PREC_FP64, device=local)
+        ref.start()
+        a = ref.step(72)[:, 1]
+        ref.close()
+        x = lib.Case(c.config, c.geom, precision=prec, device=local)
+        x.start()
+        b = x.step(72)[:, 1]
+        x.close()
+        out["accuracy"] = {"ct_max_rel_err_vs_fp64_first_rev": float(np.max(np.abs(b - a) / np.abs(a))),
+                           "steps": 72, "note": "the full 1440-step comparison is volcanor_gb300/accuracy.py"}
     if not args.no_kernel:
         # the isolated N-body kernel in both FP32 forms (the FP64 form runs
         # ~60x slower on this part: see the bench's fp64 precision)
@@ -538,21 +551,26 @@ def run_forward4(args):
         return g
 
     def advance(g, n):
-        done = 0
+        done, rows = 0, []
         while done < n:
             m = min(100, n - done)
-            g.step(m, with_ct=False)
+            rows.append(g.step(m))
             done += m
+        return np.concatenate(rows)[:, 1]
 
-    res = {}
+    res, hist = {}, {}
     for name, prec, surr in (("fp64", lib.PREC_FP64, None), ("fp32near", lib.PREC_FP32_NEAR64, None),
                              ("fp32near_surrogate", lib.PREC_FP32_NEAR64, {})):
         g = make(prec, surr)
-        advance(g, S + W)
+        hist[name] = advance(g, S + W)
         rows = g.step(K)
         ms = g.last_step_ms()
         res[name] = {"timesteps_per_s": round(K / (ms / 1e3), 3), "ms_per_step": round(ms / K, 3),
                      "ct_last": float(rows[-1, 1])}
+        if name != "fp64":
+            rel = np.abs(hist[name] - hist["fp64"]) / np.abs(hist["fp64"])
+            res[name]["ct_max_rel_err_vs_fp64_first_rev"] = float(rel[:72].max())
+            res[name]["ct_max_rel_err_vs_fp64_all_steps"] = float(rel.max())
         if surr is not None:
             res[name]["surrogate"] = g.surrogate_stats()
         g.close()
@@ -595,6 +613,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-kernel", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--kernel-reps", type=int, default=3)
     ap.add_argument("--kernel-only", action="store_true",
                     help="only the isolated ring kernel (for profiling); prints its JSON")
