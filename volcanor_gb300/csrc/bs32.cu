@@ -30,6 +30,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "vlm_bs.h"
 #include "vlm_math.h"
@@ -511,11 +512,14 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
                       int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s) {
   if (M <= 0 || nchunks <= 0) return;
   const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
-  static bool attr = false;
-  if (!attr) {
+  // the dynamic shared-memory opt-in is per device; set it once on each
+  static std::atomic<bool> attr[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || !attr[dev].load(std::memory_order_acquire)) {
     cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
+    if (dev >= 0 && dev < 64) attr[dev].store(true, std::memory_order_release);
   }
   dim3 grid((M + kTargetsPerBlock32 - 1) / kTargetsPerBlock32, nchunks);
   count_launch();
@@ -532,7 +536,7 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
 }
 
 int partial32_slots() {
-  static int cache[64] = {0};
+  static std::atomic<int> cache[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 2 * 152;
   if (!cache[dev]) {

@@ -353,6 +353,8 @@ struct Case {
   }
 
   const double* frame(int k) const { return s.frames + (size_t)k * d.fl.size; }
+  // every entry point works on the case's own device, whatever is current
+  void useDevice() const { VLM_CUDA(cudaSetDevice(opt.device)); }
   // the frame a step's kernels read: while a step is captured for replay, the
   // device-side current frame that launch_step_begin fills
   const double* stepFrame(int k) const { return replaying ? s.curFrame : frame(k); }
@@ -462,6 +464,7 @@ struct Case {
   int farRows(int rowFar) const { return std::max(d.NF - (rowFar - 1), 0); }
 
   void setSurrogate(const vlm_surrogate_options& o) {
+    useDevice();
     if (started) throw StatusError(VLM_ERR_STATE, "set the surrogate before vlm_case_start");
     if (!o.enable) {
       surr.on = false;
@@ -682,6 +685,7 @@ struct Case {
   }
 
   void start() {
+    useDevice();
     if (started) throw StatusError(VLM_ERR_STATE, "case already started");
     launch_aic(d, s, frame(0), stream);
     launch_lu_inverse(d, s, stream);
@@ -843,6 +847,7 @@ struct Case {
   }
 
   void step(int nsteps, double* ctRows) {
+    useDevice();
     checkSteps(nsteps);
     uploadFrames(nsteps);
     VLM_CUDA(cudaEventRecord(ev0, stream));
@@ -896,6 +901,7 @@ struct Case {
   }
 
   void checkpointSave(const std::string& path) {
+    useDevice();
     if (!started) throw StatusError(VLM_ERR_STATE, "checkpoint before vlm_case_start");
     if (surr.on) throw StatusError(VLM_ERR_UNSUPPORTED, "checkpoints of a case with the surrogate");
     VLM_CUDA(cudaStreamSynchronize(stream));
@@ -917,6 +923,7 @@ struct Case {
   }
 
   void checkpointLoad(const std::string& path) {
+    useDevice();
     if (surr.on) throw StatusError(VLM_ERR_UNSUPPORTED, "checkpoints of a case with the surrogate");
     std::ifstream f(path, std::ios::binary);
     if (!f) throw StatusError(VLM_ERR_IO, "cannot open " + path);
@@ -954,6 +961,7 @@ struct Case {
   // the current state (reps launches between CUDA events); reports the mean
   // launch time and the ring / single-filament pair counts of one launch.
   void profileEval(int reps, double* msPerLaunch, double* ringPairs, double* filPairs) {
+    useDevice();
     if (!started || d.NW == 0 || iter >= W.nt) throw StatusError(VLM_ERR_STATE, "needs a started case with steps left");
     const int k = iter + 1;
     const StepPlan& pl = plans[k];
@@ -999,6 +1007,7 @@ struct Case {
   }
 
   int64_t get(const std::string& k, int blade, double* out, int64_t cap) {
+    useDevice();
     std::vector<double> v;
     const int b = blade - 1;
     const bool bok = b >= 0 && b < d.nb;
@@ -1042,6 +1051,7 @@ struct Case {
   }
 
   void vindPoints(const double* P, int64_t M, double* V) {
+    useDevice();
     if (!started) throw StatusError(VLM_ERR_STATE, "vlm_case_start must be called first");
     if (M <= 0) return;
     // groups of the current state: wing + wake at the current rows
@@ -1446,6 +1456,7 @@ struct vlm_batch {
 
   void step(int nsteps, double* ctRows) {
     if (cases.empty()) return;
+    cases[0]->c.useDevice();
     const int it0 = cases[0]->c.iter;
     for (vlm_case* c : cases) {
       if (c->c.iter != it0) throw StatusError(VLM_ERR_STATE, "the batch's cases are at different steps");
