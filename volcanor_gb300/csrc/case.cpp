@@ -68,6 +68,11 @@ struct Case {
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the loads (CT row) of a step only read the solution and feed no later
+  // part of the step: they run on a side stream, joined at the step's end
+  cudaStream_t side = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
+  bool loadsForked = false;
   std::vector<StepPlan> plans;  // index = iteration (0..nt)
   double* hFrames = nullptr;    // pinned host copy of every frame; uploaded per vlm_case_step call
   std::vector<Group> hGroups;
@@ -95,6 +100,10 @@ struct Case {
     if (hFrames) cudaFreeHost(hFrames);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (side) cudaStreamSynchronize(side);
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -195,6 +204,9 @@ struct Case {
     VLM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     VLM_CUDA(cudaEventCreate(&ev0));
     VLM_CUDA(cudaEventCreate(&ev1));
+    VLM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    VLM_CUDA(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
+    VLM_CUDA(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
 
     // frames: 0 = after the initial pitch, k = after the kinematics of step k
     std::vector<double> frames((size_t)(nt + 1) * d.fl.size);
@@ -706,6 +718,12 @@ struct Case {
   }
 
   void enqueueStep(int k) {
+    loadsForked = false;
+    enqueueStepBody(k);
+    if (loadsForked) VLM_CUDA(cudaStreamWaitEvent(stream, evJoin, 0));
+  }
+
+  void enqueueStepBody(int k) {
     const StepPlan& pl = plans[k];
     const int rN = pl.rowNear, rF = pl.rowFar;
     const double* fr = stepFrame(k);
@@ -733,8 +751,13 @@ struct Case {
     } else {
       launch_solve(d, s, fr, false, stream);
     }
-    if (W.sw.rotorForcePlot != 0 && k % W.sw.rotorForcePlot == 0)
-      launch_loads(d, s, fr, chunk64, replaying ? -1 : k, stream);
+    if (W.sw.rotorForcePlot != 0 && k % W.sw.rotorForcePlot == 0) {
+      VLM_CUDA(cudaEventRecord(evFork, stream));
+      VLM_CUDA(cudaStreamWaitEvent(side, evFork, 0));
+      launch_loads(d, s, fr, chunk64, replaying ? -1 : k, side);
+      VLM_CUDA(cudaEventRecord(evJoin, side));
+      loadsForked = true;
+    }
     if (!wake) return;
     evalNodes(k, false);
     switch (W.sw.fdScheme) {
