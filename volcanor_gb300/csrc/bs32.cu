@@ -216,7 +216,7 @@ __device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, con
 // stages with bulk copies; consumers wait on a stage's FULL barrier, compute,
 // and release it through its EMPTY barrier (one arrival per consumer warp).
 constexpr int kStages = 4;
-constexpr int kTileW = 64;                  // records per stage (12 KB)
+constexpr int kTileW = 128;                 // records per stage (24 KB)
 constexpr int kConsumerWarps = 8;
 constexpr int kBlockW = (kConsumerWarps + 1) * 32;
 static_assert(kConsumerWarps * 32 * kTPT == kTargetsPerBlock32, "targets per block");
