@@ -200,9 +200,11 @@ int vlm_batch_last_step_ms(vlm_batch* b, double* ms);
  * near-wake sheet past the young_far youngest of each blade -- is the
  * surrogate's domain.  Once it holds min_far filaments per blade, the case
  * collects training pairs for collect_steps steps -- features of the
- * collocation points and every sample_stride-th near-wake node: position
- * about the hub over the rotor radius, rotor-azimuth harmonics, old-wake fill
- * -> their direct old-far-wake velocity -- and trains an MLP (layers linear
+ * collocation points and every sample_stride-th near-wake node (position
+ * about the hub over the rotor radius, rotor-azimuth harmonics, old-wake fill)
+ * and a coarse descriptor of the old wake (its |circulation|-weighted
+ * centroid about the hub / R, its mean |circulation| relative to the wing's
+ * largest) -> their direct old-far-wake velocity -- and trains an MLP (layers linear
  * layers of width hidden, tanh) for train_iters Adam steps on the GPU.  From
  * then on the network replaces the old-far-wake sum at the collocation
  * points and near-wake nodes (far-wake nodes, next to the old wake along the

@@ -464,6 +464,7 @@ struct Case {
     Mlp net;
     float *X = nullptr, *T = nullptr, *fX = nullptr, *fY = nullptr;
     double *sP = nullptr, *sV = nullptr, *outFar = nullptr, *farP = nullptr, *scale = nullptr, *audit = nullptr;
+    double* desc = nullptr;  // coarse old-far-wake descriptor of the current evaluation
     double invR = 1.0;
     bool useNow = false;
     vlm_surrogate_stats st{};
@@ -523,9 +524,10 @@ struct Case {
     int64_t perStep = d.nbC * d.npan;
     for (int k = 1; k <= W.nt; ++k) perStep = std::max<int64_t>(perStep, d.nbC * d.npan + splans[k].collectNodes);
     surr.cap = perStep * o.collect_steps;
-    surr.X = dalloc<float>((size_t)surr.cap * 8, surrOwned);
+    surr.X = dalloc<float>((size_t)surr.cap * kSurrFeatures, surrOwned);
     surr.T = dalloc<float>((size_t)surr.cap * 3, surrOwned);
-    surr.fX = dalloc<float>((size_t)std::max(maxTargets, maxSample) * 8, surrOwned);
+    surr.fX = dalloc<float>((size_t)std::max(maxTargets, maxSample) * kSurrFeatures, surrOwned);
+    surr.desc = dalloc<double>(4, surrOwned);
     surr.fY = dalloc<float>((size_t)std::max(maxTargets, maxSample) * 3, surrOwned);
     surr.sP = dalloc<double>((size_t)maxSample * 3, surrOwned);
     surr.sV = dalloc<double>((size_t)maxSample * 3, surrOwned);
@@ -534,7 +536,7 @@ struct Case {
     surr.scale = dalloc<double>(1, surrOwned);
     surr.audit = dalloc<double>(2, surrOwned);
     std::vector<int> sizes(o.layers + 1, o.hidden);
-    sizes.front() = 8;
+    sizes.front() = kSurrFeatures;
     sizes.back() = 3;
     surr.net.create(sizes, o.seed, stream);
     surr.net.reserve(std::max(o.batch, 1 << 14));
@@ -569,14 +571,16 @@ struct Case {
     launch_gather(d, s, frame(k - 1), dGroups + e.goff, e.ngroups, e.nrec, plans[k].rowNear, plans[k].rowFar, false,
                   stream);
     evaluate(e, M, 2, surr.sP, surr.sV, prec);
-    launch_surr_features(d, frame(k - 1), surr.sP, M, surr.invR, farFill(plans[k].rowFar), surr.fX, stream);
+    launch_surr_features(d, s, frame(k - 1), surr.sP, M, surr.invR, farFill(plans[k].rowFar), plans[k].rowFar,
+                         youngAt(k), false, surr.desc, surr.fX, stream);
     return M;
   }
 
   void surrTrain() {
     Surrogate& S = surr;
     const int64_t n = S.nsamp;
-    std::vector<float> hX((size_t)n * 8), hT((size_t)n * 3);
+    constexpr int F = kSurrFeatures;
+    std::vector<float> hX((size_t)n * F), hT((size_t)n * 3);
     VLM_CUDA(cudaMemcpyAsync(hX.data(), S.X, sizeof(float) * hX.size(), cudaMemcpyDeviceToHost, stream));
     VLM_CUDA(cudaMemcpyAsync(hT.data(), S.T, sizeof(float) * hT.size(), cudaMemcpyDeviceToHost, stream));
     VLM_CUDA(cudaStreamSynchronize(stream));
@@ -593,9 +597,9 @@ struct Case {
       r ^= r << 17;
       std::swap(idx[(size_t)i], idx[(size_t)(r % (uint64_t)(i + 1))]);
     }
-    std::vector<float> sX((size_t)n * 8), sT((size_t)n * 3);
+    std::vector<float> sX((size_t)n * F), sT((size_t)n * 3);
     for (int64_t i = 0; i < n; ++i) {
-      std::memcpy(&sX[(size_t)i * 8], &hX[(size_t)idx[(size_t)i] * 8], 8 * sizeof(float));
+      std::memcpy(&sX[(size_t)i * F], &hX[(size_t)idx[(size_t)i] * F], F * sizeof(float));
       for (int c = 0; c < 3; ++c) sT[(size_t)i * 3 + c] = (float)(hT[(size_t)idx[(size_t)i] * 3 + c] / scale);
     }
     VLM_CUDA(cudaMemcpyAsync(S.X, sX.data(), sizeof(float) * sX.size(), cudaMemcpyHostToDevice, stream));
@@ -605,7 +609,7 @@ struct Case {
     const int64_t nb = std::max<int64_t>(n / b, 1);
     for (int it = 0; it < S.o.train_iters; ++it) {
       const int64_t q = it % nb;
-      S.net.grad(S.X + (size_t)q * b * 8, S.T + (size_t)q * b * 3, b);
+      S.net.grad(S.X + (size_t)q * b * kSurrFeatures, S.T + (size_t)q * b * 3, b);
       // the last third of the iterations at a fifth of the rate
       S.net.adam(it < (2 * S.o.train_iters) / 3 ? S.o.lr : 0.2f * S.o.lr);
     }
@@ -633,7 +637,7 @@ struct Case {
       const int off = (int)((uint64_t)k * 2654435761ull % (uint64_t)sp.collectStride);
       const int M = surrSample(k, sp.farCollect, sp.collectNodes, sp.collectStride, off, opt.precision);
       const int n = (int)std::min<int64_t>(M, S.cap - S.nsamp);
-      launch_surr_append(n, S.fX, S.sV, S.X + (size_t)S.nsamp * 8, S.T + (size_t)S.nsamp * 3, stream);
+      launch_surr_append(n, S.fX, S.sV, S.X + (size_t)S.nsamp * kSurrFeatures, S.T + (size_t)S.nsamp * 3, stream);
       S.nsamp += n;
       if (++S.collected >= S.o.collect_steps) {
         surrTrain();
@@ -684,7 +688,8 @@ struct Case {
       launch_gather(d, s, stepFrame(k), dGroups + sp.farFar.goff, sp.farFar.ngroups, sp.farFar.nrec, pl.rowNear, pl.rowFar,
                     pred, stream);
       evaluate(sp.farFar, Mf, 2, surr.farP, surr.outFar);
-      launch_surr_features(d, frame(pred ? k : k - 1), s.targets, M, surr.invR, farFill(pl.rowFar), surr.fX, stream);
+      launch_surr_features(d, s, frame(pred ? k : k - 1), s.targets, M, surr.invR, farFill(pl.rowFar), pl.rowFar,
+                           youngAt(k), pred, surr.desc, surr.fX, stream);
       surr.net.forward(surr.fX, M, surr.fY);
       launch_surr_merge_nodes(d, pl.rowNear, pl.rowFar, 0, M, surr.fY, surr.scale, surr.outFar, s.outv, stream);
     } else {
@@ -740,7 +745,8 @@ struct Case {
         const EvalPlan& e = splans[k].rhsNoFar;
         launch_gather(d, s, fr, dGroups + e.goff, e.ngroups, e.nrec, rN, rF, false, stream);
         evaluate(e, Mcp, 1);
-        launch_surr_features(d, frame(k - 1), s.targets, Mcp, surr.invR, farFill(rF), surr.fX, stream);
+        launch_surr_features(d, s, frame(k - 1), s.targets, Mcp, surr.invR, farFill(rF), rF, youngAt(k), false,
+                             surr.desc, surr.fX, stream);
         surr.net.forward(surr.fX, Mcp, surr.fY);
         launch_surr_add(Mcp, surr.fY, surr.scale, s.outv, stream);
       } else {

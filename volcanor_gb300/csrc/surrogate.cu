@@ -75,11 +75,59 @@ __global__ void k_surr_far_targets(Dims d, DevState s, int rowFar, int young, in
   P[3 * (size_t)t + 2] = f[2];
 }
 
-// 8 features per target: position about the hub over the rotor radius,
-// cos/sin of the rotor azimuth (blade 1's azimuth axis in the frame) and of
-// nb times it, and the far wake's fill fraction
+// Coarse descriptor of the old far wake (filaments rows rowFar + young ..
+// NF of every blade), one block, fixed-order sums: desc[0..2] = its
+// |circulation|-weighted centroid about the hub over the rotor radius,
+// desc[3] = its mean |circulation| over the wing's largest |circulation|.
+__global__ void k_surr_descriptor(Dims d, DevState s, const double* fr, int rowFar, int young, int pred, double invR,
+                                  double* desc) {
+  __shared__ double red[4][256];
+  const double* rot = fr + d.fl.rot;
+  const double* fc = pred ? s.fCP : s.fC;
+  const int first = rowFar - 1 + young;
+  const int nOld = d.NF - first;
+  double gx = 0.0, gy = 0.0, gz = 0.0, g = 0.0;
+  for (int t = threadIdx.x; t < d.nb * max(nOld, 0); t += blockDim.x) {
+    const int b = t / nOld, i = first + t % nOld;
+    const size_t f = (size_t)b * d.NF + i;
+    const double a = fabs(s.fGam[f]);
+    gx += a * 0.5 * (fc[6 * f] + fc[6 * f + 3]);
+    gy += a * 0.5 * (fc[6 * f + 1] + fc[6 * f + 4]);
+    gz += a * 0.5 * (fc[6 * f + 2] + fc[6 * f + 5]);
+    g += a;
+  }
+  double wmax = 0.0;
+  for (int t = threadIdx.x; t < d.nb * d.npan; t += blockDim.x) wmax = fmax(wmax, fabs(s.wGam[t]));
+  red[0][threadIdx.x] = gx;
+  red[1][threadIdx.x] = gy;
+  red[2][threadIdx.x] = gz;
+  red[3][threadIdx.x] = g;
+  __shared__ double rmax[256];
+  rmax[threadIdx.x] = wmax;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+      rmax[threadIdx.x] = fmax(rmax[threadIdx.x], rmax[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double G = red[3][0];
+    const int n = d.nb * max(nOld, 0);
+    desc[0] = G > 0.0 ? (red[0][0] / G - rot[3]) * invR : 0.0;
+    desc[1] = G > 0.0 ? (red[1][0] / G - rot[4]) * invR : 0.0;
+    desc[2] = G > 0.0 ? (red[2][0] / G - rot[5]) * invR : 0.0;
+    desc[3] = (n > 0 && rmax[0] > 0.0) ? G / n / rmax[0] : 0.0;
+  }
+}
+
+// kSurrFeatures features per target: position about the hub over the rotor
+// radius, cos/sin of the rotor azimuth (blade 1's azimuth axis in the frame)
+// and of nb times it, the old wake's fill fraction, and the old wake's
+// descriptor (centroid about the hub / R, relative mean |circulation|)
 __global__ void k_surr_features(Dims d, const double* fr, const double* P, int M, double invR, double fill,
-                                float* X) {
+                                const double* desc, float* X) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M) return;
   const double* rot = fr + d.fl.rot;
@@ -93,7 +141,7 @@ __global__ void k_surr_features(Dims d, const double* fr, const double* P, int M
     cn = a;
     snb = b;
   }
-  float* x = X + (size_t)t * 8;
+  float* x = X + (size_t)t * kSurrFeatures;
   x[0] = (float)((P[3 * (size_t)t] - hx) * invR);
   x[1] = (float)((P[3 * (size_t)t + 1] - hy) * invR);
   x[2] = (float)((P[3 * (size_t)t + 2] - hz) * invR);
@@ -102,6 +150,7 @@ __global__ void k_surr_features(Dims d, const double* fr, const double* P, int M
   x[5] = (float)cn;
   x[6] = (float)snb;
   x[7] = (float)fill;
+  for (int k = 0; k < 4; ++k) x[8 + k] = (float)desc[k];
 }
 
 // outv[m] += scale * Y[m] for m < M
@@ -137,7 +186,7 @@ __global__ void k_surr_merge_nodes(Dims d, int rowNear, int rowFar, int young, i
 __global__ void k_surr_append(int n, const float* Xs, const double* V, float* X, float* T) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  for (int k = 0; k < 8; ++k) X[(size_t)t * 8 + k] = Xs[(size_t)t * 8 + k];
+  for (int k = 0; k < kSurrFeatures; ++k) X[(size_t)t * kSurrFeatures + k] = Xs[(size_t)t * kSurrFeatures + k];
   for (int k = 0; k < 3; ++k) T[(size_t)t * 3 + k] = (float)V[3 * (size_t)t + k];
 }
 
@@ -186,11 +235,13 @@ void launch_surr_far_targets(const Dims& d, const DevState& s, int rowFar, int y
   count_launch();
   k_surr_far_targets<<<nblk(n, 256), 256, 0, st>>>(d, s, rowFar, young, pred ? 1 : 0, P);
 }
-void launch_surr_features(const Dims& d, const double* fr, const double* P, int M, double invR, double fill, float* X,
-                          cudaStream_t st) {
+void launch_surr_features(const Dims& d, const DevState& s, const double* fr, const double* P, int M, double invR,
+                          double fill, int rowFar, int young, bool pred, double* desc, float* X, cudaStream_t st) {
   if (M <= 0) return;
   count_launch();
-  k_surr_features<<<nblk(M, 256), 256, 0, st>>>(d, fr, P, M, invR, fill, X);
+  k_surr_descriptor<<<1, 256, 0, st>>>(d, s, fr, rowFar, young, pred ? 1 : 0, invR, desc);
+  count_launch();
+  k_surr_features<<<nblk(M, 256), 256, 0, st>>>(d, fr, P, M, invR, fill, desc, X);
 }
 void launch_surr_add(int M, const float* Y, const double* scale, double* outv, cudaStream_t st) {
   if (M <= 0) return;

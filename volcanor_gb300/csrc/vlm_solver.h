@@ -158,10 +158,13 @@ void launch_surr_targets(const Dims& d, const DevState& s, const double* fr, int
 // old far-wake nodes (all but the `young` youngest) of the convecting blades
 void launch_surr_far_targets(const Dims& d, const DevState& s, int rowFar, int young, bool pred, double* P,
                              cudaStream_t st);
-// 8 FP32 features per target (position about the hub / R, rotor azimuth
-// harmonics, far-wake fill fraction)
-void launch_surr_features(const Dims& d, const double* fr, const double* P, int M, double invR, double fill, float* X,
-                          cudaStream_t st);
+// FP32 features per target (position about the hub / R, rotor azimuth
+// harmonics, old-wake fill) and the old far wake's coarse descriptor
+// (|circulation|-weighted centroid about the hub / R, relative mean
+// |circulation|), computed into desc[4] first
+constexpr int kSurrFeatures = 12;
+void launch_surr_features(const Dims& d, const DevState& s, const double* fr, const double* P, int M, double invR,
+                          double fill, int rowFar, int young, bool pred, double* desc, float* X, cudaStream_t st);
 void launch_surr_add(int M, const float* Y, const double* scale, double* outv, cudaStream_t st);
 void launch_surr_merge_nodes(const Dims& d, int rowNear, int rowFar, int young, int M, const float* Y,
                              const double* scale, const double* outFar, double* outv, cudaStream_t st);
