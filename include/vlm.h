@@ -66,6 +66,11 @@ int vlm_last_error(char* buf, size_t len);
 void vlm_default_options(vlm_options* opt);
 /* Kernels launched by this library so far (all threads and cases). */
 int64_t vlm_kernel_launch_count(void);
+/* Failure-path self-test (no counterpart in the reference): launches a wait
+ * on a device barrier that nothing releases, bounded by `limit` polls, the
+ * same bounded wait the N-body pipeline uses.  *expired = 1 when the wait gave
+ * up and reported, as it must; the context stays usable. */
+int vlm_selftest_bounded_wait(int limit, int* expired);
 /* SM count and compute capability of `device`. */
 int vlm_device_info(int device, int* sm_count, int* cc_major, int* cc_minor);
 

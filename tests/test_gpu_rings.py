@@ -72,3 +72,14 @@ def test_edge_cases():
     np.testing.assert_array_equal(V, lib.biot_savart_rings(corners, rvc, gam, P))
     with pytest.raises(lib.VlmError):
         lib.biot_savart_rings(corners, rvc, gam, P, precision=7)
+
+
+@pytest.mark.gpu
+def test_bounded_wait_gives_up_and_context_stays_usable():
+    """A pipeline wait that nothing releases gives up after its poll limit and
+    reports (no hang, no fault); the GPU keeps working afterwards."""
+    assert lib.selftest_bounded_wait(4096)
+    c = np.array([[[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]]], float)
+    V = lib.biot_savart_rings(c, np.full((1, 4), 0.01), np.array([1.0]), np.array([[0.5, 0.5, 0.3]]),
+                              lib.PREC_FP32)
+    assert np.all(np.isfinite(V)) and abs(V[0, 2]) > 0

@@ -60,9 +60,9 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 // Bounded wait for the phase with the given parity; false if the limit expired.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
   const uint32_t a = smem_u32(bar);
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -423,6 +423,16 @@ __global__ void k_near_apply(double* __restrict__ part, long long* __restrict__ 
   }
 }
 
+// Self-test of the bounded waits: one thread waits on an mbarrier that
+// nothing arrives on, with a short limit; the wait must give up and report.
+__global__ void k_wait_probe(uint32_t limit, int* out) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  out[0] = mbar_wait(&bar, 0, limit) ? 0 : 1;  // 1: the limit expired, as it must
+}
+
 // FP64 record -> FP32 record.  The edge vectors are differenced in FP64
 // (nearby corners cancel) and rounded once; everything else is FP32 (the
 // record is FP32; GB300's FP64 rate would make this kernel latency-bound).
@@ -549,6 +559,17 @@ int partial32_slots() {
     cache[dev] = std::max(1, sms) * std::max(1, per);
   }
   return cache[dev];
+}
+
+int selftest_bounded_wait(uint32_t limit) {
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return -1;
+  int h = -1;
+  count_launch();
+  k_wait_probe<<<1, 32>>>(limit, d);
+  cudaError_t e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? h : -1;
 }
 
 }  // namespace vlm

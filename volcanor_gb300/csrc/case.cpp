@@ -1685,6 +1685,17 @@ int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V) {
   return guard([&]() { c->c.vindPoints(P, M, V); });
 }
 
+int vlm_selftest_bounded_wait(int limit, int* expired) {
+  if (!expired || limit <= 0) return VLM_ERR_INVALID;
+  const int r = selftest_bounded_wait((uint32_t)limit);
+  if (r < 0) {
+    g_err = "CUDA error in the bounded-wait self-test";
+    return VLM_ERR_CUDA;
+  }
+  *expired = r;
+  return VLM_OK;
+}
+
 void vlm_default_surrogate_options(vlm_surrogate_options* o) {
   if (!o) return;
   o->enable = 1;

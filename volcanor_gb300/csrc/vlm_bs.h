@@ -124,6 +124,11 @@ void launch_combine(const double* part, int M, const Group* groups, int ngroups,
 void launch_combine_unordered(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
                               double* out, cudaStream_t s);
 
+// Launches a wait that nothing releases, bounded by `limit` polls: 1 if it
+// gave up and reported (the expected outcome), 0 if it did not, -1 on a CUDA
+// error.
+int selftest_bounded_wait(uint32_t limit);
+
 // Isolated rings (vlm_biot_savart_rings): AoS corners (N x 4 x 3), rvc (N x 4), gam (N) -> FP64 records.
 void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,
                            cudaStream_t s);

@@ -83,6 +83,7 @@ SIGNATURES = {
     "vlm_case_profile_eval": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
     "vlm_case_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "vlm_case_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "vlm_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "vlm_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
                                         ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
     "vlm_batch_destroy": (ctypes.c_int, [_vp]),
@@ -417,3 +418,10 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def selftest_bounded_wait(limit: int = 4096) -> bool:
+    """True when a device wait that nothing releases gave up and reported."""
+    out = ctypes.c_int(-1)
+    _err(load().vlm_selftest_bounded_wait(limit, ctypes.byref(out)))
+    return out.value == 1
