@@ -136,7 +136,7 @@ int vlm_case_start(vlm_case* c);
  * CFz) -- the rXXForceNonDim.csv columns (src/libPostprocess.f90:814-838). */
 int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows);
 /* Integer state: nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter,
- * nbConvect, wakeTruncateNt; nearPairs (near-field filament-target pairs of the
+ * nbConvect, wakeTruncateNt, rotorForcePlot; nearPairs (near-field filament-target pairs of the
  * last FP32 evaluation) and nodeChunks (chunks of the next step's wake-node
  * evaluation) describe this library's kernels. */
 int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
@@ -154,8 +154,20 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *   waF (blade)                     (3, 2, nFwake) far-wake filament nodes
  *   waF_gam, waF_rvc (blade)        (nFwake)
  *   velN, velF (blade)              (3, nNwake, ns+1), (3, nFwake) node velocities
- *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section */
+ *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section
+ *   forceDist (blade <= nbConvect)  (16, ns): the columns of rXXbYYForceDistNNNNN.csv
+ *                                   (src/libPostprocess.f90:850-878) for the current iteration
+ *   forceDim                        (11): the rXXForceDim.csv values (src/libPostprocess.f90:840-846) */
 int64_t vlm_case_get(vlm_case* c, const char* name, int blade, double* out, int64_t cap);
+/* The rXXParams.json text the reference writes at start-up (params2file,
+ * src/libPostprocess.f90:52-141): the case's parameters after rotor_init in
+ * the reference's key order and number layout.  Copies at most cap-1 bytes
+ * and a terminating NUL into buf (buf may be NULL when cap is 0); returns the
+ * full text length, or -1 on error. */
+int64_t vlm_case_params_json(vlm_case* c, char* buf, int64_t cap);
+/* The same text from the case files alone (host only, no device use). */
+int64_t vlm_params_json(const char* config_text, const char* geom_text, const char* base_dir, char* buf,
+                        int64_t cap);
 /* Induced velocity of the current wing + wake at M points (probes / gridgen:
  * src/libPostprocess.f90:333-361, src/gridgen.f90:115-140). */
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V);

@@ -75,6 +75,9 @@ struct Case {
   bool loadsForked = false;
   std::vector<StepPlan> plans;  // index = iteration (0..nt)
   double* hFrames = nullptr;    // pinned host copy of every frame; uploaded per vlm_case_step call
+  // per frame, per blade: the blade's yAxis[3] and secTauCapSpan[ns][3], which
+  // only the sectional output (force2file) reads
+  std::vector<double> secAxes;
   std::vector<Group> hGroups;
   std::vector<Chunk> hChunks;
   Group* dGroups = nullptr;
@@ -210,11 +213,23 @@ struct Case {
 
     // frames: 0 = after the initial pitch, k = after the kinematics of step k
     std::vector<double> frames((size_t)(nt + 1) * d.fl.size);
+    const size_t axStride = (size_t)d.nb * (3 + 3 * d.ns);
+    secAxes.assign((size_t)(nt + 1) * axStride, 0.0);
+    auto putAxes = [&](int k) {
+      double* o = secAxes.data() + (size_t)k * axStride;
+      for (int b = 0; b < d.nb; ++b) {
+        const Blade& B = W.bl[b];
+        *o++ = B.yA.x, *o++ = B.yA.y, *o++ = B.yA.z;
+        for (int is = 0; is < d.ns; ++is) *o++ = B.secTauS[is].x, *o++ = B.secTauS[is].y, *o++ = B.secTauS[is].z;
+      }
+    };
     W.start_pitch();
     W.write_frame(frames.data());
+    putAxes(0);
     for (int k = 1; k <= nt; ++k) {
       W.advance(k);
       W.write_frame(frames.data() + (size_t)k * d.fl.size);
+      putAxes(k);
     }
     // plans
     plans.assign(nt + 1, StepPlan());
@@ -308,7 +323,7 @@ struct Case {
     s.secCD = dalloc<double>(nsec, owned);
     s.secCLu = dalloc<double>(nsec, owned);
     s.bladeForce = dalloc<double>((size_t)nb * 12, owned);
-    s.rotorLift = dalloc<double>(3, owned);
+    s.rotorLift = dalloc<double>(6, owned);
     s.ctHist = dalloc<double>((size_t)(nt + 1) * 10, owned);
     s.err = dalloc<int>(4, owned);
     s.devIter = dalloc<int>(1, owned);
@@ -910,7 +925,7 @@ struct Case {
         {s.secLift, 3 * nsec * D}, {s.secForceInertial, 3 * nsec * D}, {s.secLiftUnsteady, 3 * nsec * D},
         {s.secLiftInPlane, 3 * nsec * D}, {s.secLiftOutPlane, 3 * nsec * D}, {s.secCL, nsec * D},
         {s.secCD, nsec * D},       {s.secCLu, nsec * D},           {s.bladeForce, nb * 12 * D},
-        {s.rotorLift, 3 * D},      {s.ctHist, (size_t)(W.nt + 1) * 10 * D}};
+        {s.rotorLift, 6 * D},      {s.ctHist, (size_t)(W.nt + 1) * 10 * D}};
     for (int k = 0; k < 7; ++k) {
       v.push_back({s.vN[k], nb * std::max(d.NW, 1) * (ns + 1) * 3 * D});
       v.push_back({s.vF[k], nfar * 3 * D});
@@ -923,7 +938,7 @@ struct Case {
     }
     return v;
   }
-  static constexpr uint64_t kCkptMagic = 0x3154504b434d4c56ull;  // "VLMCKPT1"
+  static constexpr uint64_t kCkptMagic = 0x3254504b434d4c56ull;  // "VLMCKPT2"
   std::vector<int64_t> ckptHeader() const {
     return {(int64_t)kCkptMagic, iter, d.nb, d.nc, d.ns, d.NW, d.NF, W.nt, opt.precision, opt.sum_chunk,
             refine ? 1 : 0};
@@ -1035,6 +1050,60 @@ struct Case {
     return h;
   }
 
+  // getAngleTan (src/libMath.f90:224-236)
+  static double angleTan(d3 a, d3 b) {
+    const double ma = sumsq3(a), mb = sumsq3(b), dd = dot3(a, b);
+    return std::atan2(std::sqrt(ma * mb - dd * dd), dd);
+  }
+
+  // The sixteen per-section columns force2file writes to
+  // rXXbYYForceDistNNNNN.csv (src/libPostprocess.f90:850-878) for the current
+  // iteration, with the angles of blade_calc_secAlpha
+  // (src/classdef.f90:2234-2265) evaluated here from the device's sectional
+  // resultant velocity and the host's copy of the step's kinematics.  Row
+  // major: ns rows of secSpan secCL secCD secCLu secLift secDrag secLiftInPl
+  // secLiftOutPl secArea secVel secChord secTheta secAlpha secPhi secViz secVix.
+  std::vector<double> forceDist(int b) {
+    const size_t ns = d.ns, off = (size_t)b * ns;
+    const auto rv = dget(s.secResVel + 3 * off, 3 * ns), lift = dget(s.secLift + 3 * off, 3 * ns);
+    const auto inP = dget(s.secLiftInPlane + 3 * off, 3 * ns), outP = dget(s.secLiftOutPlane + 3 * off, 3 * ns);
+    const auto cl = dget(s.secCL + off, ns), cd = dget(s.secCD + off, ns), clu = dget(s.secCLu + off, ns);
+    const double* fr = hFrames + (size_t)iter * d.fl.size;
+    const double* ax = secAxes.data() + (size_t)iter * d.nb * (3 + 3 * ns) + (size_t)b * (3 + 3 * ns);
+    auto at = [](const double* p) { return mk3(p[0], p[1], p[2]); };
+    const d3 hub = at(fr + d.fl.rot + 3), zAF = at(fr + d.fl.ax + 9 * b + 6), yAxis = at(ax);
+    const Blade& B = W.bl[b];
+    std::vector<double> v;
+    v.reserve(16 * ns);
+    for (size_t is = 0; is < ns; ++is) {
+      const double* sec = fr + d.fl.sec + (off + is) * kSec;
+      const d3 tauC = at(sec), normal = at(sec + 3), secCP = at(sec + 6), tauS = at(ax + 3 + 3 * is);
+      const d3 velCPm = at(fr + d.fl.pan + ((size_t)b * d.npan + is * d.nc) * kPan + 24);  // panel (1, is)
+      const d3 r = at(rv.data() + 3 * is);
+      const double alpha = std::atan2(dot3(r, normal), dot3(r, tauC));
+      const double phi = angleTan(r, noproj3(velCPm, tauS));
+      const d3 vi = r - velCPm;
+      const double vix = norm3(noproj3(vi, tauS) - mk3(0.0, 0.0, vi.z));
+      const double theta = kPi * 0.5 - angleTan(neg3(tauC), zAF);
+      const double row[16] = {dot3(secCP - hub, yAxis), cl[is], cd[is], clu[is], norm3(at(lift.data() + 3 * is)),
+                              norm3(zero3()), norm3(at(inP.data() + 3 * is)), norm3(at(outP.data() + 3 * is)),
+                              B.secArea[is], norm3(r), B.secChord[is], theta * kRad2Deg, alpha * kRad2Deg,
+                              phi * kRad2Deg, vi.z, vix};
+      v.insert(v.end(), row, row + 16);
+    }
+    return v;
+  }
+
+  // The eleven values force2file writes to rXXForceDim.csv after the
+  // iteration (src/libPostprocess.f90:840-846): |lift|, |drag|, lift, drag,
+  // forceInertial.  Drag is zero for the circulation-based loads
+  // (blade_calc_force_gamma, src/classdef.f90:1704-1896).
+  std::vector<double> forceDim() {
+    const auto lf = dget(s.rotorLift, 6);
+    const d3 L = mk3(lf[0], lf[1], lf[2]);
+    return {norm3(L), norm3(zero3()), L.x, L.y, L.z, 0.0, 0.0, 0.0, lf[3], lf[4], lf[5]};
+  }
+
   int64_t get(const std::string& k, int blade, double* out, int64_t cap) {
     useDevice();
     std::vector<double> v;
@@ -1065,6 +1134,8 @@ struct Case {
     else if (bok && k == "secLiftDir") v = dget(s.secLiftDir + 3 * b * ns, 3 * ns);
     else if (bok && k == "secChordwiseResVel") v = dget(s.secResVel + 3 * b * ns, 3 * ns);
     else if (bok && k == "secLift") v = dget(s.secLift + 3 * b * ns, 3 * ns);
+    else if (bok && b < d.nbC && k == "forceDist") v = forceDist(b);
+    else if (k == "forceDim") v = forceDim();
     else if (bok && (k == "CP" || k == "nCap" || k == "vr")) {
       auto f = dget(frame(iter), d.fl.size);
       for (size_t p = 0; p < npan; ++p) {
@@ -1652,6 +1723,7 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value) {
   else if (k == "iter") *value = C.iter;
   else if (k == "nbConvect") *value = C.d.nbC;
   else if (k == "wakeTruncateNt") *value = C.W.P.wakeTruncateNt;
+  else if (k == "rotorForcePlot") *value = C.W.sw.rotorForcePlot;
   else if (k == "nearPairs" || k == "nodeChunks") {
     // near-field filament-target pairs of the last FP32 evaluation; chunks
     // of the next step's wake-node evaluation
@@ -1678,6 +1750,35 @@ int64_t vlm_case_get(vlm_case* c, const char* name, int blade, double* out, int6
   int64_t n = -1;
   const int rc = guard([&]() { n = c->c.get(name, blade, out, cap); });
   return rc == VLM_OK ? n : -1;
+}
+
+static int64_t copy_text(const std::string& t, char* buf, int64_t cap) {
+  if (cap > 0) {
+    const size_t n = std::min<size_t>(t.size(), (size_t)cap - 1);
+    std::memcpy(buf, t.data(), n);
+    buf[n] = 0;
+  }
+  return (int64_t)t.size();
+}
+
+int64_t vlm_case_params_json(vlm_case* c, char* buf, int64_t cap) {
+  if (!c || cap < 0 || (cap > 0 && !buf)) return -1;
+  std::string t;
+  if (guard([&]() { t = c->c.W.params_json(); }) != VLM_OK) return -1;
+  return copy_text(t, buf, cap);
+}
+
+int64_t vlm_params_json(const char* config_text, const char* geom_text, const char* base_dir, char* buf,
+                        int64_t cap) {
+  if (!config_text || !geom_text || cap < 0 || (cap > 0 && !buf)) return -1;
+  std::string t;
+  const int rc = guard([&]() {
+    vlm::Wing w;
+    w.load(config_text, geom_text, base_dir ? base_dir : "");
+    t = w.params_json();
+  });
+  if (rc != VLM_OK) return -1;
+  return copy_text(t, buf, cap);
 }
 
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V) {

@@ -1149,6 +1149,7 @@ __global__ void k_loads(Dims d, DevState s, const double* fr, int iter) {
       }
     }
     st3(s.rotorLift, L);
+    st3(s.rotorLift + 3, FI);
     const double D = d.nonDimDenom;
     const double sl = fsign1(dot3(L, ld3(fr + d.fl.rot)));
     double* row = s.ctHist + 10 * (size_t)iter;

@@ -76,7 +76,7 @@ struct DevState {
   double *secResVel, *secLiftDir, *secDragDir, *secLift, *secForceInertial, *secLiftUnsteady, *secLiftInPlane,
       *secLiftOutPlane, *secCL, *secCD, *secCLu;
   double *bladeForce;  // [nb][4][3]: forceInertial, lift, drag(0), liftUnsteady
-  double* rotorLift;   // [3] previous-step lift (liftPrev)
+  double* rotorLift;   // [6] lift (liftPrev of the next step), forceInertial
   double* ctHist;      // [(nt+1) * 10]
   // N-body scratch
   double *rec64, *targets, *part, *outv;

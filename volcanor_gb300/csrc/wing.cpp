@@ -5,7 +5,9 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
@@ -251,6 +253,15 @@ void Wing::readGeom(const Namelist& g) {
   if (!ver.empty() && std::fabs(to_double(ver) - 0.15) > 1e-12) throw std::runtime_error("geomXX.nml template version does not match");
   RotorParams& r = P;
   r.surfaceType = g.i("SURFACE", "surfaceType");
+  r.imagePlane = g.i("SURFACE", "imagePlane");
+  r.imageRotorNum = g.i("SURFACE", "imageRotorNum");
+  r.thetaTwist = g.d("GEOMPARAMS", "thetaTwist");
+  r.nAirfoils = g.i("GEOMPARAMS", "nAirfoils");
+  r.alpha0 = r.nAirfoils > 0 ? g.d("AIRFOILS", "alpha0") : 0.0;
+  r.Iflap = g.d("DYNAMICS", "Iflap");
+  r.cflap = g.d("DYNAMICS", "cflap");
+  r.kflap = g.d("DYNAMICS", "kflap");
+  r.MflapConstant = g.d("DYNAMICS", "MflapConstant");
   r.nb = g.i("PANELS", "nb", 1);
   r.propConvention = g.i("PANELS", "propConvention");
   r.spanSpacing = g.i("PANELS", "spanSpacing", 1);
@@ -472,6 +483,7 @@ void Wing::init() {
   r.pts = r.pts * kDeg2Rad;
   r.preconeAngle = r.preconeAngle * kDeg2Rad;
   r.psiStart = r.psiStart * kDeg2Rad;
+  r.thetaTwist = r.thetaTwist * kDeg2Rad;  // read, converted and printed, never applied to the geometry
   r.spanwiseCore = r.spanwiseCore * r.chord;
   for (auto& s : r.streamwiseCoreVec) s = s * r.chord;
   rollupStart = (int)std::ceil(r.rollupStartRadius * double(ns));
@@ -733,6 +745,140 @@ void Wing::write_frame(double* out) const {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) r[10 + 9 * (b - 1) + 3 * i + j] = T.a[i][j];
   }
+}
+
+namespace {
+
+// List-directed output as the reference's golden rXXParams.json files show
+// it: integers right-justified in 12 columns; reals in 24 columns, as
+// F-form with 15 significant digits followed by 5 blanks when
+// 0.1 <= |x| < 1e15, else (and for zero) as d.ddddddddddddddd with a signed
+// three-digit exponent.  A blank separates a number from a following
+// character item.
+std::string ld_int(long v) {
+  char b[32];
+  std::snprintf(b, sizeof b, "%12ld", v);
+  return b;
+}
+
+std::string ld_real(double x) {
+  char b[64];
+  if (x != 0.0 && std::isfinite(x)) {
+    std::snprintf(b, sizeof b, "%.14e", std::fabs(x));  // rounded to 15 significant digits
+    const int e10 = std::atoi(std::strchr(b, 'e') + 1);
+    if (e10 >= -1 && e10 <= 14) {
+      char f[48];
+      std::snprintf(f, sizeof f, "%.*f", 14 - e10, x);
+      std::snprintf(b, sizeof b, "%19s     ", f);
+      return b;
+    }
+  }
+  if (!std::isfinite(x)) {
+    std::snprintf(b, sizeof b, "%24s", std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity"));
+    return b;
+  }
+  char m[48];
+  int e10 = 0;
+  if (x != 0.0) {
+    std::snprintf(m, sizeof m, "%.15e", x);
+    char* e = std::strchr(m, 'e');
+    e10 = std::atoi(e + 1);
+    *e = 0;
+  } else {
+    std::snprintf(m, sizeof m, "%.15f", 0.0);
+  }
+  char t[64];
+  std::snprintf(t, sizeof t, "%sE%c%03d", m, e10 < 0 ? '-' : '+', std::abs(e10));
+  std::snprintf(b, sizeof b, "%24s", t);
+  return b;
+}
+
+}  // namespace
+
+// params2file (src/libPostprocess.f90:52-141): the case's parameters after
+// rotor_init, in the reference's key order; step counts given in chords or
+// revolutions are the converted ones, angles are printed in degrees except
+// phiThetaPsi (radians, as the reference prints rotor%pts).
+std::string Wing::params_json() const {
+  const RotorParams& r = P;
+  std::string o = " {\n";
+  auto ki = [&](const char* k, long v, bool last = false) {
+    o += std::string(" \"") + k + "\": " + ld_int(v) + (last ? "" : " ,") + "\n";
+  };
+  auto kr = [&](const char* k, double v, bool last = false) {
+    o += std::string(" \"") + k + "\": " + ld_real(v) + (last ? "" : " ,") + "\n";
+  };
+  ki("nt", nt);
+  kr("dt", dt);
+  ki("nr", nr);
+  ki("restartWriteNt", sw.restartWriteNt);
+  ki("restartFromNt", sw.restartFromNt);
+  ki("ntSub", sw.ntSub);
+  ki("ntSubInit", sw.ntSubInit);
+  kr("density", density);
+  kr("velSound", velSound);
+  ki("wakePlot", sw.wakePlot);
+  ki("wakeTipPlot", sw.wakeTipPlot);
+  ki("rotorForcePlot", sw.rotorForcePlot);
+  ki("gridPlot", sw.gridPlot);
+  ki("wakeDissipation", sw.wakeDissipation);
+  ki("wakeStrain", sw.wakeStrain);
+  ki("wakeBurst", sw.wakeBurst);
+  ki("slowStart", sw.slowStart);
+  ki("slowStartNt", sw.slowStartNt);
+  ki("fdScheme", sw.fdScheme);
+  ki("initWakeVelNt", sw.initWakeVelNt);
+  ki("probe", sw.probe);
+  ki("nb", r.nb);
+  ki("propConvention", r.propConvention);
+  std::string gf = r.geometryFile.substr(0, 30);  // character(len=30)
+  gf.resize(30, ' ');
+  o += " \"geometryFile\": \"" + gf + "\",\n";
+  ki("spanSpacing", r.spanSpacing);
+  ki("chordSpacing", r.chordSpacing);
+  ki("nCamberFiles", r.nCamberFiles);
+  ki("surfaceType", r.surfaceType);
+  ki("imagePlane", r.imagePlane);
+  ki("imageRotorNum", r.imageRotorNum);
+  ki("nc", r.nc);
+  ki("ns", r.ns);
+  ki("nNwake", r.nNwake);
+  kr("radius", r.radius);
+  kr("root_cut", r.root_cut);
+  kr("chord", r.chord);
+  kr("preconeAngle", r.preconeAngle * kRad2Deg);
+  kr("Omega", r.Omega);
+  kr("phi", r.pts.x);
+  kr("theta", r.pts.y);
+  kr("psi", r.pts.z);
+  kr("theta0", r.controlPitch.x * kRad2Deg);
+  kr("thetaC", r.controlPitch.y * kRad2Deg);
+  kr("thetaS", r.controlPitch.z * kRad2Deg);
+  kr("thetaTwist", r.thetaTwist * kRad2Deg);
+  kr("u", r.velBody.x);
+  kr("v", r.velBody.y);
+  kr("w", r.velBody.z);
+  kr("nonDimForceDenom", nonDimDenom);
+  kr("alpha0", r.nAirfoils > 0 ? r.alpha0 : 0.0);
+  ki("wakeTruncateNt", r.wakeTruncateNt);
+  ki("prescWakeNt", r.prescWakeNt);
+  kr("initWakeVel", r.initWakeVel);
+  kr("psiStart", r.psiStart * kRad2Deg);
+  kr("forceCalcSwitch", double(r.forceCalcSwitch) * kRad2Deg);
+  kr("apparentViscCoeff", r.apparentViscCoeff);
+  kr("decayCoeff", r.decayCoeff);
+  ki("axisymmetrySwitch", r.axisymmetrySwitch);
+  ki("bladeDynamicsSwitch", r.bladeDynamicsSwitch);
+  kr("flapInitial", r.flapInitial);
+  kr("dFlapInitial", r.dflapInitial);
+  kr("Iflap", r.Iflap);
+  kr("cflap", r.cflap);
+  kr("kflap", r.kflap);
+  kr("MflapConstant", r.MflapConstant);
+  ki("pitchDynamicsSwitch", r.pitchDynamicsSwitch);
+  kr("dpitch", r.dpitch, true);
+  o += " }\n";
+  return o;
 }
 
 }  // namespace vlm

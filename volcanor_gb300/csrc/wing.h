@@ -53,6 +53,9 @@ struct RotorParams {  // rotor_readGeom inputs (src/classdef.f90:2541-2767)
   int bladeDynamicsSwitch = 0, pitchDynamicsSwitch = 0, bodyDynamicsSwitch = 0;
   double flapInitial = 0, dflapInitial = 0, dpitch = 0;
   int inflowPlotSwitch = 0, gammaPlotSwitch = 0, skewPlotSwitch = 0;
+  // read only to be echoed into rXXParams.json
+  int imagePlane = 0, imageRotorNum = 0, nAirfoils = 0;
+  double thetaTwist = 0, Iflap = 0, cflap = 0, kflap = 0, MflapConstant = 0, alpha0 = 0;
 };
 
 struct Panel {
@@ -84,6 +87,8 @@ class Wing {
   void advance(int iter);              // src/main.f90:412-463 kinematics of one step
   void write_frame(double* out) const;  // see vlm_solver.h for the layout
   double gettheta(double psi, int ib) const;
+  // rXXParams.json text (params2file, src/libPostprocess.f90:52-141)
+  std::string params_json() const;
 
   int nt = 0, nr = 1;
   double dt = 0, density = 1, velSound = 330, kinematicVisc = 0;

@@ -79,6 +79,8 @@ SIGNATURES = {
     "vlm_case_get_int": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_i64)]),
     "vlm_case_get": (_i64, [_vp, ctypes.c_char_p, ctypes.c_int, _dp, _i64]),
     "vlm_case_vind_points": (ctypes.c_int, [_vp, _dp, _i64, _dp]),
+    "vlm_case_params_json": (_i64, [_vp, ctypes.c_char_p, _i64]),
+    "vlm_params_json": (_i64, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _i64]),
     "vlm_case_last_step_ms": (ctypes.c_int, [_vp, _dp]),
     "vlm_case_profile_eval": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
     "vlm_case_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
@@ -128,11 +130,15 @@ def load(build_if_missing: bool = True):
     return _lib
 
 
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().vlm_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
 def _err(code: int):
     if code != VLM_OK:
-        buf = ctypes.create_string_buffer(1024)
-        load().vlm_last_error(buf, 1024)
-        raise VlmError(code, buf.value.decode(errors="replace"))
+        raise VlmError(code, last_error())
 
 
 def _ptr(a: np.ndarray):
@@ -168,6 +174,19 @@ def device_info(device: int = 0):
     sm, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     _err(load().vlm_device_info(device, ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)))
     return sm.value, ma.value, mi.value
+
+
+def params_json(config_text: str, geom_text: str, base_dir: str | os.PathLike = "") -> str:
+    """The rXXParams.json text of a case from its config.nml / geomXX.nml
+    text (host-side parsing only; no GPU needed)."""
+    L = load()
+    args = (config_text.encode(), geom_text.encode(), str(base_dir).encode())
+    n = L.vlm_params_json(*args, None, 0)
+    if n < 0:
+        raise VlmError(1, last_error())
+    buf = ctypes.create_string_buffer(int(n) + 1)
+    L.vlm_params_json(*args, buf, n + 1)
+    return buf.value.decode()
 
 
 def biot_savart_rings(corners, rvc, gam, P, precision: int = PREC_FP64) -> np.ndarray:
@@ -280,6 +299,25 @@ class Case:
 
     def ct_hist(self) -> np.ndarray:
         return self.get("ct_hist").reshape(-1, 10)
+
+    def force_dist(self, blade: int = 1) -> np.ndarray:
+        """(ns, 16) sectional loads of the current iteration in the columns of
+        rXXbYYForceDistNNNNN.csv (blade 1..nbConvect)."""
+        return self.get("forceDist", blade).reshape(-1, 16)
+
+    def force_dim(self) -> np.ndarray:
+        """The eleven rXXForceDim.csv values of the current iteration."""
+        return self.get("forceDim")
+
+    def params_json(self) -> str:
+        """The rXXParams.json text of this case."""
+        L = load()
+        n = L.vlm_case_params_json(self._h, None, 0)
+        if n < 0:
+            raise VlmError(1, "vlm_case_params_json failed")
+        buf = ctypes.create_string_buffer(int(n) + 1)
+        L.vlm_case_params_json(self._h, buf, n + 1)
+        return buf.value.decode()
 
     def vind_points(self, P) -> np.ndarray:
         P = _c64(P).reshape(-1, 3)
