@@ -57,6 +57,10 @@ typedef struct vlm_options {
                           -1 = 1 for the FP32 precisions, 0 for FP64 (default) */
   int nbody_slots;     /* resident block slots the FP32 chunk planner plans for (0 = the whole
                           device; a batch gives each of its cases a share) */
+  int lattice;         /* FP32 precisions: evaluate each near-wake lattice edge by edge, a
+                          filament shared by two rings once with their circulation
+                          difference (0 = ring by ring as the reference; -1 / nonzero =
+                          lattice form, the default).  No effect on VLM_PREC_FP64. */
 } vlm_options;
 
 /* ---- library ------------------------------------------------------------ */

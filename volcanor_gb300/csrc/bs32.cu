@@ -9,8 +9,10 @@
 // so consumer warps never wait for one another.  Each staged record is read
 // with broadcast LDS.128 and evaluated for both targets of a thread.
 //
-// Per target and ring: 4 corner vectors r_k = P - c_k with rsqrt norms, then
-// per filament k -> j = k+1 the Vatistas n=2 kernel (src/classdef.f90:476-503)
+// Per target and record: corner vectors r_k = P - c_k with rsqrt norms (c3's
+// only when edge 2 or 3 carries circulation: a lattice-form interior ring has
+// just edges 0 and 1), then per filament k -> j = k+1 the Vatistas n=2
+// kernel (src/classdef.f90:476-503)
 //   v = (r_k x r_j) w_k (e.r_k/|r_k| - e.r_j/|r_j|) / sqrt((rvc|e|)^4 + |r_k x r_j|^4)
 // with e.r_j = e.r_k - |e|^2 and the source-only terms hoisted into the
 // record, the weight w_k = gam/4pi folded into e.  A target on the filament
@@ -149,8 +151,65 @@ __device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec,
   if (dst) staged += total;
 }
 
-// Corner vectors r_k = P - c_k and 1/|r_k| (|r|^2 + 1e-30: a target on a
-// corner gets a finite 1/|r|, times r = 0).
+// Corner vector r = P - c and 1/|r| (|r|^2 + 1e-30: a target on a corner
+// gets a finite 1/|r|, times r = 0).
+__device__ __forceinline__ void corner_vector(float px, float py, float pz, float cx, float cy, float cz, float& rx,
+                                              float& ry, float& rz, float& inv) {
+  rx = px - cx;
+  ry = py - cy;
+  rz = pz - cz;
+  inv = rsqrtf(fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, kS2Min))));
+}
+
+// The staged fields of one record that the filament evaluations read.
+struct RecView {
+  float ex[4], ey[4], ez[4], eev[4], a4v[4];
+};
+__device__ __forceinline__ void load_view(const float4* __restrict__ R4, RecView& v) {
+  const float4 q3 = R4[3], q4 = R4[4], q5 = R4[5];  // weighted edges
+  const float4 ee = R4[6], a4 = R4[7];
+  v.ex[0] = q3.x, v.ex[1] = q3.w, v.ex[2] = q4.z, v.ex[3] = q5.y;
+  v.ey[0] = q3.y, v.ey[1] = q4.x, v.ey[2] = q4.w, v.ey[3] = q5.z;
+  v.ez[0] = q3.z, v.ez[1] = q4.y, v.ez[2] = q5.x, v.ez[3] = q5.w;
+  v.eev[0] = ee.x, v.eev[1] = ee.y, v.eev[2] = ee.z, v.eev[3] = ee.w;
+  v.a4v[0] = a4.x, v.a4v[1] = a4.y, v.a4v[2] = a4.z, v.a4v[3] = a4.w;
+}
+
+// Adds the FP32 velocity of filament K (c_K -> c_{K+1}) at one target, from
+// the corner vectors (r, 1/|r|) of its two ends.  CHECK: also tests the
+// filament against its near zone (record fields [32+K], [36+K], [40+K]); a
+// near filament is left out and reported through the return value.
+template <int K, bool CHECK>
+__device__ __forceinline__ bool fil_fp32(const float4* __restrict__ R4, const RecView& v, float rxk, float ryk,
+                                         float rzk, float invk, float rxj, float ryj, float rzj, float invj, float& ax,
+                                         float& ay, float& az, bool mine) {
+  const float kx = fmaf(ryk, rzj, -rzk * ryj);
+  const float ky = fmaf(rzk, rxj, -rxk * rzj);
+  const float kz = fmaf(rxk, ryj, -ryk * rxj);
+  const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
+  // w (e.r_k/|r_k| - e.r_j/|r_j|) with the weight folded into e
+  const float tt = fmaf(v.ex[K], rxk, fmaf(v.ey[K], ryk, v.ez[K] * rzk));
+  const float d = fmaf(tt, invk, -(tt - v.eev[K]) * invj);
+  float f = d * rsqrtf(fmaf(c2, c2, v.a4v[K]));
+  bool nr = false;
+  if (CHECK) {
+    const float thr = reinterpret_cast<const float*>(R4)[32 + K];
+    const float lo = reinterpret_cast<const float*>(R4)[36 + K];
+    const float hi = reinterpret_cast<const float*>(R4)[40 + K];
+    // exact zeros (target on the filament line) stay in the FP32 sum; only
+    // a target inside the record's sphere can flag (so that which pairs are
+    // near does not depend on the other lanes of its warp)
+    nr = mine && c2 < thr && c2 > kS2Min && tt > lo && tt < hi;
+    f = nr ? 0.f : f;
+  }
+  ax = fmaf(f, kx, ax);
+  ay = fmaf(f, ky, ay);
+  az = fmaf(f, kz, az);
+  return nr;
+}
+
+// A whole ring (all four edges active): the four corner vectors r_k = P - c_k
+// and 1/|r_k| (|r|^2 + 1e-30 as in corner_vector).
 __device__ __forceinline__ void corner_vectors(float px, float py, float pz, const float (&cx)[4], const float (&cy)[4],
                                                const float (&cz)[4], float (&rx)[4], float (&ry)[4], float (&rz)[4],
                                                float (&inv)[4]) {
@@ -163,8 +222,8 @@ __device__ __forceinline__ void corner_vectors(float px, float py, float pz, con
   }
 }
 
-// Adds the FP32 velocity of one record at one target (corner vectors r_k and
-// rsqrt norms given).  CHECK: also tests every filament against its near
+// Adds the FP32 velocity of a whole ring at one target (corner vectors r_k
+// and rsqrt norms given).  CHECK: also tests every filament against its near
 // zone, leaves the near ones out and returns their bit mask.
 template <bool CHECK>
 __device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, const float (&rx)[4], const float (&ry)[4],
@@ -211,6 +270,30 @@ __device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, con
   return msk;
 }
 
+// One lattice-form record at one target: corners c0..c2 and edges 0 and 1,
+// then c3 and the border edges 2 / 3 only where they carry circulation
+// (a whole ring takes all four).  CHECK: returns the mask of near filaments.
+template <bool CHECK>
+__device__ __forceinline__ unsigned rec_lat(const float4* __restrict__ R4, const RecView& v, const float (&cx)[4],
+                                            const float (&cy)[4], const float (&cz)[4], float px, float py, float pz,
+                                            float& ax, float& ay, float& az, bool mine = false) {
+  float rx[4], ry[4], rz[4], inv[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) corner_vector(px, py, pz, cx[k], cy[k], cz[k], rx[k], ry[k], rz[k], inv[k]);
+  unsigned msk = 0u;
+  if (fil_fp32<0, CHECK>(R4, v, rx[0], ry[0], rz[0], inv[0], rx[1], ry[1], rz[1], inv[1], ax, ay, az, mine)) msk |= 1u;
+  if (fil_fp32<1, CHECK>(R4, v, rx[1], ry[1], rz[1], inv[1], rx[2], ry[2], rz[2], inv[2], ax, ay, az, mine)) msk |= 2u;
+  const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
+  if (t2 || t3) {
+    corner_vector(px, py, pz, cx[3], cy[3], cz[3], rx[3], ry[3], rz[3], inv[3]);
+    if (t2 && fil_fp32<2, CHECK>(R4, v, rx[2], ry[2], rz[2], inv[2], rx[3], ry[3], rz[3], inv[3], ax, ay, az, mine))
+      msk |= 4u;
+    if (t3 && fil_fp32<3, CHECK>(R4, v, rx[3], ry[3], rz[3], inv[3], rx[0], ry[0], rz[0], inv[0], ax, ay, az, mine))
+      msk |= 8u;
+  }
+  return msk;
+}
+
 // One block = 8 consumer warps (256 threads x 2 targets) + 1 producer warp.
 // The producer's lane 0 streams the chunk's records through kStages shared
 // stages with bulk copies; consumers wait on a stage's FULL barrier, compute,
@@ -221,7 +304,9 @@ constexpr int kConsumerWarps = 8;
 constexpr int kBlockW = (kConsumerWarps + 1) * 32;
 static_assert(kConsumerWarps * 32 * kTPT == kTargetsPerBlock32, "targets per block");
 
-template <bool NEAR>
+// LAT: the records are in lattice form (edges 2 and 3 marked when they carry
+// no circulation); otherwise every record is evaluated as a whole ring.
+template <bool NEAR, bool LAT>
 __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restrict__ rec32,
                                                          const Chunk* __restrict__ chunks,
                                                          const double* __restrict__ P, int M,
@@ -320,28 +405,76 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
             const int rec = ch.rec_begin + t * kTileW + r;
 #pragma unroll
             for (int u = 0; u < kTPT; ++u) {
-              float rx[4], ry[4], rz[4], inv[4];
-              corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-              const unsigned msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u], candu[u]);
+              unsigned msk;
+              if (LAT) {
+                RecView v;
+                load_view(R4, v);
+                msk = rec_lat<true>(R4, v, cx, cy, cz, px[u], py[u], pz[u], ax[u], ay[u], az[u], candu[u]);
+              } else {
+                float rx[4], ry[4], rz[4], inv[4];
+                corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
+                msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u], candu[u]);
+              }
               near_append(msk, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
             }
             continue;
           }
-        }
-        if (NEAR) {
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) {
-            float rx[4], ry[4], rz[4], inv[4];
-            corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-            ring_fp32<false>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
+            if (LAT) {
+              RecView v;
+              load_view(R4, v);
+              rec_lat<false>(R4, v, cx, cy, cz, px[u], py[u], pz[u], ax[u], ay[u], az[u]);
+            } else {
+              float rx[4], ry[4], rz[4], inv[4];
+              corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
+              ring_fp32<false>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
+            }
           }
-        } else {
+        } else if (!LAT) {
           // both targets' corner vectors first: more independent work in flight
           float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx[u], ry[u], rz[u], inv[u]);
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) ring_fp32<false>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
+        } else {
+          // lattice form: both targets' c0..c2 vectors, edges 0 and 1, then
+          // the border edges 2 / 3 where they carry circulation (uniform
+          // branches: every lane evaluates the same record)
+          RecView v;
+          load_view(R4, v);
+          float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
+#pragma unroll
+          for (int u = 0; u < kTPT; ++u)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+              corner_vector(px[u], py[u], pz[u], cx[k], cy[k], cz[k], rx[u][k], ry[u][k], rz[u][k], inv[u][k]);
+#pragma unroll
+          for (int u = 0; u < kTPT; ++u) {
+            fil_fp32<0, false>(R4, v, rx[u][0], ry[u][0], rz[u][0], inv[u][0], rx[u][1], ry[u][1], rz[u][1], inv[u][1],
+                               ax[u], ay[u], az[u], false);
+            fil_fp32<1, false>(R4, v, rx[u][1], ry[u][1], rz[u][1], inv[u][1], rx[u][2], ry[u][2], rz[u][2], inv[u][2],
+                               ax[u], ay[u], az[u], false);
+          }
+          const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
+          if (t2 || t3) {
+#pragma unroll
+            for (int u = 0; u < kTPT; ++u)
+              corner_vector(px[u], py[u], pz[u], cx[3], cy[3], cz[3], rx[u][3], ry[u][3], rz[u][3], inv[u][3]);
+            if (t2) {
+#pragma unroll
+              for (int u = 0; u < kTPT; ++u)
+                fil_fp32<2, false>(R4, v, rx[u][2], ry[u][2], rz[u][2], inv[u][2], rx[u][3], ry[u][3], rz[u][3],
+                                   inv[u][3], ax[u], ay[u], az[u], false);
+            }
+            if (t3) {
+#pragma unroll
+              for (int u = 0; u < kTPT; ++u)
+                fil_fp32<3, false>(R4, v, rx[u][3], ry[u][3], rz[u][3], inv[u][3], rx[u][0], ry[u][0], rz[u][0],
+                                   inv[u][0], ax[u], ay[u], az[u], false);
+            }
+          }
         }
       }
 #pragma unroll
@@ -384,8 +517,8 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
 // velocity times the circulation), added in fixed point to the accumulators
 // of their (chunk, target).
 __global__ void k_near64(const NearPair* __restrict__ near, int* __restrict__ ctl, int near_cap,
-                         const double* __restrict__ rec64, const double* __restrict__ P, int M,
-                         unsigned long long* __restrict__ nacc) {
+                         const double* __restrict__ rec64, const double* __restrict__ ew,
+                         const double* __restrict__ P, int M, unsigned long long* __restrict__ nacc) {
   const int n = min(ctl[1], near_cap);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const NearPair np = near[i];
@@ -399,7 +532,7 @@ __global__ void k_near64(const NearPair* __restrict__ near, int* __restrict__ ct
       v = fil_near64(p, mk3(R[3 * k], R[3 * k + 1], R[3 * k + 2]), mk3(R[3 * j], R[3 * j + 1], R[3 * j + 2]),
                      R[12 + k]);
     }
-    v = v * R[16];
+    v = v * (ew ? ew[4 * (size_t)np.rec + np.k] : R[16]);
     unsigned long long* o = nacc + ((size_t)np.q * M + np.m) * 3;
     const double c[3] = {v.x, v.y, v.z};
     for (int a = 0; a < 3; ++a) {
@@ -436,7 +569,12 @@ __global__ void k_wait_probe(uint32_t limit, int* out) {
 // FP64 record -> FP32 record.  The edge vectors are differenced in FP64
 // (nearby corners cancel) and rounded once; everything else is FP32 (the
 // record is FP32; GB300's FP64 rate would make this kernel latency-bound).
-__global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near_factor, float* __restrict__ rec32) {
+// With edge weights ew (lattice form) edge k carries ew[k] and is active iff
+// ew[k] != 0; without, every filament of a record carries its gam unless the
+// record is skipped (|gam| <= eps with REC_SKIP), a single filament only its
+// first.  Inactive edges 2 and 3 are marked for the kernel to skip.
+__global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near_factor, float* __restrict__ rec32,
+                         const double* __restrict__ ew) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrec) return;
   const double* R = rec64 + (size_t)i * kRec64;
@@ -445,6 +583,7 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
   const double g = R[16];
   const bool skipped = (flags & REC_SKIP) && !(fabs(g) > kEps);
   const bool fil = flags & REC_FIL;
+  const double* EW = ew ? ew + 4 * (size_t)i : nullptr;
   // corner k (FP64) and core radius of filament k
   double cx[4], cy[4], cz[4];
   float rv[4];
@@ -471,7 +610,7 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
   bool anyNear = false;
   for (int k = 0; k < 4; ++k) {
     const int j = (k + 1) & 3;
-    const bool act = (!fil || k == 0) && !skipped;
+    const bool act = EW ? EW[k] != 0.0 : (!fil || k == 0) && !skipped;
     const float ex = (float)(cx[j] - cx[k]), ey = (float)(cy[j] - cy[k]), ez = (float)(cz[j] - cz[k]);
     const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
     const float sk = rv[k] * sqrtf(ee);
@@ -479,12 +618,12 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
     o[3 * k] = (float)cx[k];
     o[3 * k + 1] = (float)cy[k];
     o[3 * k + 2] = (float)cz[k];
-    const float wk = act ? w : 0.f;
+    const float wk = act ? (EW ? (float)(EW[k] * kInv4Pi) : w) : 0.f;
     o[12 + 3 * k] = wk * ex;
     o[12 + 3 * k + 1] = wk * ey;
     o[12 + 3 * k + 2] = wk * ez;
     o[24 + k] = wk * ee;
-    o[28 + k] = fmaxf(s2 * s2, 1e-36f);
+    o[28 + k] = EW && k >= 2 && !act ? -1.f : fmaxf(s2 * s2, 1e-36f);
     const bool on = act && nf > 0.f;
     const float nfs = nf * sk;
     o[32 + k] = on ? nfs * nfs : -1.f;
@@ -512,14 +651,16 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
 
 }  // namespace
 
-void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s) {
+void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s,
+                   const double* ew) {
   if (nrec <= 0) return;
   count_launch();
-  k_pack32<<<(nrec + 255) / 256, 256, 0, s>>>(rec64, nrec, near_factor, rec32);
+  k_pack32<<<(nrec + 255) / 256, 256, 0, s>>>(rec64, nrec, near_factor, rec32, ew);
 }
 
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
-                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s) {
+                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s,
+                      const double* ew) {
   if (M <= 0 || nchunks <= 0) return;
   const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
   // the dynamic shared-memory opt-in is per device; set it once on each
@@ -527,21 +668,27 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || !attr[dev].load(std::memory_order_acquire)) {
-    cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (dev >= 0 && dev < 64) attr[dev].store(true, std::memory_order_release);
   }
   dim3 grid((M + kTargetsPerBlock32 - 1) / kTargetsPerBlock32, nchunks);
   count_launch();
   if (near) {
-    k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    if (ew) k_partial32<true, true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    else k_partial32<true, false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
     count_launch();
-    k_near64<<<4 * 152, 128, 0, s>>>(near, ctl, near_cap, rec64, P, M, reinterpret_cast<unsigned long long*>(nacc));
+    k_near64<<<4 * 152, 128, 0, s>>>(near, ctl, near_cap, rec64, ew, P, M,
+                                     reinterpret_cast<unsigned long long*>(nacc));
     const size_t n = (size_t)M * nchunks * 3;
     count_launch();
     k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, 8 * 152), 256, 0, s>>>(part, nacc, n);
+  } else if (ew) {
+    k_partial32<false, true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
   } else {
-    k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    k_partial32<false, false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
   }
 }
 
@@ -552,10 +699,9 @@ int partial32_slots() {
   if (!cache[dev]) {
     int sms = 0, per = 0;
     const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
-    cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true>, kBlockW, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true, false>, kBlockW, smem);
     cache[dev] = std::max(1, sms) * std::max(1, per);
   }
   return cache[dev];

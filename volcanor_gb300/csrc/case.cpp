@@ -364,6 +364,7 @@ struct Case {
     scratchOwned.clear();
     s.rec64 = dalloc<double>((size_t)maxRecords * kRec64, scratchOwned);
     s.rec32 = dalloc<float>((size_t)maxRecords * kRec32, scratchOwned);
+    s.edgeW = lattice() ? dalloc<double>((size_t)maxRecords * 4, scratchOwned) : nullptr;
     s.targets = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.outv = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.part = dalloc<double>((size_t)maxPart * 3, scratchOwned);
@@ -452,10 +453,10 @@ struct Case {
       launch_partial64(s.rec64, ch, e.nchunks, P, M, s.part, stream);
     } else {
       const bool nearOn = prec == VLM_PREC_FP32_NEAR64;
-      launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream);
+      launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream, s.edgeW);
       VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
       launch_partial32(s.rec32, s.rec64, ch, e.nchunks, P, M, s.part, s.err + 2, nearOn ? s.near : nullptr,
-                       s.nearCap, s.nacc, stream);
+                       s.nearCap, s.nacc, stream, s.edgeW);
     }
     if (e.nchunks == 0) {
       VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M, stream));
@@ -487,6 +488,9 @@ struct Case {
   Surrogate surr;
   std::vector<SurrPlans> splans;
   std::vector<void*> surrOwned;
+
+  // lattice form of the near-wake rings for the FP32 precisions
+  bool lattice() const { return opt.precision != VLM_PREC_FP64 && opt.lattice != 0; }
 
   int nearNodeCount(int rowNear) const { return d.nbC * (d.NW - (rowNear - 1)) * (d.ns + 1); }
   int farRows(int rowFar) const { return std::max(d.NF - (rowFar - 1), 0); }
@@ -1017,13 +1021,14 @@ struct Case {
                   stream);
     const Chunk* ch = dChunks + pl.node.coff;
     const double nf = opt.precision == VLM_PREC_FP32_NEAR64 ? opt.near_factor : 0.0;
-    if (opt.precision != VLM_PREC_FP64) launch_pack32(s.rec64, pl.node.nrec, nf, s.rec32, stream);
+    if (opt.precision != VLM_PREC_FP64) launch_pack32(s.rec64, pl.node.nrec, nf, s.rec32, stream, s.edgeW);
     auto launch = [&]() {
       if (opt.precision == VLM_PREC_FP64) launch_partial64(s.rec64, ch, pl.node.nchunks, s.targets, M, s.part, stream);
       else {
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
         launch_partial32(s.rec32, s.rec64, ch, pl.node.nchunks, s.targets, M, s.part, s.err + 2,
-                         opt.precision == VLM_PREC_FP32_NEAR64 ? s.near : nullptr, s.nearCap, s.nacc, stream);
+                         opt.precision == VLM_PREC_FP32_NEAR64 ? s.near : nullptr, s.nearCap, s.nacc, stream,
+                         s.edgeW);
       }
     };
     launch();  // warm
@@ -1201,6 +1206,7 @@ struct Case {
       VLM_CUDA(cudaMemcpy(dP, P, (size_t)M * 3 * sizeof(double), cudaMemcpyHostToDevice));
       DevState t = s;
       t.rec64 = rec64;
+      t.edgeW = nullptr;  // ring by ring: the probe's record count is not the plans'
       launch_gather(d, t, frame(iter), dg, (int)g.size(), rec, rN, rF, false, stream);
       if (opt.precision == VLM_PREC_FP64) {
         launch_partial64(rec64, dc, nq, dP, (int)M, part, stream);
@@ -1414,6 +1420,7 @@ void vlm_default_options(vlm_options* o) {
   o->use_graph = 1;
   o->solve_mode = -1;
   o->nbody_slots = 0;
+  o->lattice = -1;
 }
 
 int vlm_device_info(int device, int* sm_count, int* cc_major, int* cc_minor) {

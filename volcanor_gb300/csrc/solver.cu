@@ -494,6 +494,41 @@ __global__ void k_scatter_nodes(Dims d, DevState s, const double* fr, int rowNea
 }
 
 // ---- source gather ----------------------------------------------------------
+// Lattice form of near-wake ring (b, i, j) (i the absolute row): the edge
+// weights of its record (see vlm_bs.h).  Ring (i, j-1)'s edge 2 runs from
+// its c2 to its c3, which are ring (i, j)'s c1 and c0, so with equal cores
+// the two filaments are one with the circulation difference; likewise ring
+// (i+1, j)'s edge 3 (its c3 -> c0 = ring (i, j)'s c2 -> c1).  Circulations
+// at or below eps count as zero (the skip of blade_vind_bywake,
+// src/classdef.f90:1452-1466).
+__device__ __forceinline__ bool same3(const double* a, const double* b) {
+  return a[0] == b[0] && a[1] == b[1] && a[2] == b[2];
+}
+__device__ void lattice_weights(const Dims& d, const DevState& s, const double* nc, int b, int i, int j, int rowNear,
+                                double* W) {
+  auto gam = [&](size_t r) {
+    const double g = s.nGam[r];
+    return fabs(g) > kEps ? g : 0.0;
+  };
+  // streamwise edge between stations: ring (i, jj-1) edge 2 == ring (i, jj) edge 0
+  auto mergeS = [&](int jj) {
+    const size_t a = ringI(d, b, i, jj - 1), c = ringI(d, b, i, jj);
+    return same3(nc + 12 * a + 9, nc + 12 * c) && same3(nc + 12 * a + 6, nc + 12 * c + 3) &&
+           s.nRvc[4 * a + 2] == s.nRvc[4 * c];
+  };
+  // spanwise edge between rows: ring (ii, j) edge 1 == ring (ii+1, j) edge 3
+  auto mergeC = [&](int ii) {
+    const size_t a = ringI(d, b, ii, j), c = ringI(d, b, ii + 1, j);
+    return same3(nc + 12 * c, nc + 12 * a + 3) && same3(nc + 12 * c + 9, nc + 12 * a + 6) &&
+           s.nRvc[4 * c + 3] == s.nRvc[4 * a + 1];
+  };
+  const double G = gam(ringI(d, b, i, j));
+  W[0] = j > 0 && mergeS(j) ? G - gam(ringI(d, b, i, j - 1)) : G;
+  W[1] = i + 1 < d.NW && mergeC(i) ? G - gam(ringI(d, b, i + 1, j)) : G;
+  W[2] = j + 1 < d.ns && mergeS(j + 1) ? 0.0 : G;
+  W[3] = i > rowNear - 1 && mergeC(i - 1) ? 0.0 : G;
+}
+
 __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* groups, int ngroups, int nrec,
                          int rowNear, int rowFar, int pred) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -512,6 +547,8 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
     for (int k = 0; k < 4; ++k) R[12 + k] = s.wRvc[4 * ((size_t)b * d.npan + p) + k];
     R[16] = s.wGam[(size_t)b * d.npan + p];
     R[17] = 0.0;
+    if (s.edgeW)
+      for (int k = 0; k < 4; ++k) s.edgeW[4 * (size_t)t + k] = R[16];  // wing rings: no eps skip
     return;
   }
   const int rowsN = d.NW - (rowNear - 1);
@@ -528,6 +565,7 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
     for (int k = 0; k < 4; ++k) R[12 + k] = s.nRvc[4 * r + k];
     R[16] = s.nGam[r];
     R[17] = (double)REC_SKIP;
+    if (s.edgeW) lattice_weights(d, s, nc, b, i, j, rowNear, s.edgeW + 4 * (size_t)t);
   } else if (l < nNear + hs) {
     const size_t r = ringI(d, b, d.NW - 1, l - nNear);
     for (int k = 0; k < 6; ++k) R[k] = nc[12 * r + 3 + k];
@@ -536,6 +574,11 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
     R[13] = R[14] = R[15] = 0.0;
     R[16] = -s.nGam[r];
     R[17] = (double)REC_FIL;
+    if (s.edgeW) {
+      double* W = s.edgeW + 4 * (size_t)t;
+      W[0] = R[16];
+      W[1] = W[2] = W[3] = 0.0;
+    }
   } else {
     const size_t f = (size_t)b * d.NF + rowFar - 1 + (l - nNear - hs);
     const double* fc = pred ? s.fCP : s.fC;
@@ -545,6 +588,11 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
     R[13] = R[14] = R[15] = 0.0;
     R[16] = s.fGam[f];
     R[17] = (double)(REC_FIL | REC_SKIP);
+    if (s.edgeW) {
+      double* W = s.edgeW + 4 * (size_t)t;
+      W[0] = fabs(R[16]) > kEps ? R[16] : 0.0;
+      W[1] = W[2] = W[3] = 0.0;
+    }
   }
 }
 

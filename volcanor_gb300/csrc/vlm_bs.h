@@ -31,9 +31,12 @@ constexpr int REC_SKIP = 2;
 
 // FP32 source record, 48 floats (192 B, 16-byte aligned for bulk copies):
 //   [0..11]  corners c0..c3
-//   [12..23] weighted edge vectors w_k e_k, e_k = c_{k+1} - c_k, w_k = gam/(4 pi)
+//   [12..23] weighted edge vectors w_k e_k, e_k = c_{k+1} - c_k, w_k = gam_k/(4 pi)
+//            (gam_k = gam, or the edge's own circulation in lattice form)
 //   [24..27] w_k |e_k|^2
-//   [28..31] (rvc_k |e_k|)^4, floored at 1e-36 so the kernel needs no clamp
+//   [28..31] (rvc_k |e_k|)^4, floored at 1e-36 so the kernel needs no clamp;
+//            [30], [31] are -1 when edge 2 / edge 3 carries no circulation
+//            (the kernel then skips it and, if both, corner c3's vector)
 //   [32..35] near-field threshold on |r1 x r2|^2: (near_factor rvc_k |e_k|)^2, -1 if off
 //   [36..39] lower near-field bound on (w_k e_k).r1
 //   [40..43] upper near-field bound on (w_k e_k).r1
@@ -45,6 +48,17 @@ constexpr int REC_SKIP = 2;
 // s = near_factor rvc_k |e_k|; the second test is stored multiplied by w_k,
 // so [36+k] < (w_k e_k).r1 < [40+k] (bounds swapped when w_k < 0).
 constexpr int kRec32 = 48;
+
+// Lattice form (FP32 paths): a near-wake lattice has every interior
+// filament twice, once in each of the two rings that share it, in opposite
+// directions.  With an edge-weight array ew (4 doubles per record), ring
+// (i, j) carries edge 0 (c0 -> c1, shared with ring (i, j-1)) and edge 1
+// (c1 -> c2, shared with ring (i+1, j)) with the circulation difference of
+// the two rings, and edges 2 and 3 only where no neighbour absorbs them
+// (the lattice's border, or a neighbour whose shared corners or core radius
+// differ).  The sum over the lattice is unchanged; an interior ring costs two
+// filament evaluations and three corner vectors instead of four and four.
+// Records outside lattices get ew = gam on their active filaments.
 
 // One near-field filament-target pair found by the FP32 kernel: target m,
 // chunk q (partial sum to correct), global record index, filament k.
@@ -104,10 +118,15 @@ void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const
 // a third.  ctl[0] receives a nonzero code if a bounded wait on the tile
 // pipeline expired (1, 2), the near list overflowed (3) or a near-field
 // velocity left the fixed-point range (4).  ctl must be zeroed before the call.
+// ew: the records' edge weights in lattice form (FP64 near field multiplies
+// by ew[4 rec + k] instead of the record's circulation), or null.
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
-                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s);
-// Converts FP64 records to FP32 records (near_factor <= 0 disables near-field).
-void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s);
+                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s,
+                      const double* ew = nullptr);
+// Converts FP64 records to FP32 records (near_factor <= 0 disables near-field);
+// ew as above (null: every active filament of a record carries its gam).
+void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s,
+                   const double* ew = nullptr);
 
 // Combines partials: total = sum over wing groups + sum over wake groups,
 // each group the in-order sum of its chunk partials, each from zero.

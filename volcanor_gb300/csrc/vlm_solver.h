@@ -81,6 +81,9 @@ struct DevState {
   // N-body scratch
   double *rec64, *targets, *part, *outv;
   float* rec32;
+  // lattice-form edge weights of the gathered records ([rec][4]; null: the
+  // records are evaluated ring by ring), written by the gather
+  double* edgeW;
   NearPair* near;
   long long* nacc;  // fixed-point near-field accumulators, zero between evaluations
   int nearCap;

@@ -36,7 +36,7 @@ class VlmError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("sum_chunk", ctypes.c_int), ("near_factor", ctypes.c_double),
                 ("device", ctypes.c_int), ("use_graph", ctypes.c_int), ("solve_mode", ctypes.c_int),
-                ("nbody_slots", ctypes.c_int)]
+                ("nbody_slots", ctypes.c_int), ("lattice", ctypes.c_int)]
 
 
 class SurrogateOptions(ctypes.Structure):
@@ -230,12 +230,14 @@ class Case:
     def __init__(self, config_text: str, geom_text: str, base_dir: str | os.PathLike = "",
                  precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
                  solve_mode: Optional[int] = None, use_graph: bool = True, nbody_slots: int = 0,
-                 device: int = 0):
+                 device: int = 0, lattice: Optional[bool] = None):
         L = load()
         self._h = _vp()
         self.opt = options(precision, sum_chunk, near_factor, device=device, use_graph=use_graph,
                            solve_mode=solve_mode)
         self.opt.nbody_slots = nbody_slots
+        if lattice is not None:
+            self.opt.lattice = 1 if lattice else 0
         _err(L.vlm_case_create(config_text.encode(), geom_text.encode(), str(base_dir).encode(),
                                ctypes.byref(self.opt), ctypes.byref(self._h)))
 
@@ -418,12 +420,14 @@ class Batch:
     steady state); cases = [(config_text, geom_text, base_dir), ...]."""
 
     def __init__(self, cases, precision: int = PREC_FP64, sum_chunk: Optional[int] = None,
-                 nbody_slots: int = 0, use_graph: bool = True):
+                 nbody_slots: int = 0, use_graph: bool = True, lattice: Optional[bool] = None):
         n = len(cases)
         enc = lambda i: (ctypes.c_char_p * n)(*[str(c[i]).encode() for c in cases])
         self._cfg, self._geo, self._dir = enc(0), enc(1), enc(2)
         self.opt = options(precision, sum_chunk, use_graph=use_graph)
         self.opt.nbody_slots = nbody_slots
+        if lattice is not None:
+            self.opt.lattice = 1 if lattice else 0
         self.n = n
         self._h = _vp()
         _err(load().vlm_batch_create(n, self._cfg, self._geo, self._dir, ctypes.byref(self.opt), ctypes.byref(self._h)))
