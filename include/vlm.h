@@ -161,7 +161,9 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section
  *   forceDist (blade <= nbConvect)  (16, ns): the columns of rXXbYYForceDistNNNNN.csv
  *                                   (src/libPostprocess.f90:850-878) for the current iteration
- *   forceDim                        (11): the rXXForceDim.csv values (src/libPostprocess.f90:840-846) */
+ *   forceDim                        (11): the rXXForceDim.csv values (src/libPostprocess.f90:840-846)
+ *   profileWork                     (2): flops and filament-target evaluations the FP32 kernel
+ *                                   executed per launch in the last vlm_case_profile_eval */
 int64_t vlm_case_get(vlm_case* c, const char* name, int blade, double* out, int64_t cap);
 /* The rXXParams.json text the reference writes at start-up (params2file,
  * src/libPostprocess.f90:52-141): the case's parameters after rotor_init in

@@ -294,6 +294,49 @@ __device__ __forceinline__ unsigned rec_lat(const float4* __restrict__ R4, const
   return msk;
 }
 
+// Both targets of a thread, one lattice-form record, no near test: both
+// targets' c0..c2 vectors first (more independent work in flight), edges 0
+// and 1, then c3 and the border edges 2 / 3 where they carry circulation
+// (uniform branches: every lane evaluates the same record).
+template <int T>
+__device__ __forceinline__ void rec_lat_pair(const float4* __restrict__ R4, const float (&cx)[4], const float (&cy)[4],
+                                             const float (&cz)[4], const float (&px)[T], const float (&py)[T],
+                                             const float (&pz)[T], float (&ax)[T], float (&ay)[T], float (&az)[T]) {
+  RecView v;
+  load_view(R4, v);
+  float rx[T][4], ry[T][4], rz[T][4], inv[T][4];
+#pragma unroll
+  for (int u = 0; u < T; ++u)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      corner_vector(px[u], py[u], pz[u], cx[k], cy[k], cz[k], rx[u][k], ry[u][k], rz[u][k], inv[u][k]);
+#pragma unroll
+  for (int u = 0; u < T; ++u) {
+    fil_fp32<0, false>(R4, v, rx[u][0], ry[u][0], rz[u][0], inv[u][0], rx[u][1], ry[u][1], rz[u][1], inv[u][1], ax[u],
+                       ay[u], az[u], false);
+    fil_fp32<1, false>(R4, v, rx[u][1], ry[u][1], rz[u][1], inv[u][1], rx[u][2], ry[u][2], rz[u][2], inv[u][2], ax[u],
+                       ay[u], az[u], false);
+  }
+  const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
+  if (t2 || t3) {
+#pragma unroll
+    for (int u = 0; u < T; ++u)
+      corner_vector(px[u], py[u], pz[u], cx[3], cy[3], cz[3], rx[u][3], ry[u][3], rz[u][3], inv[u][3]);
+    if (t2) {
+#pragma unroll
+      for (int u = 0; u < T; ++u)
+        fil_fp32<2, false>(R4, v, rx[u][2], ry[u][2], rz[u][2], inv[u][2], rx[u][3], ry[u][3], rz[u][3], inv[u][3],
+                           ax[u], ay[u], az[u], false);
+    }
+    if (t3) {
+#pragma unroll
+      for (int u = 0; u < T; ++u)
+        fil_fp32<3, false>(R4, v, rx[u][3], ry[u][3], rz[u][3], inv[u][3], rx[u][0], ry[u][0], rz[u][0], inv[u][0],
+                           ax[u], ay[u], az[u], false);
+    }
+  }
+}
+
 // One block = 8 consumer warps (256 threads x 2 targets) + 1 producer warp.
 // The producer's lane 0 streams the chunk's records through kStages shared
 // stages with bulk copies; consumers wait on a stage's FULL barrier, compute,
@@ -403,33 +446,35 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
           if (__any_sync(kFull, cand)) {
             // some lane of the warp is within reach of this record
             const int rec = ch.rec_begin + t * kTileW + r;
+            if (LAT) {
+              RecView v;
+              load_view(R4, v);
+              unsigned msk[kTPT];
 #pragma unroll
-            for (int u = 0; u < kTPT; ++u) {
-              unsigned msk;
-              if (LAT) {
-                RecView v;
-                load_view(R4, v);
-                msk = rec_lat<true>(R4, v, cx, cy, cz, px[u], py[u], pz[u], ax[u], ay[u], az[u], candu[u]);
-              } else {
+              for (int u = 0; u < kTPT; ++u)
+                msk[u] = rec_lat<true>(R4, v, cx, cy, cz, px[u], py[u], pz[u], ax[u], ay[u], az[u], candu[u]);
+#pragma unroll
+              for (int u = 0; u < kTPT; ++u) near_append(msk[u], mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
+            } else {
+#pragma unroll
+              for (int u = 0; u < kTPT; ++u) {
                 float rx[4], ry[4], rz[4], inv[4];
                 corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-                msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u], candu[u]);
+                const unsigned msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u], candu[u]);
+                near_append(msk, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
               }
-              near_append(msk, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
             }
+            continue;
+          }
+          if (LAT) {
+            rec_lat_pair<kTPT>(R4, cx, cy, cz, px, py, pz, ax, ay, az);
             continue;
           }
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) {
-            if (LAT) {
-              RecView v;
-              load_view(R4, v);
-              rec_lat<false>(R4, v, cx, cy, cz, px[u], py[u], pz[u], ax[u], ay[u], az[u]);
-            } else {
-              float rx[4], ry[4], rz[4], inv[4];
-              corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-              ring_fp32<false>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
-            }
+            float rx[4], ry[4], rz[4], inv[4];
+            corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
+            ring_fp32<false>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
           }
         } else if (!LAT) {
           // both targets' corner vectors first: more independent work in flight
@@ -439,42 +484,7 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) ring_fp32<false>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
         } else {
-          // lattice form: both targets' c0..c2 vectors, edges 0 and 1, then
-          // the border edges 2 / 3 where they carry circulation (uniform
-          // branches: every lane evaluates the same record)
-          RecView v;
-          load_view(R4, v);
-          float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
-#pragma unroll
-          for (int u = 0; u < kTPT; ++u)
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-              corner_vector(px[u], py[u], pz[u], cx[k], cy[k], cz[k], rx[u][k], ry[u][k], rz[u][k], inv[u][k]);
-#pragma unroll
-          for (int u = 0; u < kTPT; ++u) {
-            fil_fp32<0, false>(R4, v, rx[u][0], ry[u][0], rz[u][0], inv[u][0], rx[u][1], ry[u][1], rz[u][1], inv[u][1],
-                               ax[u], ay[u], az[u], false);
-            fil_fp32<1, false>(R4, v, rx[u][1], ry[u][1], rz[u][1], inv[u][1], rx[u][2], ry[u][2], rz[u][2], inv[u][2],
-                               ax[u], ay[u], az[u], false);
-          }
-          const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
-          if (t2 || t3) {
-#pragma unroll
-            for (int u = 0; u < kTPT; ++u)
-              corner_vector(px[u], py[u], pz[u], cx[3], cy[3], cz[3], rx[u][3], ry[u][3], rz[u][3], inv[u][3]);
-            if (t2) {
-#pragma unroll
-              for (int u = 0; u < kTPT; ++u)
-                fil_fp32<2, false>(R4, v, rx[u][2], ry[u][2], rz[u][2], inv[u][2], rx[u][3], ry[u][3], rz[u][3],
-                                   inv[u][3], ax[u], ay[u], az[u], false);
-            }
-            if (t3) {
-#pragma unroll
-              for (int u = 0; u < kTPT; ++u)
-                fil_fp32<3, false>(R4, v, rx[u][3], ry[u][3], rz[u][3], inv[u][3], rx[u][0], ry[u][0], rz[u][0],
-                                   inv[u][0], ax[u], ay[u], az[u], false);
-            }
-          }
+          rec_lat_pair<kTPT>(R4, cx, cy, cz, px, py, pz, ax, ay, az);
         }
       }
 #pragma unroll

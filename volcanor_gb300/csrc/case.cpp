@@ -1008,6 +1008,7 @@ struct Case {
   // Times the partial-sum kernel of the next step's wake-node evaluation on
   // the current state (reps launches between CUDA events); reports the mean
   // launch time and the ring / single-filament pair counts of one launch.
+  double profileWork[2] = {0.0, 0.0};  // executed flops, filament-target evaluations of the last profileEval
   void profileEval(int reps, double* msPerLaunch, double* ringPairs, double* filPairs) {
     useDevice();
     if (!started || d.NW == 0 || iter >= W.nt) throw StatusError(VLM_ERR_STATE, "needs a started case with steps left");
@@ -1022,6 +1023,25 @@ struct Case {
     const Chunk* ch = dChunks + pl.node.coff;
     const double nf = opt.precision == VLM_PREC_FP32_NEAR64 ? opt.near_factor : 0.0;
     if (opt.precision != VLM_PREC_FP64) launch_pack32(s.rec64, pl.node.nrec, nf, s.rec32, stream, s.edgeW);
+    // the work the FP32 kernel executes per target (9 flop per corner vector,
+    // 35 per filament): a whole ring 4 + 4; a lattice-form record 3 corners
+    // and edges 0, 1, plus corner c3 and edges 2 / 3 where they carry
+    // circulation
+    profileWork[0] = profileWork[1] = 0.0;
+    if (opt.precision != VLM_PREC_FP64) {
+      double corners = 4.0 * pl.node.nrec, fils = 4.0 * pl.node.nrec;
+      if (s.edgeW) {
+        const auto ew = dget(s.edgeW, (size_t)pl.node.nrec * 4);
+        corners = fils = 0.0;
+        for (int r = 0; r < pl.node.nrec; ++r) {
+          const bool t2 = ew[4 * r + 2] != 0.0, t3 = ew[4 * r + 3] != 0.0;
+          corners += (t2 || t3) ? 4.0 : 3.0;
+          fils += 2.0 + (t2 ? 1.0 : 0.0) + (t3 ? 1.0 : 0.0);
+        }
+      }
+      profileWork[0] = (9.0 * corners + 35.0 * fils) * M;
+      profileWork[1] = fils * M;
+    }
     auto launch = [&]() {
       if (opt.precision == VLM_PREC_FP64) launch_partial64(s.rec64, ch, pl.node.nchunks, s.targets, M, s.part, stream);
       else {
@@ -1141,6 +1161,7 @@ struct Case {
     else if (bok && k == "secLift") v = dget(s.secLift + 3 * b * ns, 3 * ns);
     else if (bok && b < d.nbC && k == "forceDist") v = forceDist(b);
     else if (k == "forceDim") v = forceDim();
+    else if (k == "profileWork") v = {profileWork[0], profileWork[1]};
     else if (bok && (k == "CP" || k == "nCap" || k == "vr")) {
       auto f = dget(frame(iter), d.fl.size);
       for (size_t p = 0; p < npan; ++p) {
