@@ -101,6 +101,15 @@ int64_t vlm_biot_savart_rings_scratch_bytes(int64_t N, int64_t M, int precision)
  * are summed in consecutive blocks of this many, each block from zero, the
  * block sums then added in order (N = one block = the reference's order). */
 int64_t vlm_biot_savart_rings_sum_chunk(int64_t N, int64_t M, int precision);
+/* V[m] = sum_n vf_vind(filament n, P[m]) * gam[n] over N single filaments
+ * (src/classdef.f90:476-503; the trailing-edge and far-wake filaments of
+ * gridgen, src/gridgen.f90:128-136).  fc: N x 2 x 3 (fc(:,1), fc(:,2));
+ * rvc, gam: N.  No |gam| skip.  Same summation blocks, scratch and
+ * precisions as the ring kernel. */
+int vlm_biot_savart_filaments(const double* fc, const double* rvc, const double* gam, int64_t N,
+                              const double* P, int64_t M, double* V, int precision);
+int vlm_biot_savart_filaments_device(const double* fc, const double* rvc, const double* gam, int64_t N,
+                                     const double* P, int64_t M, double* V, int precision, void* stream);
 
 /* Allocation-free form of the device-buffer ring kernel.  It has no
  * counterpart in the reference.  It is for callers that cannot allocate
@@ -157,6 +166,10 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *   waN_gam, waN_rvc (blade)        (nNwake, ns), (4, nNwake, ns)
  *   waF (blade)                     (3, 2, nFwake) far-wake filament nodes
  *   waF_gam, waF_rvc (blade)        (nFwake)
+ *   waF_rvc0, waF_l0, waF_lc, waF_age (blade)  (nFwake) initial core, original and current
+ *                                   length, age of the far-wake filaments
+ *   waN_age (blade)                 (nNwake, ns) near-wake ring ages
+ *   vr_rvc (blade)                  (4, nc, ns) wing ring filament core radii
  *   velN, velF (blade)              (3, nNwake, ns+1), (3, nFwake) node velocities
  *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section
  *   forceDist (blade <= nbConvect)  (16, ns): the columns of rXXbYYForceDistNNNNN.csv

@@ -65,6 +65,7 @@ def lib():
         L.or_get.restype = i64
         L.or_sim_vind_points.argtypes = [vp, dp, i64, dp, i32]
         L.or_vind_rings.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
+        L.or_vind_filaments.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
         L.or_vf_vind.argtypes = [dp, dp, ctypes.c_double, dp, dp]
         L.or_inv2.argtypes = [dp, i32, dp]
         L.or_matvec.argtypes = [dp, dp, i32, dp]
@@ -182,6 +183,17 @@ def vind_rings(corners, rvc, gam, P, chunk: int = 0) -> np.ndarray:
     P = _f64(P).reshape(-1, 3)
     V = np.zeros_like(P)
     _check(lib().or_vind_rings(_ptr(corners), _ptr(rvc), _ptr(gam), corners.shape[0], _ptr(P), P.shape[0], _ptr(V), int(chunk)))
+    return V
+
+
+def vind_filaments(fc, rvc, gam, P, chunk: int = 0) -> np.ndarray:
+    """V[m] = sum_n vf_vind(filament n, P[m]) * gam[n] (in order; chunked when chunk > 0)."""
+    fc = _f64(fc).reshape(-1, 2, 3)
+    rvc = _f64(rvc).reshape(-1)
+    gam = _f64(gam).reshape(-1)
+    P = _f64(P).reshape(-1, 3)
+    V = np.zeros_like(P)
+    _check(lib().or_vind_filaments(_ptr(fc), _ptr(rvc), _ptr(gam), fc.shape[0], _ptr(P), P.shape[0], _ptr(V), int(chunk)))
     return V
 
 

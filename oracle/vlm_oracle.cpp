@@ -2210,6 +2210,29 @@ int or_vind_rings(const double* corners, const double* rvc, const double* gam, l
   });
 }
 
+// Isolated filaments: V[m] = sum_n vf_vind(filament n, P[m]) * gam[n] in
+// order (chunked when chunk > 0), no |gam| skip (src/gridgen.f90:128-136).
+// fc: N x 2 x 3, rvc and gam: N.
+int or_vind_filaments(const double* fc, const double* rvc, const double* gam, long N, const double* P, long M,
+                      double* V, int chunk) {
+  return guarded([&]() {
+    std::vector<VF> f(N);
+    for (long n = 0; n < N; ++n) {
+      f[n].fc1 = mk(fc[6 * n], fc[6 * n + 1], fc[6 * n + 2]);
+      f[n].fc2 = mk(fc[6 * n + 3], fc[6 * n + 4], fc[6 * n + 5]);
+      f[n].rVc = rvc[n];
+    }
+#pragma omp parallel for schedule(static)
+    for (long m = 0; m < M; ++m) {
+      V3 p = mk(P[3 * m], P[3 * m + 1], P[3 * m + 2]);
+      ChunkSum s(chunk);
+      for (long n = 0; n < N; ++n) s.add(vf_vind(f[n], p) * gam[n]);
+      V3 r = V3() + s.result();
+      V[3 * m] = r.x; V[3 * m + 1] = r.y; V[3 * m + 2] = r.z;
+    }
+  });
+}
+
 // Single filament (vf_vind) for kernel unit checks.
 void or_vf_vind(const double* fc1, const double* fc2, double rvc, const double* P, double* V) {
   VF f;

@@ -149,6 +149,22 @@ __global__ void k_rings_to_rec64(const double* __restrict__ corners, const doubl
   R[17] = 0.0;
 }
 
+// Single filaments fc1 -> fc2 (vf_vind, src/classdef.f90:476-503) as
+// REC_FIL records; no |gam| skip (gridgen sums every filament,
+// src/gridgen.f90:128-136).
+__global__ void k_fils_to_rec64(const double* __restrict__ fc, const double* __restrict__ rvc,
+                                const double* __restrict__ gam, int64_t N, double* __restrict__ rec) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double* R = rec + n * kRec64;
+  for (int k = 0; k < 6; ++k) R[k] = fc[n * 6 + k];
+  for (int k = 6; k < 12; ++k) R[k] = 0.0;
+  R[12] = rvc[n];
+  R[13] = R[14] = R[15] = 0.0;
+  R[16] = gam[n];
+  R[17] = (double)REC_FIL;
+}
+
 }  // namespace
 
 static std::atomic<long> g_launches{0};
@@ -199,6 +215,13 @@ void launch_combine_unordered(const double* part, int M, const Group* groups, in
   const size_t threads = (size_t)M * G;
   count_launch();
   k_combine_tree<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(part, M, groups, ngroups, mode, G, out);
+}
+
+void launch_fils_to_rec64(const double* fc, const double* rvc, const double* gam, int64_t N, double* rec,
+                          cudaStream_t s) {
+  if (N <= 0) return;
+  count_launch();
+  k_fils_to_rec64<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(fc, rvc, gam, N, rec);
 }
 
 void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,

@@ -1153,6 +1153,12 @@ struct Case {
     else if (bok && k == "waF") v = dget(s.fC + 6 * b * NF, 6 * NF);
     else if (bok && k == "waF_gam") v = dget(s.fGam + b * NF, NF);
     else if (bok && k == "waF_rvc") v = dget(s.fRvc + b * NF, NF);
+    else if (bok && k == "waF_rvc0") v = dget(s.fRvc0 + b * NF, NF);
+    else if (bok && k == "waF_l0") v = dget(s.fL0 + b * NF, NF);
+    else if (bok && k == "waF_lc") v = dget(s.fLc + b * NF, NF);
+    else if (bok && k == "waF_age") v = dget(s.fAge + b * NF, NF);
+    else if (bok && k == "waN_age") v = dget(s.nAge + b * NW * ns, NW * ns);
+    else if (bok && k == "vr_rvc") v = dget(s.wRvc + 4 * b * npan, 4 * npan);
     else if (bok && k == "velN") v = dget(s.vN[0] + 3 * b * NW * (ns + 1), 3 * NW * (ns + 1));
     else if (bok && k == "velF") v = dget(s.vF[0] + 3 * b * NF, 3 * NF);
     else if (bok && k == "secCL") v = dget(s.secCL + b * ns, ns);
@@ -1333,8 +1339,10 @@ int64_t ring_sum_chunk(int64_t N, int64_t M, int precision) {
   return c;
 }
 
+// fil: the sources are single filaments (corners = N x [fc1, fc2], rvc and
+// gam one per filament) instead of rings.
 void rings_device(const double* corners, const double* rvc, const double* gam, int64_t N, const double* P, int64_t M,
-                  double* V, int precision, cudaStream_t st) {
+                  double* V, int precision, cudaStream_t st, bool fil = false) {
   if (precision < 0 || precision > 2) throw StatusError(VLM_ERR_INVALID, "precision must be 0, 1 or 2");
   if (N < 0 || M < 0 || N > (1LL << 30) || M > (1LL << 30)) throw StatusError(VLM_ERR_INVALID, "N and M must be in [0, 2^30]");
   if (M == 0) return;
@@ -1364,7 +1372,8 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   VLM_CUDA(cudaMemcpyAsync(R.group, &g, sizeof(Group), cudaMemcpyHostToDevice, st));
   VLM_CUDA(cudaMemsetAsync(R.err, 0, 4 * sizeof(int), st));
   if (N > 0) {
-    launch_rings_to_rec64(corners, rvc, gam, N, R.rec64, st);
+    if (fil) launch_fils_to_rec64(corners, rvc, gam, N, R.rec64, st);
+    else launch_rings_to_rec64(corners, rvc, gam, N, R.rec64, st);
     if (precision == VLM_PREC_FP64) {
       launch_partial64(R.rec64, R.chunks, nq, P, (int)M, R.part, st);
     } else {
@@ -1467,26 +1476,31 @@ int64_t vlm_biot_savart_rings_sum_chunk(int64_t N, int64_t M, int precision) {
   return ring_sum_chunk(N, M, precision);
 }
 
-int vlm_biot_savart_rings(const double* corners, const double* rvc, const double* gam, int64_t N, const double* P,
-                          int64_t M, double* V, int precision) {
+// Host-buffer form of rings_device: nc / nr doubles per source of corners /
+// core radii (rings 12 / 4, filaments 6 / 1).
+static int sources_host(const double* corners, const double* rvc, const double* gam, int64_t N, const double* P,
+                        int64_t M, double* V, int precision, bool fil) {
+  const size_t nc = fil ? 6 : 12, nr = fil ? 1 : 4;
   return guard([&]() {
+    if (N < 0 || M < 0) throw StatusError(VLM_ERR_INVALID, "N and M must be non-negative");
+    if ((N > 0 && (!corners || !rvc || !gam)) || (M > 0 && (!P || !V))) throw StatusError(VLM_ERR_INVALID, "null array");
     std::vector<void*> own;
     auto cleanup = [&]() {
       for (void* p : own) cudaFree(p);
     };
     try {
-      double* dc = dalloc<double>((size_t)std::max<int64_t>(N, 1) * 12, own);
-      double* dr = dalloc<double>((size_t)std::max<int64_t>(N, 1) * 4, own);
+      double* dc = dalloc<double>((size_t)std::max<int64_t>(N, 1) * nc, own);
+      double* dr = dalloc<double>((size_t)std::max<int64_t>(N, 1) * nr, own);
       double* dg = dalloc<double>((size_t)std::max<int64_t>(N, 1), own);
       double* dp = dalloc<double>((size_t)std::max<int64_t>(M, 1) * 3, own);
       double* dv = dalloc<double>((size_t)std::max<int64_t>(M, 1) * 3, own);
       if (N > 0) {
-        VLM_CUDA(cudaMemcpy(dc, corners, (size_t)N * 12 * 8, cudaMemcpyHostToDevice));
-        VLM_CUDA(cudaMemcpy(dr, rvc, (size_t)N * 4 * 8, cudaMemcpyHostToDevice));
+        VLM_CUDA(cudaMemcpy(dc, corners, (size_t)N * nc * 8, cudaMemcpyHostToDevice));
+        VLM_CUDA(cudaMemcpy(dr, rvc, (size_t)N * nr * 8, cudaMemcpyHostToDevice));
         VLM_CUDA(cudaMemcpy(dg, gam, (size_t)N * 8, cudaMemcpyHostToDevice));
       }
       if (M > 0) VLM_CUDA(cudaMemcpy(dp, P, (size_t)M * 3 * 8, cudaMemcpyHostToDevice));
-      rings_device(dc, dr, dg, N, dp, M, dv, precision, nullptr);
+      rings_device(dc, dr, dg, N, dp, M, dv, precision, nullptr, fil);
       if (M > 0) VLM_CUDA(cudaMemcpy(V, dv, (size_t)M * 3 * 8, cudaMemcpyDeviceToHost));
     } catch (...) {
       cleanup();
@@ -1494,6 +1508,21 @@ int vlm_biot_savart_rings(const double* corners, const double* rvc, const double
     }
     cleanup();
   });
+}
+
+int vlm_biot_savart_rings(const double* corners, const double* rvc, const double* gam, int64_t N, const double* P,
+                          int64_t M, double* V, int precision) {
+  return sources_host(corners, rvc, gam, N, P, M, V, precision, false);
+}
+
+int vlm_biot_savart_filaments(const double* fc, const double* rvc, const double* gam, int64_t N, const double* P,
+                              int64_t M, double* V, int precision) {
+  return sources_host(fc, rvc, gam, N, P, M, V, precision, true);
+}
+
+int vlm_biot_savart_filaments_device(const double* fc, const double* rvc, const double* gam, int64_t N,
+                                     const double* P, int64_t M, double* V, int precision, void* stream) {
+  return guard([&]() { rings_device(fc, rvc, gam, N, P, M, V, precision, (cudaStream_t)stream, true); });
 }
 
 // ---------------------------------------------------------------------------

@@ -151,5 +151,9 @@ int selftest_bounded_wait(uint32_t limit);
 // Isolated rings (vlm_biot_savart_rings): AoS corners (N x 4 x 3), rvc (N x 4), gam (N) -> FP64 records.
 void launch_rings_to_rec64(const double* corners, const double* rvc, const double* gam, int64_t N, double* rec,
                            cudaStream_t s);
+// Single filaments (fc: N x [fc1 xyz, fc2 xyz], one core radius and one
+// circulation each) to FP64 records.
+void launch_fils_to_rec64(const double* fc, const double* rvc, const double* gam, int64_t N, double* rec,
+                          cudaStream_t s);
 
 }  // namespace vlm

@@ -70,6 +70,8 @@ SIGNATURES = {
     "vlm_biot_savart_rings_scratch_bytes": (_i64, [_i64, _i64, ctypes.c_int]),
     "vlm_biot_savart_rings_sum_chunk": (_i64, [_i64, _i64, ctypes.c_int]),
     "vlm_biot_savart_rings_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_int, _vp]),
+    "vlm_biot_savart_filaments": (ctypes.c_int, [_dp, _dp, _dp, _i64, _dp, _i64, _dp, ctypes.c_int]),
+    "vlm_biot_savart_filaments_device": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_int, _vp]),
     "vlm_case_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(Options),
                                        ctypes.POINTER(_vp)]),
     "vlm_case_create_from_dir": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
@@ -198,6 +200,19 @@ def biot_savart_rings(corners, rvc, gam, P, precision: int = PREC_FP64) -> np.nd
     V = np.zeros_like(P)
     _err(load().vlm_biot_savart_rings(_ptr(corners), _ptr(rvc), _ptr(gam), corners.shape[0], _ptr(P), P.shape[0],
                                       _ptr(V), precision))
+    return V
+
+
+def biot_savart_filaments(fc, rvc, gam, P, precision: int = PREC_FP64) -> np.ndarray:
+    """Single-filament Biot-Savart sum (vf_vind x gam) through the host-buffer
+    C entry point; fc is N x 2 x 3 (start, end)."""
+    fc = _c64(fc).reshape(-1, 2, 3)
+    rvc = _c64(rvc).reshape(-1)
+    gam = _c64(gam).reshape(-1)
+    P = _c64(P).reshape(-1, 3)
+    V = np.zeros_like(P)
+    _err(load().vlm_biot_savart_filaments(_ptr(fc), _ptr(rvc), _ptr(gam), fc.shape[0], _ptr(P), P.shape[0],
+                                          _ptr(V), precision))
     return V
 
 
