@@ -15,7 +15,11 @@ ageAzimuthal; vr_class = vf(4), gam, skew (src/classdef.f90:57-104).
 :func:`filaments_from_case` takes them from a running case (the engine
 keeps fc, rVc and gam of every element, and l0, lc, rVc0 and age of the far
 wake; the fields it does not keep are written as zero -- gridgen reads only
-fc, rVc and gam).
+fc, rVc and gam).  It reads the state between two steps: after step k's
+wake convection.  The reference writes its file of iteration k inside step
+k, after the loads and before that convection (src/main.f90:785-790), so a
+file written here after step k holds the wake of the reference's file k
+convected by one step (same elements and circulations, moved nodes).
 
 ``gridgen`` (src/gridgen.f90) reads ``gridconfig.nml`` and the filament
 files of a run and writes ``Results/gridNNNNN.tec``: the induced velocity
