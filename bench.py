@@ -523,7 +523,7 @@ def run_batch(args):
     out = {"metric": "batched free-wake case-timesteps/s", "value": round(value, 2), "unit": "case-timesteps/s",
            "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
-           "data": "synthetic (256 seeded uneven rotor cases, volcanor_gb300/cases.py batch_sweep)",
+           "data": f"synthetic ({n} seeded uneven rotor cases, volcanor_gb300/cases.py batch_sweep)",
            "config": {"workload": f"{n} independent rotor cases: 2-4 blades, 24-400 rings, collective 2-12 deg, "
                                   "advance ratio 0-0.3, wakes of 1-8 revolutions (5k-120k filaments), steady state, "
                                   "one CUDA-graph launch per batch step", "precision": args.precision},
