@@ -187,6 +187,17 @@ int64_t vlm_case_params_json(vlm_case* c, char* buf, int64_t cap);
 /* The same text from the case files alone (host only, no device use). */
 int64_t vlm_params_json(const char* config_text, const char* geom_text, const char* base_dir, char* buf,
                         int64_t cap);
+/* Prescribed wing kinematics from the case files alone (host only, no
+ * device use): the initial pitch and the motion of iterations 1..iter
+ * (src/main.f90:43-58,412-463; blade_rotate / blade_move,
+ * src/classdef.f90:1160-1281) applied to the geometry of rotor_init, then
+ * one array of blade `blade` (1-based) copied into out (at most cap doubles):
+ *   PC    (3, 4, nc, ns) panel corners      vr    (3, 4, nc, ns) vortex-ring corners
+ *   CP    (3, nc, ns) collocation points    nCap  (3, nc, ns) panel normals
+ *   secCP (3, ns) section reference points
+ * Returns the element count, or -1 on error (vlm_last_error says why). */
+int64_t vlm_wing_kinematics(const char* config_text, const char* geom_text, const char* base_dir, int iter,
+                            const char* name, int blade, double* out, int64_t cap);
 /* Induced velocity of the current wing + wake at M points (probes / gridgen:
  * src/libPostprocess.f90:333-361, src/gridgen.f90:115-140). */
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V);

@@ -1838,6 +1838,32 @@ int64_t vlm_params_json(const char* config_text, const char* geom_text, const ch
   return copy_text(t, buf, cap);
 }
 
+int64_t vlm_wing_kinematics(const char* config_text, const char* geom_text, const char* base_dir, int iter,
+                            const char* name, int blade, double* out, int64_t cap) {
+  if (!config_text || !geom_text || !name || iter < 0 || cap < 0 || (cap > 0 && !out)) return -1;
+  std::vector<double> v;
+  const int rc = guard([&]() {
+    vlm::Wing w;
+    w.load(config_text, geom_text, base_dir ? base_dir : "");
+    if (blade < 1 || blade > (int)w.bl.size()) throw StatusError(VLM_ERR_INVALID, "blade out of range");
+    if (iter > w.nt) throw StatusError(VLM_ERR_INVALID, "iteration beyond nt");
+    w.start_pitch();
+    for (int k = 1; k <= iter; ++k) w.advance(k);
+    const vlm::Blade& B = w.bl[blade - 1];
+    const std::string k = name;
+    auto put = [&](vlm::d3 a) { v.push_back(a.x), v.push_back(a.y), v.push_back(a.z); };
+    if (k == "PC") { for (const auto& p : B.p) for (int c = 0; c < 4; ++c) put(p.PC[c]); }
+    else if (k == "vr") { for (const auto& p : B.p) for (int c = 0; c < 4; ++c) put(p.C[c]); }
+    else if (k == "CP") { for (const auto& p : B.p) put(p.CP); }
+    else if (k == "nCap") { for (const auto& p : B.p) put(p.nCap); }
+    else if (k == "secCP") { for (const auto& c : B.secCP) put(c); }
+    else throw StatusError(VLM_ERR_INVALID, "unknown kinematics array " + k);
+  });
+  if (rc != VLM_OK) return -1;
+  if (out && cap > 0) std::memcpy(out, v.data(), sizeof(double) * std::min<int64_t>((int64_t)v.size(), cap));
+  return (int64_t)v.size();
+}
+
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V) {
   if (!c || (M > 0 && (!P || !V))) return VLM_ERR_INVALID;
   return guard([&]() { c->c.vindPoints(P, M, V); });

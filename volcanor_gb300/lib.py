@@ -83,6 +83,8 @@ SIGNATURES = {
     "vlm_case_vind_points": (ctypes.c_int, [_vp, _dp, _i64, _dp]),
     "vlm_case_params_json": (_i64, [_vp, ctypes.c_char_p, _i64]),
     "vlm_params_json": (_i64, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _i64]),
+    "vlm_wing_kinematics": (_i64, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p,
+                                   ctypes.c_int, _dp, _i64]),
     "vlm_case_last_step_ms": (ctypes.c_int, [_vp, _dp]),
     "vlm_case_profile_eval": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
     "vlm_case_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
@@ -189,6 +191,21 @@ def params_json(config_text: str, geom_text: str, base_dir: str | os.PathLike = 
     buf = ctypes.create_string_buffer(int(n) + 1)
     L.vlm_params_json(*args, buf, n + 1)
     return buf.value.decode()
+
+
+def wing_kinematics(config_text: str, geom_text: str, iteration: int, name: str, blade: int = 1,
+                    base_dir: str | os.PathLike = "") -> np.ndarray:
+    """A wing array (PC, vr, CP, nCap, secCP) after the prescribed motion of
+    iterations 1..iteration, from the case files alone (host side, no GPU)."""
+    L = load()
+    args = (config_text.encode(), geom_text.encode(), str(base_dir).encode(), int(iteration), name.encode(),
+            int(blade))
+    n = L.vlm_wing_kinematics(*args, None, 0)
+    if n < 0:
+        raise VlmError(1, last_error())
+    out = np.zeros(max(n, 1))
+    L.vlm_wing_kinematics(*args, _ptr(out), n)
+    return out[:n]
 
 
 def biot_savart_rings(corners, rvc, gam, P, precision: int = PREC_FP64) -> np.ndarray:
