@@ -195,6 +195,7 @@ int64_t vlm_params_json(const char* config_text, const char* geom_text, const ch
  *   PC    (3, 4, nc, ns) panel corners      vr    (3, 4, nc, ns) vortex-ring corners
  *   CP    (3, nc, ns) collocation points    nCap  (3, nc, ns) panel normals
  *   secCP (3, ns) section reference points
+ *   vr_rvc (4, nc, ns) ring filament core radii; secArea, secChord (ns)
  * Returns the element count, or -1 on error (vlm_last_error says why). */
 int64_t vlm_wing_kinematics(const char* config_text, const char* geom_text, const char* base_dir, int iter,
                             const char* name, int blade, double* out, int64_t cap);

@@ -45,6 +45,9 @@ def test_host_kinematics_match_oracle(name, tmp_path):
             for arr in ("PC", "CP", "nCap", "secCP"):
                 np.testing.assert_array_equal(lib.wing_kinematics(cfg, geo, it, arr, b, base), r.get(arr, b),
                                               err_msg=f"{name} iter {it} blade {b} {arr}")
+            for arr in ("vr_rvc", "secArea", "secChord"):
+                np.testing.assert_array_equal(lib.wing_kinematics(cfg, geo, it, arr, b, base), r.get(arr, b),
+                                              err_msg=f"{name} iter {it} blade {b} {arr}")
             ring = lib.wing_kinematics(cfg, geo, it, "vr", b, base).reshape(-1, 4, 3)
             np.testing.assert_array_equal(ring, r.get("vr", b).reshape(-1, 4, 2, 3)[:, :, 0],
                                           err_msg=f"{name} iter {it} blade {b} vr")

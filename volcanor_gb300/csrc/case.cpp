@@ -1857,6 +1857,9 @@ int64_t vlm_wing_kinematics(const char* config_text, const char* geom_text, cons
     else if (k == "CP") { for (const auto& p : B.p) put(p.CP); }
     else if (k == "nCap") { for (const auto& p : B.p) put(p.nCap); }
     else if (k == "secCP") { for (const auto& c : B.secCP) put(c); }
+    else if (k == "vr_rvc") { for (const auto& p : B.p) v.insert(v.end(), p.rvc, p.rvc + 4); }
+    else if (k == "secArea") v = B.secArea;
+    else if (k == "secChord") v = B.secChord;
     else throw StatusError(VLM_ERR_INVALID, "unknown kinematics array " + k);
   });
   if (rc != VLM_OK) return -1;
