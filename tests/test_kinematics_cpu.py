@@ -61,3 +61,22 @@ def test_kinematics_errors():
         lib.wing_kinematics(h.config, h.geom, 1, "CP", 3)   # no blade 3
     with pytest.raises(lib.VlmError):
         lib.wing_kinematics(h.config, h.geom, 1, "nope")
+
+
+@pytest.mark.parametrize("tutorial", ["caradonna", "simplewing", "tr1208"])
+def test_host_kinematics_match_oracle_on_reference_tutorials(golden_dir, tutorial):
+    """The reference's tutorial cases (Caradonna-Tung rotor, simple wing,
+    TR1208 wing from PLOT3D), as shipped: geometry and motion of the first
+    steps bit for bit."""
+    d = golden_dir / f"tutorial-{tutorial}"
+    cfg, geo = (d / "config.nml").read_text(), (d / "geom01.nml").read_text()
+    nb = int(O.Sim(cfg, geo, str(d)).geti("nb"))
+    for it in (0, 1, 4):
+        r = O.Sim(cfg, geo, str(d))
+        r.start()
+        if it:
+            r.step(it)
+        for b in range(1, nb + 1):
+            for arr in ("PC", "CP", "nCap", "secCP", "vr_rvc", "secArea", "secChord"):
+                np.testing.assert_array_equal(lib.wing_kinematics(cfg, geo, it, arr, b, d), r.get(arr, b),
+                                              err_msg=f"{tutorial} iter {it} blade {b} {arr}")
