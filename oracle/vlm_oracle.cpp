@@ -440,6 +440,9 @@ struct Rotor {
   V3 hubCoords, cgCoords, fromCoords, pts;
   double radius = 0, root_cut = 0, chord = 0, preconeAngle = 0, Omega = 0, omegaSlow = 0;
   V3 shaftAxis, velBody, omegaBody, controlPitch;
+  // customTrajectorySwitch = 1: body velocity and rates of every step
+  // (velBodyHistory, omegaBodyHistory; classdef.f90:3065-3081)
+  std::vector<V3> velBodyHistory, omegaBodyHistory;
   double thetaTwist = 0;
   int ductSwitch = 0, axisymmetrySwitch = 0, spanwiseLiftSwitch = 0, symmetricTau = 0;
   int customTrajectorySwitch = 0, forceCalcSwitch = 0, nAirfoils = 0;
@@ -1461,8 +1464,10 @@ struct Sim {
     if (R.nCamberFiles > 0) throw std::runtime_error("camber files are not supported by this oracle");
     if (R.ductSwitch != 0) throw std::runtime_error("ductSwitch is not supported by this oracle");
     if (R.forceCalcSwitch != 0) throw std::runtime_error("only forceCalcSwitch = 0 is supported");
-    if (R.bladeDynamicsSwitch != 0 || R.bodyDynamicsSwitch != 0 || R.customTrajectorySwitch != 0)
-      throw std::runtime_error("blade/body dynamics and custom trajectories are not supported");
+    if (R.bladeDynamicsSwitch != 0 || R.bodyDynamicsSwitch != 0)
+      throw std::runtime_error("blade/body dynamics are not supported");
+    if (R.customTrajectorySwitch != 0 && R.customTrajectorySwitch != 1)
+      throw std::runtime_error("customTrajectorySwitch must be 0 or 1");
   }
   // classdef.f90:3957-4020
   std::vector<V3> readPlot3d(const std::string& path, int& nx, int& ny) {
@@ -1483,6 +1488,32 @@ struct Sim {
     return g;
   }
   // classdef.f90:2769-3891
+  // trajectory01.in (classdef.f90:3065-3081): nt list-directed records of
+  // u v w p q r; a record's values may run over lines, extra values on its
+  // last line are skipped
+  void readTrajectory() {
+    std::string path = "trajectory01.in";
+    if (!baseDir.empty()) path = baseDir + "/" + path;
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    R.velBodyHistory.assign(nt, V3());
+    R.omegaBodyHistory.assign(nt, V3());
+    std::string line;
+    for (int i = 0; i < nt; ++i) {
+      double v[6];
+      int got = 0;
+      while (got < 6) {
+        if (!std::getline(f, line)) throw std::runtime_error(path + ": fewer than nt records");
+        for (char& c : line) if (c == ',' || c == 'd' || c == 'D') c = (c == ',') ? ' ' : 'e';
+        std::istringstream ls(line);
+        double x;
+        while (got < 6 && ls >> x) v[got++] = x;
+      }
+      R.velBodyHistory[i] = mk(v[0], v[1], v[2]);
+      R.omegaBodyHistory[i] = mk(v[3], v[4], v[5]);
+    }
+  }
+
   void init() {
     Rotor& r = R;
     if (dt < 0 || std::signbit(dt)) {
@@ -1505,6 +1536,7 @@ struct Sim {
     if (r.nNwake > 0 && r.nNwake < 2) throw std::runtime_error("Atleast 2 near wake rows mandatory");
     r.xAxisBody = mk(1, 0, 0); r.yAxisBody = mk(0, 1, 0); r.zAxisBody = mk(0, 0, 1);
     r.nNwake = std::min(r.nNwake, nt);
+    if (r.customTrajectorySwitch == 1) readTrajectory();
     r.nFwake = r.wakeTruncateNt == 0 ? nt - r.nNwake : r.wakeTruncateNt - r.nNwake;
     if (r.nNwake == 0) r.nFwake = 0;
     r.nbConvect = r.axisymmetrySwitch == 1 ? 1 : r.nb;
@@ -1754,6 +1786,10 @@ struct Sim {
     R.omegaSlow = sw.slowStart > 0 ? 0.0 : R.Omega;
     t = 0.0;
     iter = 0;
+    if (R.customTrajectorySwitch == 1) {  // main.f90:111-116
+      R.velBody = R.velBodyHistory[0];
+      R.omegaBody = R.omegaBodyHistory[0];
+    }
     for (int i = 0; i <= sw.ntSubInit; ++i) {
       solveCirculation(false);
       if (sw.ntSubInit != 0) {
@@ -1781,6 +1817,10 @@ struct Sim {
     t = t + dt;
     R.rowNear = std::max(R.rowNear - 1, 1);
     if (iter > R.nNwake) R.rowFar = std::max(R.rowFar - 1, 1);
+    if (R.customTrajectorySwitch == 1) {  // main.f90:419-424
+      R.velBody = R.velBodyHistory[iter - 1];
+      R.omegaBody = R.omegaBodyHistory[iter - 1];
+    }
     switch (sw.slowStart) {
       case 0: R.omegaSlow = R.Omega; break;
       case 1: R.omegaSlow = double(std::min(float(sw.slowStartNt), float(iter + 1))) * R.Omega / double(sw.slowStartNt); break;

@@ -215,3 +215,21 @@ def test_lattice_form_matches_ring_form(name, prec, tmp_path):
     assert np.max(np.abs(ct_lat - ct64) / np.abs(ct64)) < 1e-4
     vl, vr = runs["lat"][1], runs["ring"][1]
     assert np.max(np.abs(vl - vr)) <= 1e-4 * np.max(np.abs(vr))
+
+
+def test_custom_trajectory_bitwise(tmp_path):
+    """customTrajectorySwitch = 1 (trajectory01.in: body velocity and rates
+    per step): the motion enters through the host-computed frames only, so
+    the FP64 run stays bit-identical to the oracle."""
+    nt = 12
+    cfg = C.config_text(nt=nt, dt=0.025, density=1.0, fdScheme=3, wakeDissipation=1, kinematicVisc=1.5e-5)
+    geo = C.geom_text(nb=1, nc=3, ns=5, nNwake=6, span=2.0, chord=0.5, theta0=6.0, velBody=(-10.0, 0.0, 0.0),
+                      wakeTruncateNt=10, customTrajectorySwitch=1, cgCoords=(0.1, 0.0, 0.0))
+    rng = np.random.default_rng(7)
+    rows = []
+    for i in range(nt):
+        rows.append(f"{-10.0 + 0.5 * np.sin(0.3 * i):.12e} {0.2 * rng.normal():.12e} {0.3 * np.cos(0.2 * i):.12e} "
+                    f"{0.05 * rng.normal():.12e} {0.1 * np.sin(0.1 * i):.12e} {0.02 * rng.normal():.12e}")
+    (tmp_path / "trajectory01.in").write_text("\n".join(rows) + "\n")
+    g, r = run_both(cfg, geo, nt, base=tmp_path, chunk=16)
+    assert_same_state(g, r)

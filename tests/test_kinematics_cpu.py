@@ -80,3 +80,64 @@ def test_host_kinematics_match_oracle_on_reference_tutorials(golden_dir, tutoria
             for arr in ("PC", "CP", "nCap", "secCP", "vr_rvc", "secArea", "secChord"):
                 np.testing.assert_array_equal(lib.wing_kinematics(cfg, geo, it, arr, b, d), r.get(arr, b),
                                               err_msg=f"{tutorial} iter {it} blade {b} {arr}")
+
+
+def _trajectory_text(nt, seed, split_every=0):
+    """trajectory01.in: nt records of u v w p q r; every split_every-th record
+    runs over two lines and uses Fortran d exponents."""
+    rng = np.random.default_rng(seed)
+    lines = []
+    for i in range(nt):
+        u, v, w = -10.0 + 0.5 * np.sin(0.3 * i), 0.2 * rng.normal(), 0.3 * np.cos(0.2 * i)
+        p, q, r = 0.05 * rng.normal(), 0.1 * np.sin(0.1 * i), 0.02 * rng.normal()
+        if split_every and i % split_every == 0:
+            lines.append(f"{u:.10e}, {v:.10e}, {w:.10e}".replace("e", "d"))
+            lines.append(f"{p:.10e} {q:.10e} {r:.10e} 99.0")
+        else:
+            lines.append(f"{u:.12e} {v:.12e} {w:.12e} {p:.12e} {q:.12e} {r:.12e}")
+    return "\n".join(lines) + "\n"
+
+
+@pytest.mark.parametrize("kind", ["wing", "rotor"])
+def test_custom_trajectory_kinematics_match_oracle(tmp_path, kind):
+    """customTrajectorySwitch = 1: the body velocity and rates of every step
+    come from trajectory01.in (src/classdef.f90:3065-3081, src/main.f90:111-116,419-424)."""
+    nt = 9
+    if kind == "wing":
+        cfg = C.config_text(nt=nt, dt=0.025, density=1.0, fdScheme=3)
+        geo = C.geom_text(nb=1, nc=3, ns=4, nNwake=4, span=2.0, chord=0.5, theta0=5.0, velBody=(-10.0, 0.0, 0.0),
+                          customTrajectorySwitch=1, cgCoords=(0.1, 0.0, 0.0))
+    else:
+        cfg = C.config_text(nt=nt, dt=0.0, density=1.2, fdScheme=3)
+        geo = C.geom_text(nb=2, nc=1, ns=5, nNwake=4, span=1.0, rootcut=0.2, chord=0.08, Omega=100.0,
+                          shaftAxis=(0.0, 0.0, 1.0), theta0=8.0, velBody=(-5.0, 0.0, 0.0), customTrajectorySwitch=1)
+    (tmp_path / "trajectory01.in").write_text(_trajectory_text(nt, 5, split_every=3))
+    base = str(tmp_path)
+    nb = int(O.Sim(cfg, geo, base).geti("nb"))
+    for it in (0, 1, 4, nt):
+        r = O.Sim(cfg, geo, base)
+        r.start()
+        if it:
+            r.step(it)
+        for b in range(1, nb + 1):
+            for arr in ("PC", "CP", "nCap", "secCP"):
+                np.testing.assert_array_equal(lib.wing_kinematics(cfg, geo, it, arr, b, base), r.get(arr, b),
+                                              err_msg=f"{kind} iter {it} blade {b} {arr}")
+    # the motion differs from the namelist's constant velocity
+    steady = lib.wing_kinematics(cfg, geo.replace("customTrajectorySwitch = 1", "customTrajectorySwitch = 0"),
+                                 nt, "CP", 1, base)
+    assert not np.array_equal(steady, lib.wing_kinematics(cfg, geo, nt, "CP", 1, base))
+    # rXXParams.json echoes the namelist velocity (params2file runs before any step)
+    import json
+    assert json.loads(lib.params_json(cfg, geo, base))["u"] == pytest.approx(-10.0 if kind == "wing" else -5.0)
+
+
+def test_custom_trajectory_missing_or_short_file(tmp_path):
+    cfg = C.config_text(nt=5, dt=0.025, density=1.0, fdScheme=3)
+    geo = C.geom_text(nb=1, nc=2, ns=3, nNwake=3, span=2.0, chord=0.5, theta0=5.0, velBody=(-10.0, 0.0, 0.0),
+                      customTrajectorySwitch=1)
+    with pytest.raises(lib.VlmError):
+        lib.wing_kinematics(cfg, geo, 1, "CP", 1, tmp_path)
+    (tmp_path / "trajectory01.in").write_text(_trajectory_text(3, 0))
+    with pytest.raises(lib.VlmError):
+        lib.wing_kinematics(cfg, geo, 1, "CP", 1, tmp_path)

@@ -290,6 +290,7 @@ void Wing::readGeom(const Namelist& g) {
   r.symmetricTau = g.i("GEOMPARAMS", "symmetricTau");
   r.customTrajectorySwitch = g.i("GEOMPARAMS", "customTrajectorySwitch");
   r.velBody = g.v3("GEOMPARAMS", "velBody");
+  r.velBodyInput = r.velBody;
   r.omegaBody = g.v3("GEOMPARAMS", "omegaBody");
   r.forceCalcSwitch = g.i("GEOMPARAMS", "forceCalcSwitch");
   r.apparentViscCoeff = g.d("WAKEPARAMS", "apparentViscCoeff");
@@ -322,9 +323,40 @@ void Wing::readGeom(const Namelist& g) {
   if (r.nCamberFiles > 0) throw std::runtime_error("unsupported: camber files");
   if (r.ductSwitch != 0) throw std::runtime_error("unsupported: ductSwitch");
   if (r.forceCalcSwitch != 0) throw std::runtime_error("unsupported: forceCalcSwitch != 0 (C81 tables)");
-  if (r.bladeDynamicsSwitch != 0 || r.bodyDynamicsSwitch != 0 || r.customTrajectorySwitch != 0)
-    throw std::runtime_error("unsupported: blade/body dynamics or custom trajectories");
+  if (r.bladeDynamicsSwitch != 0 || r.bodyDynamicsSwitch != 0)
+    throw std::runtime_error("unsupported: blade/body dynamics");
+  if (r.customTrajectorySwitch != 0 && r.customTrajectorySwitch != 1)
+    throw std::runtime_error("customTrajectorySwitch must be 0 or 1");
   if (r.nc < 1 || r.ns < 1 || r.nb < 1) throw std::runtime_error("nb, nc and ns must be positive");
+}
+
+// trajectory01.in (src/classdef.f90:3065-3081): nt list-directed records of
+// u v w p q r (body velocity and rates); a record's values may run over
+// lines, extra values on its last line are skipped.
+void Wing::readTrajectory() {
+  std::string path = "trajectory01.in";
+  if (!baseDir.empty()) path = baseDir + "/" + path;
+  std::ifstream f(path);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  P.velBodyHistory.assign(nt, zero3());
+  P.omegaBodyHistory.assign(nt, zero3());
+  std::string line;
+  for (int i = 0; i < nt; ++i) {
+    double v[6];
+    int got = 0;
+    while (got < 6) {
+      if (!std::getline(f, line)) throw std::runtime_error(path + ": fewer than nt records");
+      for (char& c : line) {
+        if (c == ',') c = ' ';
+        else if (c == 'd' || c == 'D') c = 'e';
+      }
+      std::istringstream ls(line);
+      double x;
+      while (got < 6 && ls >> x) v[got++] = x;
+    }
+    P.velBodyHistory[i] = mk3(v[0], v[1], v[2]);
+    P.omegaBodyHistory[i] = mk3(v[3], v[4], v[5]);
+  }
 }
 
 // src/classdef.f90:5133-5148
@@ -465,6 +497,7 @@ void Wing::init() {
   yBody = mk3(0, 1, 0);
   zBody = mk3(0, 0, 1);
   r.nNwake = std::min(r.nNwake, nt);
+  if (r.customTrajectorySwitch == 1) readTrajectory();
   nFwake = r.wakeTruncateNt == 0 ? nt - r.nNwake : r.wakeTruncateNt - r.nNwake;
   if (r.nNwake == 0) nFwake = 0;
   nbConvect = r.axisymmetrySwitch == 1 ? 1 : r.nb;
@@ -675,10 +708,18 @@ void Wing::start_pitch() {
     b.theta = gettheta(P.psiStart, ib + 1);
     blade_rot_pitch(b, fsign1(P.Omega) * b.theta);
   }
+  if (P.customTrajectorySwitch == 1) {  // src/main.f90:111-116, before the initial solve
+    P.velBody = P.velBodyHistory[0];
+    P.omegaBody = P.omegaBodyHistory[0];
+  }
 }
 
 // src/main.f90:412-463
 void Wing::advance(int iter) {
+  if (P.customTrajectorySwitch == 1) {  // src/main.f90:419-424
+    P.velBody = P.velBodyHistory[iter - 1];
+    P.omegaBody = P.omegaBodyHistory[iter - 1];
+  }
   switch (sw.slowStart) {
     case 0: omegaSlow = P.Omega; break;
     case 1: omegaSlow = double(std::min(float(sw.slowStartNt), float(iter + 1))) * P.Omega / double(sw.slowStartNt); break;
@@ -855,9 +896,9 @@ std::string Wing::params_json() const {
   kr("thetaC", r.controlPitch.y * kRad2Deg);
   kr("thetaS", r.controlPitch.z * kRad2Deg);
   kr("thetaTwist", r.thetaTwist * kRad2Deg);
-  kr("u", r.velBody.x);
-  kr("v", r.velBody.y);
-  kr("w", r.velBody.z);
+  kr("u", r.velBodyInput.x);  // params2file runs before any trajectory step
+  kr("v", r.velBodyInput.y);
+  kr("w", r.velBodyInput.z);
   kr("nonDimForceDenom", nonDimDenom);
   kr("alpha0", r.nAirfoils > 0 ? r.alpha0 : 0.0);
   ki("wakeTruncateNt", r.wakeTruncateNt);

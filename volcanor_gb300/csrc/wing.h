@@ -53,6 +53,11 @@ struct RotorParams {  // rotor_readGeom inputs (src/classdef.f90:2541-2767)
   int bladeDynamicsSwitch = 0, pitchDynamicsSwitch = 0, bodyDynamicsSwitch = 0;
   double flapInitial = 0, dflapInitial = 0, dpitch = 0;
   int inflowPlotSwitch = 0, gammaPlotSwitch = 0, skewPlotSwitch = 0;
+  // customTrajectorySwitch = 1: body velocity and rates of every step from
+  // trajectory01.in (velBodyHistory / omegaBodyHistory,
+  // src/classdef.f90:3065-3081); velBodyInput is the namelist value
+  std::vector<d3> velBodyHistory, omegaBodyHistory;
+  d3 velBodyInput{0, 0, 0};
   // read only to be echoed into rXXParams.json
   int imagePlane = 0, imageRotorNum = 0, nAirfoils = 0;
   double thetaTwist = 0, Iflap = 0, cflap = 0, kflap = 0, MflapConstant = 0, alpha0 = 0;
@@ -105,6 +110,7 @@ class Wing {
   void readGeom(const Namelist& g);
   void init();
   void toChordsRevs(int& n) const;
+  void readTrajectory();
   void blade_move(Blade& b, d3 d);
   void blade_rot_pts(Blade& b, d3 pts, d3 o);
   void blade_rotate(Blade& b, double ang, d3 axis, d3 o, int type);
