@@ -193,6 +193,27 @@ double pwl_interp1d(const std::vector<double>& x, const std::vector<double>& y, 
   return y[idx] + (y[idx + 1] - y[idx]) / (x[idx + 1] - x[idx]) * (q - x[idx]);
 }
 
+// libMath.f90:520-575, order 2: Lagrange interpolation through the two or
+// three table points around xq (x ascending; xq within the table).
+double interp1d2(double xq, const std::vector<double>& x, const std::vector<double>& y) {
+  const int n = (int)x.size();
+  int ix = -1;
+  for (int i = 0; i < n; ++i)
+    if (xq <= x[i]) { ix = i; break; }
+  if (ix < 0) throw std::runtime_error("interp1d: query beyond the table");
+  if (std::fabs(xq - x[ix]) <= EPS) return y[ix];
+  if (ix == 0) throw std::runtime_error("interp1d: query before the table");
+  if (std::sqrt(y[ix - 1] * y[ix - 1] + y[ix] * y[ix]) <= EPS) return 0.0;
+  if (n == 2) return y[ix - 1] + (xq - x[ix - 1]) * (y[ix] - y[ix - 1]) / (x[ix] - x[ix - 1]);
+  int a, b, c;
+  if (ix == 1) { a = 0; b = 1; c = 2; }
+  else { a = ix - 2; b = ix - 1; c = ix; }
+  const double L0 = (xq - x[b]) * (xq - x[c]) / ((x[a] - x[b]) * (x[a] - x[c]));
+  const double L1 = (xq - x[a]) * (xq - x[c]) / ((x[b] - x[a]) * (x[b] - x[c]));
+  const double L2 = (xq - x[a]) * (xq - x[b]) / ((x[c] - x[a]) * (x[c] - x[b]));
+  return y[a] * L0 + y[b] * L1 + y[c] * L2;
+}
+
 // libMath.f90:293-426 -- native Doolittle inverse used by lsq2.  Its pivot
 // search compares the ORIGINAL matrix against the running maximum, so for the
 // matrices lsq2 builds it never swaps a row; the literal search is kept.
@@ -443,6 +464,9 @@ struct Rotor {
   // customTrajectorySwitch = 1: body velocity and rates of every step
   // (velBodyHistory, omegaBodyHistory; classdef.f90:3065-3081)
   std::vector<V3> velBodyHistory, omegaBodyHistory;
+  // camber sections (CAMBERSECTIONS namelist, classdef.f90:2614-2687)
+  std::vector<double> camberSectionLimit;
+  std::vector<std::string> camberFile;
   double thetaTwist = 0;
   int ductSwitch = 0, axisymmetrySwitch = 0, spanwiseLiftSwitch = 0, symmetricTau = 0;
   int customTrajectorySwitch = 0, forceCalcSwitch = 0, nAirfoils = 0;
@@ -539,10 +563,10 @@ struct Namelist {
     if (it == kv.end() || it->second.empty()) return def;
     return (int)std::lround(todouble(it->second[0]));
   }
-  std::string s(const std::string& g, const std::string& k, const std::string& def = "0") const {
+  std::string s(const std::string& g, const std::string& k, const std::string& def = "0", size_t idx = 0) const {
     auto it = kv.find(lower(g) + "." + lower(k));
-    if (it == kv.end() || it->second.empty()) return def;
-    return it->second[0];
+    if (it == kv.end() || it->second.size() <= idx) return def;
+    return it->second[idx];
   }
   V3 v3(const std::string& g, const std::string& k) const { return mk(d(g, k, 0, 0), d(g, k, 0, 1), d(g, k, 0, 2)); }
   size_t count(const std::string& g, const std::string& k) const {
@@ -1461,7 +1485,12 @@ struct Sim {
     R.gammaPlotSwitch = g.i("PLOTS", "gammaPlotSwitch");
     R.skewPlotSwitch = g.i("PLOTS", "skewPlotSwitch");
     if (R.surfaceType < 0 || std::abs(R.surfaceType) == 2) throw std::runtime_error("only lifting surfaces (surfaceType 0/1) are supported");
-    if (R.nCamberFiles > 0) throw std::runtime_error("camber files are not supported by this oracle");
+    if (R.nCamberFiles > 0) {
+      for (int k = 0; k < R.nCamberFiles; ++k) {
+        R.camberSectionLimit.push_back(g.d("CAMBERSECTIONS", "camberSectionLimit", 1.0, k));
+        R.camberFile.push_back(g.s("CAMBERSECTIONS", "camberFile", "0", k));
+      }
+    }
     if (R.ductSwitch != 0) throw std::runtime_error("ductSwitch is not supported by this oracle");
     if (R.forceCalcSwitch != 0) throw std::runtime_error("only forceCalcSwitch = 0 is supported");
     if (R.bladeDynamicsSwitch != 0 || R.bodyDynamicsSwitch != 0)
@@ -1488,6 +1517,54 @@ struct Sim {
     return g;
   }
   // classdef.f90:2769-3891
+  // rotor_getCamber (classdef.f90:4060-4112): z of the chordwise points x at
+  // the spanwise stations y from the camber files (first value the point
+  // count, then x z pairs; normalised by the last x), the file of a station
+  // the first section whose limit is >= y/span.  Returns [i + nx j].
+  std::vector<double> getCamber(const std::vector<double>& x, const std::vector<double>& y) {
+    const int nx = (int)x.size(), ny = (int)y.size(), nf = R.nCamberFiles;
+    const double chord = x[nx - 1] - x[0];
+    const double span = y[ny - 1] - y[0];
+    std::vector<std::vector<double>> xc(nf), zc(nf);
+    for (int j = 0; j < nf; ++j) {
+      if (R.camberFile[j].empty() || R.camberFile[j][0] == '0') {
+        xc[j] = {0.0, 1.0};
+        zc[j] = {0.0, 0.0};
+        continue;
+      }
+      std::string path = R.camberFile[j];
+      if (path[0] != '/' && !baseDir.empty()) path = baseDir + "/" + path;
+      std::ifstream f(path);
+      if (!f) throw std::runtime_error("cannot open camber file " + path);
+      std::stringstream ss;
+      ss << f.rdbuf();
+      std::string t = ss.str();
+      for (char& c : t) if (c == ',') c = ' '; else if (c == 'd' || c == 'D') c = 'e';
+      std::istringstream in(t);
+      double np = 0;
+      if (!(in >> np) || np < 2) throw std::runtime_error(path + ": bad point count");
+      for (int i = 0; i < (int)np; ++i) {
+        double a, b;
+        if (!(in >> a >> b)) throw std::runtime_error(path + ": fewer points than its count");
+        xc[j].push_back(a);
+        zc[j].push_back(b);
+      }
+      const double xl = xc[j].back();
+      for (auto& v : zc[j]) v = v / xl;
+      for (auto& v : xc[j]) v = v / xl;
+    }
+    std::vector<double> out((size_t)nx * ny, 0.0);
+    int fNum = -1;
+    for (int j = 0; j < ny; ++j) {
+      for (int k = 0; k < nf; ++k)
+        if (y[j] / span <= R.camberSectionLimit[k]) { fNum = k; break; }
+      if (fNum < 0) throw std::runtime_error("camberSectionLimit does not cover the first station");
+      for (int i = 0; i < nx; ++i)
+        out[(size_t)i + (size_t)nx * j] = chord * interp1d2((x[i] - x[0]) / chord, xc[fNum], zc[fNum]);
+    }
+    return out;
+  }
+
   // trajectory01.in (classdef.f90:3065-3081): nt list-directed records of
   // u v w p q r; a record's values may run over lines, extra values on its
   // last line are skipped
@@ -1590,14 +1667,17 @@ struct Sim {
         case 4: yv = tanspace(s0, s1, ns + 1); break;
         default: throw std::runtime_error("bad spanSpacing");
       }
+      std::vector<double> zv((size_t)(nc + 1) * (ns + 1), 0.0);  // [i + (nc+1) j]
+      if (r.nCamberFiles > 0) zv = getCamber(xVec, yv);
+      auto z = [&](int i, int j) { return zv[(size_t)i + (size_t)(nc + 1) * j]; };
       for (auto& b : r.blade)
         for (int j = 0; j < ns; ++j)
           for (int i = 0; i < nc; ++i) {
             WingPanel& p = b.w(i, j);
-            p.PC[0] = mk(xVec[i], yv[j], 0.0);
-            p.PC[1] = mk(xVec[i + 1], yv[j], 0.0);
-            p.PC[2] = mk(xVec[i + 1], yv[j + 1], 0.0);
-            p.PC[3] = mk(xVec[i], yv[j + 1], 0.0);
+            p.PC[0] = mk(xVec[i], yv[j], z(i, j));
+            p.PC[1] = mk(xVec[i + 1], yv[j], z(i + 1, j));
+            p.PC[2] = mk(xVec[i + 1], yv[j + 1], z(i + 1, j + 1));
+            p.PC[3] = mk(xVec[i], yv[j + 1], z(i, j + 1));
           }
     } else {
       int nx, ny;

@@ -233,3 +233,18 @@ def test_custom_trajectory_bitwise(tmp_path):
     (tmp_path / "trajectory01.in").write_text("\n".join(rows) + "\n")
     g, r = run_both(cfg, geo, nt, base=tmp_path, chunk=16)
     assert_same_state(g, r)
+
+
+def test_cambered_wing_bitwise(tmp_path):
+    """Camber sections (nCamberFiles > 0): the cambered geometry enters
+    through the host geometry only, so the FP64 run stays bit-identical to
+    the oracle."""
+    xs = np.linspace(0.0, 1.0, 9)
+    (tmp_path / "camber.dat").write_text(f"{len(xs)}\n" + "\n".join(f"{x:.12f} {0.06 * x * (1 - x):.12f}" for x in xs))
+    cfg = C.config_text(nt=10, dt=0.025, density=1.0, fdScheme=3)
+    geo = C.geom_text(nb=1, nc=3, ns=5, nNwake=5, span=2.0, chord=0.5, theta0=3.0, velBody=(-10.0, 0.0, 0.0),
+                      wakeTruncateNt=8, chordSpacing=2, nCamberFiles=2)
+    geo = geo.replace("&ORIENT", "&CAMBERSECTIONS\ncamberSectionLimit = 0.5, 1.0\n"
+                      "camberFile = 'camber.dat', '0'\n/\n&ORIENT", 1)
+    g, r = run_both(cfg, geo, 10, base=tmp_path, chunk=16)
+    assert_same_state(g, r)

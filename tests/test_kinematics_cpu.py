@@ -141,3 +141,51 @@ def test_custom_trajectory_missing_or_short_file(tmp_path):
     (tmp_path / "trajectory01.in").write_text(_trajectory_text(3, 0))
     with pytest.raises(lib.VlmError):
         lib.wing_kinematics(cfg, geo, 1, "CP", 1, tmp_path)
+
+
+def _camber_case(tmp, omega, theta0=4.0, limits=(0.5, 1.0), files=("naca.dat", "tab.dat")):
+    xs = np.linspace(0.0, 1.0, 11)
+    (tmp / "naca.dat").write_text(f"{len(xs)}\n" + "\n".join(f"{x * 2.0:.12f} {0.08 * x * (1 - x) * 2.0:.12f}"
+                                                              for x in xs) + "\n")
+    tab = [(0.0, 0.0), (0.1, 0.012), (0.3, 0.03), (0.55, 0.028), (0.8, 0.015), (1.0, 0.0)]
+    (tmp / "tab.dat").write_text(f"{len(tab)}\n" + "\n".join(f"{a}d0, {b}D0" for a, b in tab) + "\n")
+    nf = len(files)
+    geo = C.geom_text(nb=2 if omega else 1, nc=4, ns=6, nNwake=3, span=1.5, rootcut=0.2 if omega else 0.0,
+                      chord=0.3, Omega=omega, shaftAxis=(0.0, 0.0, 1.0), theta0=theta0,
+                      velBody=(0.0, 0.0, 0.0) if omega else (-10.0, 0.0, 0.0), chordSpacing=2, spanSpacing=2,
+                      nCamberFiles=nf)
+    sect = ("&CAMBERSECTIONS\ncamberSectionLimit = " + ", ".join(str(v) for v in limits[:nf]) +
+            "\ncamberFile = " + ", ".join(f"'{f}'" for f in files) + "\n/\n")
+    geo = geo.replace("&ORIENT", sect + "&ORIENT", 1)
+    cfg = C.config_text(nt=4, dt=0.0 if omega else 0.025, density=1.0, fdScheme=3)
+    return cfg, geo
+
+
+@pytest.mark.parametrize("omega", [0.0, 60.0, -60.0])
+def test_camber_sections_match_oracle(tmp_path, omega):
+    """nCamberFiles > 0 (rotor_getCamber, src/classdef.f90:4060-4112, with
+    libMath interp1d of order 2): cambered panels, bit for bit against the oracle."""
+    cfg, geo = _camber_case(tmp_path, omega)
+    assert "&CAMBERSECTIONS" in geo
+    base = str(tmp_path)
+    nb = int(O.Sim(cfg, geo, base).geti("nb"))
+    for it in (0, 3):
+        r = O.Sim(cfg, geo, base)
+        r.start()
+        if it:
+            r.step(it)
+        for b in range(1, nb + 1):
+            for arr in ("PC", "CP", "nCap", "secCP"):
+                np.testing.assert_array_equal(lib.wing_kinematics(cfg, geo, it, arr, b, base), r.get(arr, b),
+                                              err_msg=f"omega {omega} iter {it} blade {b} {arr}")
+
+
+def test_camber_reproduces_a_parabola(tmp_path):
+    """A parabolic camber line is reproduced exactly by the quadratic
+    Lagrange interpolation (no pitch, so the panel corners keep the camber)."""
+    cfg, geo = _camber_case(tmp_path, 0.0, theta0=0.0, limits=(1.0,), files=("naca.dat",))
+    pc = lib.wing_kinematics(cfg, geo, 0, "PC", 1, tmp_path).reshape(6, 4, 4, 3)  # [j][i][corner]
+    x, z = pc[..., 0], pc[..., 2]
+    xi = (x - -0.3) / 0.3  # chord from -c (leading edge) to 0
+    np.testing.assert_allclose(z, 0.3 * 0.08 * xi * (1 - xi), rtol=0, atol=1e-14)
+    assert np.max(z) > 0.005

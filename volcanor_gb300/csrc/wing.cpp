@@ -122,10 +122,10 @@ int Namelist::i(const std::string& g, const std::string& k, int def) const {
   if (it == kv_.end() || it->second.empty()) return def;
   return (int)std::lround(to_double(it->second[0]));
 }
-std::string Namelist::s(const std::string& g, const std::string& k, const std::string& def) const {
+std::string Namelist::s(const std::string& g, const std::string& k, const std::string& def, size_t idx) const {
   auto it = kv_.find(lower(g) + "." + lower(k));
-  if (it == kv_.end() || it->second.empty()) return def;
-  return it->second[0];
+  if (it == kv_.end() || it->second.size() <= idx) return def;
+  return it->second[idx];
 }
 d3 Namelist::v3(const std::string& g, const std::string& k) const { return mk3(d(g, k, 0, 0), d(g, k, 0, 1), d(g, k, 0, 2)); }
 size_t Namelist::count(const std::string& g, const std::string& k) const {
@@ -320,7 +320,10 @@ void Wing::readGeom(const Namelist& g) {
   r.gammaPlotSwitch = g.i("PLOTS", "gammaPlotSwitch");
   r.skewPlotSwitch = g.i("PLOTS", "skewPlotSwitch");
   if (r.surfaceType < 0 || std::abs(r.surfaceType) == 2) throw std::runtime_error("unsupported: image or non-lifting surfaces");
-  if (r.nCamberFiles > 0) throw std::runtime_error("unsupported: camber files");
+  for (int k = 0; k < r.nCamberFiles; ++k) {
+    r.camberSectionLimit.push_back(g.d("CAMBERSECTIONS", "camberSectionLimit", 1.0, k));
+    r.camberFile.push_back(g.s("CAMBERSECTIONS", "camberFile", "0", k));
+  }
   if (r.ductSwitch != 0) throw std::runtime_error("unsupported: ductSwitch");
   if (r.forceCalcSwitch != 0) throw std::runtime_error("unsupported: forceCalcSwitch != 0 (C81 tables)");
   if (r.bladeDynamicsSwitch != 0 || r.bodyDynamicsSwitch != 0)
@@ -328,6 +331,82 @@ void Wing::readGeom(const Namelist& g) {
   if (r.customTrajectorySwitch != 0 && r.customTrajectorySwitch != 1)
     throw std::runtime_error("customTrajectorySwitch must be 0 or 1");
   if (r.nc < 1 || r.ns < 1 || r.nb < 1) throw std::runtime_error("nb, nc and ns must be positive");
+}
+
+// libMath interp1d with order 2 (src/libMath.f90:520-575): Lagrange
+// interpolation through the two or three table points around xq (x
+// ascending, xq within the table).
+static double interp1d2(double xq, const std::vector<double>& x, const std::vector<double>& y) {
+  const int n = (int)x.size();
+  int ix = -1;
+  for (int i = 0; i < n; ++i)
+    if (xq <= x[i]) {
+      ix = i;
+      break;
+    }
+  if (ix < 0) throw std::runtime_error("camber interpolation beyond the table");
+  if (std::fabs(xq - x[ix]) <= kEps) return y[ix];
+  if (ix == 0) throw std::runtime_error("camber interpolation before the table");
+  if (std::sqrt(y[ix - 1] * y[ix - 1] + y[ix] * y[ix]) <= kEps) return 0.0;
+  if (n == 2) return y[ix - 1] + (xq - x[ix - 1]) * (y[ix] - y[ix - 1]) / (x[ix] - x[ix - 1]);
+  const int a = ix == 1 ? 0 : ix - 2, b = a + 1, c = a + 2;
+  const double L0 = (xq - x[b]) * (xq - x[c]) / ((x[a] - x[b]) * (x[a] - x[c]));
+  const double L1 = (xq - x[a]) * (xq - x[c]) / ((x[b] - x[a]) * (x[b] - x[c]));
+  const double L2 = (xq - x[a]) * (xq - x[b]) / ((x[c] - x[a]) * (x[c] - x[b]));
+  return y[a] * L0 + y[b] * L1 + y[c] * L2;
+}
+
+// rotor_getCamber (src/classdef.f90:4060-4112): z of the chordwise points x
+// at the spanwise stations y from the camber files (a point count, then x z
+// pairs, normalised by the last x; '0' = no camber), each station using the
+// first section whose limit is >= y/span.  Returns [i + nx j].
+std::vector<double> Wing::getCamber(const std::vector<double>& x, const std::vector<double>& y) const {
+  const int nx = (int)x.size(), ny = (int)y.size(), nf = P.nCamberFiles;
+  const double chord = x[nx - 1] - x[0];
+  const double span = y[ny - 1] - y[0];
+  std::vector<std::vector<double>> xc(nf), zc(nf);
+  for (int j = 0; j < nf; ++j) {
+    if (P.camberFile[j].empty() || P.camberFile[j][0] == '0') {
+      xc[j] = {0.0, 1.0};
+      zc[j] = {0.0, 0.0};
+      continue;
+    }
+    std::string path = P.camberFile[j];
+    if (path[0] != '/' && !baseDir.empty()) path = baseDir + "/" + path;
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open camber file " + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string t = ss.str();
+    for (char& c : t) {
+      if (c == ',') c = ' ';
+      else if (c == 'd' || c == 'D') c = 'e';
+    }
+    std::istringstream in(t);
+    double np = 0;
+    if (!(in >> np) || np < 2) throw std::runtime_error(path + ": bad point count");
+    for (int i = 0; i < (int)np; ++i) {
+      double a, b;
+      if (!(in >> a >> b)) throw std::runtime_error(path + ": fewer points than its count");
+      xc[j].push_back(a);
+      zc[j].push_back(b);
+    }
+    const double xl = xc[j].back();
+    for (auto& v : zc[j]) v = v / xl;
+    for (auto& v : xc[j]) v = v / xl;
+  }
+  std::vector<double> out((size_t)nx * ny, 0.0);
+  int fNum = -1;
+  for (int j = 0; j < ny; ++j) {
+    for (int k = 0; k < nf; ++k)
+      if (y[j] / span <= P.camberSectionLimit[k]) {
+        fNum = k;
+        break;
+      }
+    if (fNum < 0) throw std::runtime_error("camberSectionLimit does not cover the first station");
+    for (int i = 0; i < nx; ++i) out[(size_t)i + (size_t)nx * j] = chord * interp1d2((x[i] - x[0]) / chord, xc[fNum], zc[fNum]);
+  }
+  return out;
 }
 
 // trajectory01.in (src/classdef.f90:3065-3081): nt list-directed records of
@@ -529,14 +608,17 @@ void Wing::init() {
     const double cs = r.Omega >= 0 ? -r.chord : r.chord;
     const auto xv = spacing(r.chordSpacing, cs, 0.0, nc + 1);
     const auto yv = spacing(r.spanSpacing, r.root_cut * r.radius, r.radius, ns + 1);
+    std::vector<double> zv((size_t)(nc + 1) * (ns + 1), 0.0);  // [i + (nc+1) j]
+    if (r.nCamberFiles > 0) zv = getCamber(xv, yv);
+    auto z = [&](int i, int j) { return zv[(size_t)i + (size_t)(nc + 1) * j]; };
     for (auto& b : bl)
       for (int j = 0; j < ns; ++j)
         for (int i = 0; i < nc; ++i) {
           Panel& p = b.w(i, j);
-          p.PC[0] = mk3(xv[i], yv[j], 0.0);
-          p.PC[1] = mk3(xv[i + 1], yv[j], 0.0);
-          p.PC[2] = mk3(xv[i + 1], yv[j + 1], 0.0);
-          p.PC[3] = mk3(xv[i], yv[j + 1], 0.0);
+          p.PC[0] = mk3(xv[i], yv[j], z(i, j));
+          p.PC[1] = mk3(xv[i + 1], yv[j], z(i + 1, j));
+          p.PC[2] = mk3(xv[i + 1], yv[j + 1], z(i + 1, j + 1));
+          p.PC[3] = mk3(xv[i], yv[j + 1], z(i, j + 1));
         }
   } else {
     // src/classdef.f90:3957-4020 (PLOT3D, nx = nc+1, ny = ns+1, nz = 1)

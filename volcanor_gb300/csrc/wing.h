@@ -23,7 +23,7 @@ class Namelist {
   bool has(const std::string& group, const std::string& key) const;
   double d(const std::string& group, const std::string& key, double def = 0.0, size_t idx = 0) const;
   int i(const std::string& group, const std::string& key, int def = 0) const;
-  std::string s(const std::string& group, const std::string& key, const std::string& def = "0") const;
+  std::string s(const std::string& group, const std::string& key, const std::string& def = "0", size_t idx = 0) const;
   d3 v3(const std::string& group, const std::string& key) const;
   size_t count(const std::string& group, const std::string& key) const;
 
@@ -58,6 +58,9 @@ struct RotorParams {  // rotor_readGeom inputs (src/classdef.f90:2541-2767)
   // src/classdef.f90:3065-3081); velBodyInput is the namelist value
   std::vector<d3> velBodyHistory, omegaBodyHistory;
   d3 velBodyInput{0, 0, 0};
+  // camber sections (CAMBERSECTIONS namelist, src/classdef.f90:2614-2687)
+  std::vector<double> camberSectionLimit;
+  std::vector<std::string> camberFile;
   // read only to be echoed into rXXParams.json
   int imagePlane = 0, imageRotorNum = 0, nAirfoils = 0;
   double thetaTwist = 0, Iflap = 0, cflap = 0, kflap = 0, MflapConstant = 0, alpha0 = 0;
@@ -111,6 +114,7 @@ class Wing {
   void init();
   void toChordsRevs(int& n) const;
   void readTrajectory();
+  std::vector<double> getCamber(const std::vector<double>& x, const std::vector<double>& y) const;
   void blade_move(Blade& b, d3 d);
   void blade_rot_pts(Blade& b, d3 pts, d3 o);
   void blade_rotate(Blade& b, double ang, d3 axis, d3 o, int type);
