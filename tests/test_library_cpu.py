@@ -67,3 +67,27 @@ def test_fp32_chunk_plan_shapes():
     mid = lib.rings_sum_chunk(12480, 13395, lib.PREC_FP32_NEAR64)
     assert 128 <= mid < 12480
     assert lib.rings_sum_chunk(0, 100, lib.PREC_FP32) == 0
+
+
+def test_binding_arity_matches_header():
+    """Every ctypes signature takes as many arguments as include/vlm.h declares."""
+    text = (ROOT / "include" / "vlm.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    for name, params in re.findall(r"\b(vlm_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        p = params.strip()
+        n = 0 if p in ("", "void") else p.count(",") + 1
+        assert len(lib.SIGNATURES[name][1]) == n, (name, n, len(lib.SIGNATURES[name][1]))
+
+
+def test_options_struct_matches_header():
+    """vlm_options field order and types (the Fortran type and ctypes mirror it)."""
+    text = (ROOT / "include" / "vlm.h").read_text()
+    body = re.search(r"typedef struct vlm_options \{(.*?)\} vlm_options;", text, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"\b(int|double)\s+(\w+)\s*;", body)
+    mirror = [(("double" if t is ctypes.c_double else "int"), n) for n, t in lib.Options._fields_]
+    assert fields == mirror
+    integ = (ROOT / "INTEGRATION.md").read_text()
+    ftype = re.search(r"type, bind\(c\) :: vlm_options(.*?)end type", integ, flags=re.S).group(1)
+    fnames = re.findall(r"::\s*(\w+)", ftype)
+    assert fnames == [n for _, n in fields]
