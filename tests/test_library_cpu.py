@@ -91,3 +91,19 @@ def test_options_struct_matches_header():
     ftype = re.search(r"type, bind\(c\) :: vlm_options(.*?)end type", integ, flags=re.S).group(1)
     fnames = re.findall(r"::\s*(\w+)", ftype)
     assert fnames == [n for _, n in fields]
+
+
+def test_fortran_interfaces_match_header():
+    """The iso_c_binding interfaces shipped for Fortran hosts bind existing
+    symbols with the header's argument counts."""
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "vlm.h").read_text(), flags=re.S)
+    arity = {}
+    for name, params in re.findall(r"\b(vlm_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        p = params.strip()
+        arity[name] = 0 if p in ("", "void") else p.count(",") + 1
+    integ = (ROOT / "INTEGRATION.md").read_text().replace("&\n", " ")
+    found = re.findall(r"(?:function|subroutine)\s+\w+\(([^)]*)\)\s*bind\(c,\s*name='(vlm_\w+)'\)", integ)
+    assert len(found) >= 10
+    for args, name in found:
+        n = len([a for a in args.split(",") if a.strip()])
+        assert arity[name] == n, (name, arity[name], n)
