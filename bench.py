@@ -14,7 +14,9 @@ e2e:   the same steps through the public C entry point vlm_case_step, one call
        per step: the step's wing kinematics frame host->device, the kernels,
        the step's CT row device->host, wall clock.
 --impl reference: the reference algorithm on the host CPU (the C++ oracle,
-       all cores), a bounded sample of the same workload per step.
+       all cores) stepping the same case through the same steady-state steps,
+       from the state the FP64 GPU solver reaches there (the oracle cannot
+       afford the first 432 steps in a bench run; see run_reference).
 """
 from __future__ import annotations
 
@@ -150,50 +152,38 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample(case_gpu, seconds: float = 12.0, max_targets: int = 4096):
-    """Oracle (C++ restatement, OpenMP all cores) on a bounded sample of the
-    steady-state wake: sampled wake-node targets x every near-wake ring of the
-    GPU state.  Returns (ring pairs/s, threads, description)."""
+def cpu_handoff(c, case_gpu, chunk: int = 256):
+    """An oracle (the C++ FP64 restatement of the reference's path, OpenMP
+    over targets on all host cores) of case files c, brought to the flow state
+    of GPU case_gpu at its iteration (oracle/handoff.py)."""
+    from oracle import handoff
     from oracle import oracle as O
-    nb = case_gpu.geti("nb")
-    corners, rvc, gam, nodes = [], [], [], []
-    for b in range(1, nb + 1):
-        c = case_gpu.get("waN", b).reshape(-1, 4, 3)
-        corners.append(c)
-        rvc.append(case_gpu.get("waN_rvc", b).reshape(-1, 4))
-        gam.append(case_gpu.get("waN_gam", b))
-        nodes.append(c[:, 1])
-    corners, rvc, gam = np.concatenate(corners), np.concatenate(rvc), np.concatenate(gam)
-    nodes = np.concatenate(nodes)
-    rng = np.random.default_rng(0)
-    threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    m = 64
-    t = 0.0
-    while True:
-        P = nodes[rng.choice(len(nodes), size=min(m, len(nodes)), replace=False)]
+    O.set_threads(os.cpu_count() or 1)
+    sim = O.Sim(c.config, c.geom)
+    sim.set_sum_chunk(chunk)
+    sim.start()
+    handoff.load_case_state(sim, case_gpu)
+    return sim
+
+
+def cpu_steps(sim, gpu_rows, seconds: float):
+    """Times whole oracle timesteps from its current state (at least one, up
+    to `seconds`), and checks their CT rows against the FP64 GPU rows of the
+    same steps from the same state (gpu_rows)."""
+    times = []
+    while len(times) < len(gpu_rows) and (not times or sum(times) < seconds):
         t0 = time.perf_counter()
-        O.vind_rings(corners, rvc, gam, P)
-        t = time.perf_counter() - t0
-        if t > seconds / 4 or m >= max_targets:
-            break
-        m *= 2
-    pairs = float(P.shape[0]) * corners.shape[0]
-    desc = (f"{P.shape[0]} wake-node targets x {corners.shape[0]} near-wake rings of the steady-state wake "
-            f"({pairs:.3g} ring pairs, {t:.2f} s)")
-    return pairs / t, threads, desc
-
-
-def pairs_per_step(case_gpu):
-    """Ring-equivalent pairs (4 filament pairs = 1 ring pair) of one steady-state
-    step: two wake-node evaluations (wing + wake sources) and the
-    collocation-point evaluation (wake sources)."""
-    g = case_gpu.geti
-    nb, nc, ns, NW, NF, nbc = g("nb"), g("nc"), g("ns"), g("nNwake"), g("nFwake"), g("nbConvect")
-    m_nodes = nbc * (NW * (ns + 1) + NF)
-    src_wake = nb * NW * ns + nb * (ns + NF) / 4.0
-    src_all = nb * nc * ns + src_wake
-    return 2.0 * m_nodes * src_all + nbc * nc * ns * src_wake
+        sim.step(1)
+        times.append(time.perf_counter() - t0)
+    n = len(times)
+    ref = sim.ct_hist()[-n:]
+    same = bool(np.array_equal(ref, gpu_rows[:n]))
+    threads = os.cpu_count() or 1
+    return {"value": round(n / sum(times), 4), "unit": "timesteps/s", "cores": threads, "kind": "port",
+            "sample": (f"{n} whole timesteps (steps {int(ref[0, 0])}-{int(ref[-1, 0])}) of the same case from the "
+                       f"timed window's start state, {sum(times):.1f} s; oracle = C++ FP64 restatement of the "
+                       "reference's path with OpenMP over targets (no Fortran compiler for the reference itself)"),
+            "ct_rows_bitwise_equal_to_fp64_gpu": same}
 
 
 def cfg3_rings(M: int, N: int, seed: int = 0):
@@ -280,6 +270,12 @@ def run_ours(args):
         n = min(100, FULL_WAKE_STEP + W - done)
         case.step(n, with_ct=False)
         done += n
+    # the state at the start of the timed window: the FP64 GPU form, the
+    # accuracy check and the CPU baseline all continue from it
+    import tempfile
+    tmpdir = tempfile.TemporaryDirectory()
+    ck = Path(tmpdir.name) / "window_start.ckpt"
+    case.checkpoint_save(ck)
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
@@ -319,6 +315,10 @@ def run_ours(args):
     sm_count = lib.device_info(local)[0]
     fp32_peak = sm_count * 128 * 2 * sm_max * 1e6 / 1e12
     clocks = clk.summary()
+    # the FP32 CUDA-core peak measured on this device (the library's
+    # FMA-chain kernel), with the SM clock sampled while it runs
+    with ClockSampler(local) as pclk:
+        fp32_meas, fp32_meas_ms = lib.measure_fp32_peak(local, reps=200)
     out = {
         "metric": METRIC,
         "value": round(value, 3),
@@ -355,11 +355,40 @@ def run_ours(args):
                                   "rings once, so the kernel executes fewer flops: executed_* (9 per corner "
                                   "vector, 35 per filament evaluated)",
                      "peak_note": "nominal FP32 CUDA-core peak (SMs x 128 lanes x 2 x max SM clock); "
-                                  "MEASURED_PEAKS.json has no FP32 figure"},
+                                  "MEASURED_PEAKS.json has no FP32 figure",
+                     "peak_measured": round(fp32_meas, 2),
+                     "frac_measured": round(achieved / fp32_meas, 4),
+                     "executed_frac_measured": round(exec_flops / (ms_l / 1e3) / 1e12 / fp32_meas, 4),
+                     "peak_measured_note": "vlm_measure_fp32_peak: independent FMA chains on every SM, "
+                                           f"{fp32_meas_ms:.3f} ms per launch, CUDA events, 200 launches",
+                     "peak_measured_clocks": pclk.summary()},
         "clocks": clocks,
         "ct_last": float(rows[-1, 1]),
     }
     out["pairs_per_s"] = round(rp / (ms_l / 1e3), 1)
+    if rank == 0 and not args.no_accuracy:
+        # the plain FP64 GPU form over the same K steps from the same state:
+        # its rate, and this precision's CT error against it on the timed
+        # window (K steps stay inside the free wake's pre-chaotic horizon)
+        f64 = lib.Case(c.config, c.geom, precision=lib.PREC_FP64, device=local)
+        f64.checkpoint_load(ck)
+        sim = None
+        if not args.no_cpu:
+            sim = cpu_handoff(c, f64)
+        r64 = f64.step(K)
+        ms64 = f64.last_step_ms()
+        v64 = K / (ms64 / 1e3)
+        out["fp64_gpu"] = {"value": round(v64, 3), "unit": "timesteps/s", "ms_per_step": round(ms64 / K, 3),
+                           "value_over_fp64": round(value / v64, 2),
+                           "note": "plain FP64 GPU form (FP64 pairs, FP64 inverse) over the same K steps from the "
+                                   "same start state"}
+        rel = np.abs(rows[:, 1] - r64[:, 1]) / np.abs(r64[:, 1])
+        out["accuracy"] = {"ct_max_rel_err_timed_window": float(rel.max()), "timed_window_steps": K,
+                           "timed_window": [int(rows[0, 0]), int(rows[-1, 0])],
+                           "against": "the FP64 GPU form from the same start state"}
+        if sim is not None:
+            out["cpu_baseline"] = cpu_steps(sim, r64, args.cpu_seconds)
+        f64.close()
     if rank == 0 and not args.no_accuracy and prec != lib.PREC_FP64:
         # this precision's CT error against the FP64 GPU form over the first
         # revolution (the free wake's pre-chaotic horizon; see the accuracy module)
@@ -371,8 +400,10 @@ def run_ours(args):
         x.start()
         b = x.step(72)[:, 1]
         x.close()
-        out["accuracy"] = {"ct_max_rel_err_vs_fp64_first_rev": float(np.max(np.abs(b - a) / np.abs(a))),
-                           "steps": 72, "note": "the full 1440-step comparison is volcanor_gb300/accuracy.py"}
+        out.setdefault("accuracy", {})
+        out["accuracy"].update({"ct_max_rel_err_vs_fp64_first_rev": float(np.max(np.abs(b - a) / np.abs(a))),
+                                "first_rev_steps": 72,
+                                "note": "the full 1440-step comparison is volcanor_gb300/accuracy.py"})
     if not args.no_kernel:
         # the isolated N-body kernel in both FP32 forms (the FP64 form runs
         # ~60x slower on this part: see the bench's fp64 precision)
@@ -383,15 +414,7 @@ def run_ours(args):
             k3["workload"] = ("isolated kernel: 2^20 targets x 2^18 rings (U[0,1]^3, edges U(0.005,0.05), "
                               "core 0.002)")
             out[key] = k3
-    if rank == 0 and not args.no_cpu:
-        try:
-            rate, threads, desc = cpu_sample(case, seconds=args.cpu_seconds)
-            eq = pairs_per_step(case)
-            out["cpu_baseline"] = {"value": round(rate / eq, 4), "unit": "timesteps/s", "cores": threads,
-                                   "kind": "port", "sample": desc + f"; converted at {eq:.4g} ring pairs per step"}
-        except Exception as e:  # the baseline is reported, never required
-            out["cpu_baseline"] = {"value": None, "unit": "timesteps/s", "cores": None, "kind": "port",
-                                   "sample": f"failed: {e}"}
+    tmpdir.cleanup()
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -399,94 +422,62 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def helix_wake(nb: int, ns: int, nw: int, radius: float, rootcut: float, omega: float, dt: float,
-               core: float, seed: int = 0):
-    """Near-wake rings of a prescribed helical hover wake with the case's node
-    counts (nb blades x nw rows x ns rings): node (i, j) of blade b at radius
-    r_j, azimuth 2 pi b / nb - omega dt i, descending at the momentum-theory
-    induced velocity.  The FP64 filament kernel's cost does not depend on the
-    positions, so this stands in for the solver's wake in CPU timing."""
-    rng = np.random.default_rng(seed)
-    r = np.linspace(rootcut * radius, radius, ns + 1)
-    vi = omega * radius * np.sqrt(0.0035 / 2.0)
-    corners = []
-    for b in range(nb):
-        i = np.arange(nw + 1)[:, None]
-        psi = 2.0 * np.pi * b / nb - omega * dt * i
-        x, y = r[None, :] * np.cos(psi), r[None, :] * np.sin(psi)
-        z = np.broadcast_to(-vi * dt * i, x.shape)
-        nodes = np.stack([x, y, z], -1)  # [row][station]
-        c = np.stack([nodes[:-1, :-1], nodes[1:, :-1], nodes[1:, 1:], nodes[:-1, 1:]], 2)  # [row][ring][4][3]
-        corners.append(c.reshape(-1, 4, 3))
-    corners = np.concatenate(corners)
-    rvc = np.full((corners.shape[0], 4), core)
-    gam = rng.normal(0.0, 0.05, corners.shape[0])
-    nodes = corners[:, 1]
-    return corners, rvc, gam, nodes
-
-
-def oracle_pairs_per_step(sim):
-    """pairs_per_step from the oracle's case dimensions."""
-    g = sim.geti
-    nb, nc, ns, NW, NF, nbc = g("nb"), g("nc"), g("ns"), g("nNwake"), g("nFwake"), g("nbConvect")
-    m_nodes = nbc * (NW * (ns + 1) + NF)
-    src_wake = nb * NW * ns + nb * (ns + NF) / 4.0
-    src_all = nb * nc * ns + src_wake
-    return 2.0 * m_nodes * src_all + nbc * nc * ns * src_wake
-
-
 def run_reference(args):
-    """Reference arm: the reference algorithm on the host cores, no GPU.  The
-    reference is Fortran and no Fortran compiler exists here, so this times
-    the oracle (the C++ FP64 restatement, OpenMP over targets like the
-    reference): each "step" is a bounded sample -- sampled wake-node targets x
-    every near-wake ring of a steady-state-sized helical wake -- converted to
-    timesteps/s by the ring pairs of one steady-state step of the case."""
+    """Reference arm: the reference's CPU algorithm on the host cores.
+
+    The reference is Fortran and neither machine has a Fortran compiler, so
+    the arm runs the oracle -- the C++ FP64 restatement of the reference's
+    path, OpenMP over targets as the reference's drivers -- on every host
+    core.  It steps the same case through the same steady-state steps as the
+    GPU arm's timed window (steps FULL_WAKE_STEP + W + 1 .. + K).  The oracle
+    needs tens of minutes for the first 432 steps of this wake, so it starts
+    from the state the FP64 GPU solver reaches at step FULL_WAKE_STEP (set-up
+    only, outside the timed region: the GPU and the oracle are bit-identical
+    step by step in FP64 with the same summation blocks,
+    tests/test_gpu_parity_full.py), runs W untimed warm-up steps and K timed
+    steps.  The GPU's FP64 form then runs the same W + K steps from the same
+    state, and the line reports whether the CT rows agree bit for bit."""
     rank = env_int("RANK", 0)
     if rank != 0:
         return
-    import tempfile
-    from oracle import oracle as O
+    from volcanor_gb300 import lib
     K, W = args.steps, args.warmup
-    c = C.rotor_2blade_hover(nt=1440)
-    with tempfile.TemporaryDirectory() as d:
-        c.write(d)
-        sim = O.Sim.from_case_dir(d)
-    eq = oracle_pairs_per_step(sim)
-    nb, ns, NW = sim.geti("nb"), sim.geti("ns"), sim.geti("nNwake")
-    corners, rvc, gam, nodes = helix_wake(nb, ns, NW, 1.0, 0.2, 100.0, 5.0 * np.pi / 180.0 / 100.0, 0.004)
+    start = FULL_WAKE_STEP
+    c = C.rotor_2blade_hover(nt=max(start + W + K + 2, 1440))
+    g = lib.Case(c.config, c.geom, precision=lib.PREC_FP64, sum_chunk=256, device=env_int("LOCAL_RANK", 0))
+    g.start()
+    t_setup = time.perf_counter()
+    done = 0
+    while done < start:
+        n = min(100, start - done)
+        g.step(n, with_ct=False)
+        done += n
+    sim = cpu_handoff(c, g)
+    t_setup = time.perf_counter() - t_setup
     threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    rng = np.random.default_rng(0)
-    per_step = args.cpu_seconds / max(1, W + K)
-    # size the sample once: doubling target counts until one call takes a step's share
-    m = 64
-    while True:
-        P = nodes[rng.choice(len(nodes), size=min(m, len(nodes)), replace=False)]
+    times = []
+    for _ in range(W + K):
         t0 = time.perf_counter()
-        O.vind_rings(corners, rvc, gam, P)
-        t = time.perf_counter() - t0
-        if t > per_step / 2 or m >= 4096:
-            break
-        m *= 2
-    rates = []
-    for i in range(W + K):
-        P = nodes[rng.choice(len(nodes), size=P.shape[0], replace=False)]
-        t0 = time.perf_counter()
-        O.vind_rings(corners, rvc, gam, P)
-        t = time.perf_counter() - t0
-        if i >= W:
-            rates.append(P.shape[0] * corners.shape[0] / t)
-    val = float(np.mean(rates)) / eq
-    desc = (f"{P.shape[0]} wake-node targets x {corners.shape[0]} near-wake rings of a helical wake with the case's "
-            f"node counts, {K} timed samples after {W} warm-up; oracle (C++ FP64 restatement, not the Fortran "
-            f"reference: no Fortran compiler); converted at {eq:.4g} ring pairs per step")
+        sim.step(1)
+        times.append(time.perf_counter() - t0)
+    timed = float(sum(times[W:]))
+    val = K / timed
+    rows_cpu = sim.ct_hist()[-(W + K):]
+    rows_gpu = g.step(W + K)
+    same = bool(np.array_equal(rows_cpu, rows_gpu))
+    desc = (f"{K} whole timesteps (steps {start + W + 1}-{start + W + K}) after {W} untimed warm-up steps, from the "
+            f"FP64 GPU solver's state at step {start}; oracle = C++ FP64 restatement of the reference's path "
+            f"(OpenMP over targets, {threads} threads, summation blocks of 256) -- the Fortran reference cannot be "
+            "compiled on these machines")
     out = {"impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "timesteps/s", "n_gpus": 1,
-           "steps": K, "warmup": W, "ms_per_step": round(1e3 / val, 3), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD},
+           "steps": K, "warmup": W, "ms_per_step": round(1e3 * timed / K, 2), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (volcanor_gb300/cases.py)",
+           "config": {"workload": WORKLOAD, "precision": "fp64 (reference arithmetic)"},
            "cpu_baseline": {"value": round(val, 4), "unit": "timesteps/s", "cores": threads, "kind": "port",
                             "sample": desc},
-           "e2e": {"value": round(val, 4), "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": round(val, 4), "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "ct_rows_bitwise_equal_to_fp64_gpu": same, "setup_s": round(t_setup, 1),
+           "timed_s": round(timed, 2)}
     print(json.dumps(out))
 
 

@@ -77,6 +77,11 @@ int64_t vlm_kernel_launch_count(void);
 int vlm_selftest_bounded_wait(int limit, int* expired);
 /* SM count and compute capability of `device`. */
 int vlm_device_info(int device, int* sm_count, int* cc_major, int* cc_minor);
+/* FP32 CUDA-core throughput of `device` as measured (no counterpart in the
+ * reference): a kernel of independent FMA chains on every SM, `reps` timed
+ * launches after one warm-up, CUDA events.  *tflops = 2 flop per FMA / time;
+ * the denominator of the N-body kernel's measured roofline fraction. */
+int vlm_measure_fp32_peak(int device, int reps, double* tflops, double* ms_per_launch);
 
 /* ---- isolated Biot-Savart kernel ------------------------------------------
  * V[m] = sum_n vr_vind(ring n, P[m]) * gam[n]: the unit-strength Vatistas
@@ -121,8 +126,10 @@ int vlm_biot_savart_filaments_device(const double* fc, const double* rvc, const 
  * Limits: N <= 16384 rings, M <= 65536 points, at most 65536 near-field
  * pairs (VLM_PREC_FP32_NEAR64); larger sizes return VLM_ERR_INVALID with a
  * message.  The rings are summed in one block, i.e. in the reference's order.
- * The first call on a device looks up the scratch array's device address,
- * so make that first call before any CUDA stream capture.  All calls on a
+ * The first call on a device looks up the scratch array's device address
+ * and keeps it for the life of the process, so make that first call before
+ * any CUDA stream capture, and do not reset the device (cudaDeviceReset)
+ * once it has been made.  All calls on a
  * device share the scratch and the call returns after its stream has
  * finished; calls that overlap on the GPU (other host threads or streams at
  * the same time) race on the scratch and must be serialised by the caller. */
@@ -171,6 +178,10 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *   waN_age (blade)                 (nNwake, ns) near-wake ring ages
  *   vr_rvc (blade)                  (4, nc, ns) wing ring filament core radii
  *   velN, velF (blade)              (3, nNwake, ns+1), (3, nFwake) node velocities
+ *   velN1..velN3, velF1..velF3 (blade)  the same shapes: the velocity history of the
+ *                                   multi-step schemes (velNwake1..3, velFwake1..3)
+ *   gamPrev (blade)                 (nc, ns) the previous step's trapezoidal circulation
+ *                                   (the unsteady term of the loads)
  *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section
  *   forceDist (blade <= nbConvect)  (16, ns): the columns of rXXbYYForceDistNNNNN.csv
  *                                   (src/libPostprocess.f90:850-878) for the current iteration
@@ -207,9 +218,13 @@ int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V);
  * restartFromNt, src/main.f90:389-397,1443-1450).  save writes the case's
  * whole solver state (step counter, circulations, wake, loads history, AIC
  * factors) to a binary file; load restores it into a case created from the
- * same case files and options (started or not), which then continues
- * bit-identically.  A different case, options or format -> VLM_ERR_INVALID.
- * Not available with the surrogate (VLM_ERR_UNSUPPORTED). */
+ * same case files (started or not).  With the same options the case then
+ * continues bit-identically; the state is FP64 in every precision, so a case
+ * of another precision, summation block or solve mode may also load it and
+ * continue in its own arithmetic (a refining case factors the restored AIC
+ * in FP32 when the file has no FP32 factors).  A case of other dimensions or
+ * another format -> VLM_ERR_INVALID.  Not available with the surrogate
+ * (VLM_ERR_UNSUPPORTED). */
 int vlm_case_checkpoint_save(vlm_case* c, const char* path);
 int vlm_case_checkpoint_load(vlm_case* c, const char* path);
 /* Device time of the kernels of the last vlm_case_step call, milliseconds

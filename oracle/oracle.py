@@ -64,6 +64,8 @@ def lib():
         L.or_get.argtypes = [vp, cp, i32, dp, i64]
         L.or_get.restype = i64
         L.or_sim_vind_points.argtypes = [vp, dp, i64, dp, i32]
+        L.or_sim_skip_to.argtypes = [vp, i32]
+        L.or_set.argtypes = [vp, cp, i32, dp, i64]
         L.or_vind_rings.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
         L.or_vind_filaments.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
         L.or_vf_vind.argtypes = [dp, dp, ctypes.c_double, dp, dp]
@@ -126,6 +128,16 @@ class Sim:
 
     def step(self, n: int = 1):
         _check(lib().or_sim_step(self._h, int(n)))
+
+    def skip_to(self, k: int):
+        """Advance to iteration k with the prescribed kinematics only (no
+        flow); the flow state of iteration k is then set with :meth:`set`."""
+        _check(lib().or_sim_skip_to(self._h, int(k)))
+
+    def set(self, name: str, ib: int, values) -> None:
+        """Set a named flow-state array (layouts of :meth:`get`)."""
+        v = _f64(values).reshape(-1)
+        _check(lib().or_set(self._h, name.encode(), int(ib), _ptr(v), v.size))
 
     # unit-test primitives
     def rot_pitch(self, ib: int, theta: float):

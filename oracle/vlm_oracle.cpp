@@ -1893,6 +1893,41 @@ struct Sim {
   void step() {
     if (!started) start();
     if (iter >= nt) throw std::runtime_error("all timesteps done");
+    advanceKinematics();
+    if (sw.wakeSuppress == 0 && R.nNwake > 0) {
+      assignshed(true);
+      age_wake();
+      if (sw.wakeDissipation == 1) dissipate_wake();
+      if (sw.wakeBurst != 0) throw std::runtime_error("wakeBurst is not supported");
+    }
+    for (int i = 0; i <= sw.ntSub; ++i) {
+      solveCirculation(true);
+      if (sw.ntSub != 0) {
+        double s = 0.0;
+        for (int k = 0; k < R.n(); ++k) s = s + (R.gamVec[k] - R.gamVecPrev[k]) * (R.gamVec[k] - R.gamVecPrev[k]);
+        if (std::sqrt(s) <= EPS) break;
+      }
+    }
+    if (sw.rotorForcePlot != 0 && iter % sw.rotorForcePlot == 0) {
+      computeForces();
+      force2file();
+    }
+    if (sw.wakeSuppress == 0 && R.nNwake > 0) wakeUpdate();
+  }
+
+  // Iterations iter+1..k with their kinematics only (counters, slow start,
+  // body motion, azimuth and pitch): the prescribed motion does not depend on
+  // the flow, so this reaches iteration k's wing geometry exactly; the flow
+  // state of iteration k is then set from outside (or_set).
+  void skipTo(int k) {
+    if (!started) start();
+    if (k < iter || k > nt) throw std::runtime_error("skip target out of range");
+    while (iter < k) advanceKinematics();
+  }
+
+  // main.f90:410-463: the iteration counter, rowNear/rowFar, custom
+  // trajectory, slow start and the rotor's motion for one iteration
+  void advanceKinematics() {
     ++iter;
     t = t + dt;
     R.rowNear = std::max(R.rowNear - 1, 1);
@@ -1913,25 +1948,6 @@ struct Sim {
     rotor_move(R.velBody * dt);
     rotor_rot_pts(R.omegaBody * dt, R.cgCoords);
     rotor_rot_advance(R.omegaSlow * dt, false);
-    if (sw.wakeSuppress == 0 && R.nNwake > 0) {
-      assignshed(true);
-      age_wake();
-      if (sw.wakeDissipation == 1) dissipate_wake();
-      if (sw.wakeBurst != 0) throw std::runtime_error("wakeBurst is not supported");
-    }
-    for (int i = 0; i <= sw.ntSub; ++i) {
-      solveCirculation(true);
-      if (sw.ntSub != 0) {
-        double s = 0.0;
-        for (int k = 0; k < R.n(); ++k) s = s + (R.gamVec[k] - R.gamVecPrev[k]) * (R.gamVec[k] - R.gamVecPrev[k]);
-        if (std::sqrt(s) <= EPS) break;
-      }
-    }
-    if (sw.rotorForcePlot != 0 && iter % sw.rotorForcePlot == 0) {
-      computeForces();
-      force2file();
-    }
-    if (sw.wakeSuppress == 0 && R.nNwake > 0) wakeUpdate();
   }
 
   void addInitWakeVel(Blade& b, bool pred) {
@@ -2174,6 +2190,74 @@ int or_dir_lift_drag(void* h) { return guarded([&]() { static_cast<Sim*>(h)->rot
 int or_calc_sec_alpha(void* h) { return guarded([&]() { static_cast<Sim*>(h)->rotor_calc_secAlpha(); }); }
 int or_calc_force(void* h) { return guarded([&]() { static_cast<Sim*>(h)->rotor_calc_force(); }); }
 
+// Kinematics-only advance to iteration k (see Sim::skipTo).
+int or_sim_skip_to(void* h, int k) { return guarded([&]() { static_cast<Sim*>(h)->skipTo(k); }); }
+
+// Sets a named flow-state array (the layouts of or_get; n values).  With
+// or_sim_skip_to this restores a state taken from elsewhere at iteration k:
+//   gam, gamPrev (blade)              [ic + nc*is]  wing circulation, previous trapezoidal circulation
+//   gamVec                            n
+//   waN (blade)                       [i + NW*j][filament][fc1, fc2]
+//   waN_gam, waN_age (blade)          [i + NW*j] (the age goes to all four filaments)
+//   waN_rvc (blade)                   [i + NW*j][filament]
+//   waF (blade)                       [i][fc1, fc2]
+//   waF_gam, waF_rvc, waF_rvc0, waF_l0, waF_lc, waF_age (blade)   [i]
+//   velN, velN1, velN2, velN3 (blade) [i + NW*j][xyz] (j to ns)
+//   velF, velF1, velF2, velF3 (blade) [i][xyz]
+int or_set(void* h, const char* name, int ib, const double* in, long n) {
+  return guarded([&]() {
+    Sim* s = static_cast<Sim*>(h);
+    Rotor& r = s->R;
+    const std::string k = name;
+    auto need = [&](size_t m) {
+      if ((size_t)n != m) throw std::runtime_error("or_set " + k + ": expected " + std::to_string(m) + " values");
+    };
+    auto v3 = [&](size_t i) { return mk(in[3 * i], in[3 * i + 1], in[3 * i + 2]); };
+    if (k == "gamVec") {
+      need(r.gamVec.size());
+      for (size_t i = 0; i < r.gamVec.size(); ++i) r.gamVec[i] = in[i];
+      return;
+    }
+    if (ib < 1 || ib > (int)r.blade.size()) throw std::runtime_error("or_set: blade out of range");
+    Blade& b = r.blade[ib - 1];
+    auto vel = [&](std::vector<V3>& a) { need(3 * a.size()); for (size_t i = 0; i < a.size(); ++i) a[i] = v3(i); };
+    if (k == "gam") { need(b.wiP.size()); for (size_t i = 0; i < b.wiP.size(); ++i) b.wiP[i].vr.gam = in[i]; }
+    else if (k == "gamPrev") { need(b.wiP.size()); for (size_t i = 0; i < b.wiP.size(); ++i) b.wiP[i].gamPrev = in[i]; }
+    else if (k == "waN") {
+      need(b.waN.size() * 24);
+      for (size_t i = 0; i < b.waN.size(); ++i)
+        for (int f = 0; f < 4; ++f) {
+          b.waN[i].vf[f].fc1 = v3(8 * i + 2 * f);
+          b.waN[i].vf[f].fc2 = v3(8 * i + 2 * f + 1);
+        }
+    } else if (k == "waN_gam") { need(b.waN.size()); for (size_t i = 0; i < b.waN.size(); ++i) b.waN[i].gam = in[i]; }
+    else if (k == "waN_age") {
+      need(b.waN.size());
+      for (size_t i = 0; i < b.waN.size(); ++i) for (int f = 0; f < 4; ++f) b.waN[i].vf[f].age = in[i];
+    } else if (k == "waN_rvc") {
+      need(b.waN.size() * 4);
+      for (size_t i = 0; i < b.waN.size(); ++i) for (int f = 0; f < 4; ++f) b.waN[i].vf[f].rVc = in[4 * i + f];
+    } else if (k == "waF") {
+      need(b.waF.size() * 6);
+      for (size_t i = 0; i < b.waF.size(); ++i) { b.waF[i].vf.fc1 = v3(2 * i); b.waF[i].vf.fc2 = v3(2 * i + 1); }
+    } else if (k == "waF_gam") { need(b.waF.size()); for (size_t i = 0; i < b.waF.size(); ++i) b.waF[i].gam = in[i]; }
+    else if (k == "waF_rvc") { need(b.waF.size()); for (size_t i = 0; i < b.waF.size(); ++i) b.waF[i].vf.rVc = in[i]; }
+    else if (k == "waF_rvc0") { need(b.waF.size()); for (size_t i = 0; i < b.waF.size(); ++i) b.waF[i].vf.rVc0 = in[i]; }
+    else if (k == "waF_l0") { need(b.waF.size()); for (size_t i = 0; i < b.waF.size(); ++i) b.waF[i].vf.l0 = in[i]; }
+    else if (k == "waF_lc") { need(b.waF.size()); for (size_t i = 0; i < b.waF.size(); ++i) b.waF[i].vf.lc = in[i]; }
+    else if (k == "waF_age") { need(b.waF.size()); for (size_t i = 0; i < b.waF.size(); ++i) b.waF[i].vf.age = in[i]; }
+    else if (k == "velN") vel(b.velN);
+    else if (k == "velN1") vel(b.velN1);
+    else if (k == "velN2") vel(b.velN2);
+    else if (k == "velN3") vel(b.velN3);
+    else if (k == "velF") vel(b.velF);
+    else if (k == "velF1") vel(b.velF1);
+    else if (k == "velF2") vel(b.velF2);
+    else if (k == "velF3") vel(b.velF3);
+    else throw std::runtime_error("or_set: unknown array " + k);
+  });
+}
+
 // Integer state: name in {nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter, nbConvect, ctRows}
 long or_geti(void* h, const char* name) {
   Sim* s = static_cast<Sim*>(h);
@@ -2279,6 +2363,18 @@ long or_get(void* h, const char* name, int ib, double* out, long cap) {
     else if (k == "waF_rvc") { for (auto& f : b->waF) v.push_back(f.vf.rVc); }
     else if (k == "velN") { for (auto& a : b->velN) push3(a); }
     else if (k == "velF") { for (auto& a : b->velF) push3(a); }
+    else if (k == "velN1") { for (auto& a : b->velN1) push3(a); }
+    else if (k == "velN2") { for (auto& a : b->velN2) push3(a); }
+    else if (k == "velN3") { for (auto& a : b->velN3) push3(a); }
+    else if (k == "velF1") { for (auto& a : b->velF1) push3(a); }
+    else if (k == "velF2") { for (auto& a : b->velF2) push3(a); }
+    else if (k == "velF3") { for (auto& a : b->velF3) push3(a); }
+    else if (k == "gamPrev") { for (auto& p : b->wiP) v.push_back(p.gamPrev); }
+    else if (k == "waN_age") { for (auto& w : b->waN) v.push_back(w.vf[0].age); }
+    else if (k == "waF_rvc0") { for (auto& f : b->waF) v.push_back(f.vf.rVc0); }
+    else if (k == "waF_l0") { for (auto& f : b->waF) v.push_back(f.vf.l0); }
+    else if (k == "waF_lc") { for (auto& f : b->waF) v.push_back(f.vf.lc); }
+    else if (k == "waF_age") { for (auto& f : b->waF) v.push_back(f.vf.age); }
     else return -1;
   } else return -1;
   long nOut = (long)v.size();

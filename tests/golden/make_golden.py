@@ -1,8 +1,8 @@
 """Copy the reference's own full-case fixtures into tests/golden/.
 
-Run once in a container where the reference checkout exists:
+Run once where a checkout of the reference exists, giving its root:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 
 It copies, unchanged, the inputs (config.nml, geom01.nml, PLOT3D blade file)
 and the reference results (referenceResults/*.ref) of the reference's two
@@ -50,4 +50,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout>")
+    main(sys.argv[1])

@@ -181,6 +181,35 @@ def test_checkpoint_resume_is_bit_identical(prec, tmp_path):
         o.checkpoint_load(ck)
 
 
+def test_checkpoint_loads_across_precisions(tmp_path):
+    """The saved state is FP64 in every precision: an FP32 + near-field case
+    continues from an FP64 state (factoring the restored AIC in FP32 for its
+    refined solve) within the FP32 tolerance of the FP64 continuation, and an
+    FP64 case continues from the FP32 case's state exactly as a second FP64
+    case loaded from the same file."""
+    c = C.rotor_2blade_hover(nt=60, n_nwake=20, truncate_nt=30)
+    a = lib.Case(c.config, c.geom, precision=lib.PREC_FP64)
+    a.start()
+    a.step(30)
+    ck64 = tmp_path / "ck64.bin"
+    a.checkpoint_save(ck64)
+    r64 = a.step(10)[:, 1]
+    b = lib.Case(c.config, c.geom, precision=lib.PREC_FP32_NEAR64)
+    b.checkpoint_load(ck64)
+    assert b.geti("iter") == 30
+    r32 = b.step(10)[:, 1]
+    assert np.max(np.abs(r32 - r64) / np.abs(r64)) < 1e-4
+    assert 0.0 <= b.get("lu_residual")[0] < 1e-12
+    ck32 = tmp_path / "ck32.bin"
+    b.checkpoint_save(ck32)
+    x = lib.Case(c.config, c.geom, precision=lib.PREC_FP64)
+    x.checkpoint_load(ck32)
+    y = lib.Case(c.config, c.geom, precision=lib.PREC_FP64)
+    y.checkpoint_load(ck32)
+    assert x.geti("iter") == 40
+    assert np.array_equal(x.step(5), y.step(5))
+
+
 def _lattice_cases():
     h = C.rotor_2blade_hover(nt=48, n_nwake=24, truncate_nt=36)
     f = C.rotor_4blade_forward(nt=40, n_nwake=16, truncate_nt=30)

@@ -87,7 +87,7 @@ def test_options_struct_matches_header():
     fields = re.findall(r"\b(int|double)\s+(\w+)\s*;", body)
     mirror = [(("double" if t is ctypes.c_double else "int"), n) for n, t in lib.Options._fields_]
     assert fields == mirror
-    integ = (ROOT / "INTEGRATION.md").read_text()
+    integ = (ROOT / "include" / "vlm_gb300.f90").read_text()
     ftype = re.search(r"type, bind\(c\) :: vlm_options(.*?)end type", integ, flags=re.S).group(1)
     fnames = re.findall(r"::\s*(\w+)", ftype)
     assert fnames == [n for _, n in fields]
@@ -101,7 +101,7 @@ def test_fortran_interfaces_match_header():
     for name, params in re.findall(r"\b(vlm_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
         p = params.strip()
         arity[name] = 0 if p in ("", "void") else p.count(",") + 1
-    integ = (ROOT / "INTEGRATION.md").read_text().replace("&\n", " ")
+    integ = (ROOT / "include" / "vlm_gb300.f90").read_text().replace("&\n", " ")
     found = re.findall(r"(?:function|subroutine)\s+\w+\(([^)]*)\)\s*bind\(c,\s*name='(vlm_\w+)'\)", integ)
     assert len(found) >= 10
     for args, name in found:

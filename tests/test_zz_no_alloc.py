@@ -61,6 +61,14 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls(precision):
         np.testing.assert_allclose(got, ref, rtol=0, atol=TOL[precision] * scale)
 
 
+@pytest.mark.parametrize("precision", [lib.PREC_FP64, lib.PREC_FP32_NEAR64])
+def test_noalloc_without_rings_writes_zeros(precision):
+    rng = np.random.default_rng(7)
+    P = rng.uniform(0, 1, size=(300, 3))
+    got = call_noalloc(np.zeros((0, 4, 3)), np.zeros((0, 4)), np.zeros(0), P, precision)
+    assert np.array_equal(got, np.zeros_like(P))
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     L = lib.load()
     rc = L.vlm_biot_savart_rings_noalloc(None, None, None, 16385, None, 10, None, lib.PREC_FP64, None)

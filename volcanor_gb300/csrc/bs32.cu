@@ -375,16 +375,24 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   if (warp == kConsumerWarps) {
     // ---- producer ----
     if (lane == 0) {
+      int issued = 0;
       for (int t = 0; t < ntiles; ++t) {
         const int s = t % kStages;
-        if (t >= kStages && !mbar_wait(&empty[s], ((t / kStages) - 1) & 1)) atomicExch(ctl, 1);
+        // a stage the consumers have not released may still be read: after an
+        // expired wait no further copy is issued (the consumers' own bounded
+        // waits for the missing tiles expire and they stop)
+        if (t >= kStages && !mbar_wait(&empty[s], ((t / kStages) - 1) & 1)) {
+          atomicExch(ctl, 1);
+          break;
+        }
         const int n = min(kTileW, ch.rec_count - t * kTileW);
         const uint32_t bytes = (uint32_t)n * kRec32 * 4u;
         mbar_expect_tx(&full[s], bytes);
         bulk_g2s(stage + s * kTileW * kRec32, rec32 + (size_t)(ch.rec_begin + t * kTileW) * kRec32, bytes, &full[s]);
+        issued = t + 1;
       }
       // the block must not retire with a copy still writing its shared memory
-      for (int t = max(0, ntiles - kStages); t < ntiles; ++t)
+      for (int t = max(0, issued - kStages); t < issued; ++t)
         if (!mbar_wait(&full[t % kStages], (t / kStages) & 1)) atomicExch(ctl, 2);
     }
     return;
@@ -413,8 +421,9 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   bool ok = true;
   for (int t = 0; t < ntiles; ++t) {
     const int s = t % kStages;
-    // the warp goes on only if every lane saw the stage arrive
-    if (!__all_sync(kFull, mbar_wait(&full[s], (t / kStages) & 1))) {
+    // the warp goes on only if every lane saw the stage arrive; after one
+    // expired wait it waits no more (ok is uniform across the warp)
+    if (ok && !__all_sync(kFull, mbar_wait(&full[s], (t / kStages) & 1))) {
       ok = false;
       if (lane == 0) atomicExch(ctl, 1);
     }
@@ -689,12 +698,13 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   if (near) {
     if (ew) k_partial32<true, true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
     else k_partial32<true, false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    const int sms = device_sm_count();
     count_launch();
-    k_near64<<<4 * 152, 128, 0, s>>>(near, ctl, near_cap, rec64, ew, P, M,
+    k_near64<<<4 * sms, 128, 0, s>>>(near, ctl, near_cap, rec64, ew, P, M,
                                      reinterpret_cast<unsigned long long*>(nacc));
     const size_t n = (size_t)M * nchunks * 3;
     count_launch();
-    k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, 8 * 152), 256, 0, s>>>(part, nacc, n);
+    k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * sms), 256, 0, s>>>(part, nacc, n);
   } else if (ew) {
     k_partial32<false, true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
   } else {
@@ -702,17 +712,33 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   }
 }
 
+// A host without a usable device still plans (sizes are queried before any
+// launch): it plans for a GB300's 152 SMs.
+constexpr int kPlanSmsWithoutDevice = 152;
+
+int device_sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kPlanSmsWithoutDevice;
+  if (!cache[dev]) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      return kPlanSmsWithoutDevice;
+    cache[dev] = sms;
+  }
+  return cache[dev];
+}
+
 int partial32_slots() {
   static std::atomic<int> cache[64];
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 2 * 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 2 * kPlanSmsWithoutDevice;
   if (!cache[dev]) {
-    int sms = 0, per = 0;
+    int per = 0;
     const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
     cudaFuncSetAttribute(k_partial32<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true, false>, kBlockW, smem);
-    cache[dev] = std::max(1, sms) * std::max(1, per);
+    cache[dev] = device_sm_count() * std::max(1, per);
   }
   return cache[dev];
 }

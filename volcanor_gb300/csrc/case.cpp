@@ -912,7 +912,9 @@ struct Case {
   // ---- checkpoint / resume (the reference's Restart/restartNNNNN.dat:
   // src/main.f90:389-397 reads t and the rotor object, :1443-1450 writes
   // them every restartWriteNt steps) -------------------------------------------
-  std::vector<std::pair<void*, size_t>> stateArrays() {
+  // the solver state (all FP64) and, last, the FP32 factors of the refined
+  // solve (present when `refined`)
+  std::vector<std::pair<void*, size_t>> stateArrays(bool refined) {
     const size_t nb = d.nb, npan = d.npan, n = d.n, ns = d.ns;
     const size_t nring = nb * std::max(d.NW, 1) * ns, nfar = nb * std::max(d.NF, 1), nsec = nb * ns;
     const size_t D = sizeof(double);
@@ -934,7 +936,7 @@ struct Case {
       v.push_back({s.vN[k], nb * std::max(d.NW, 1) * (ns + 1) * 3 * D});
       v.push_back({s.vF[k], nfar * 3 * D});
     }
-    if (refine) {
+    if (refined) {
       v.push_back({s.LU32, n * n * sizeof(float)});
       v.push_back({s.AICinv32, n * n * sizeof(float)});
       v.push_back({s.piv32, n * sizeof(int)});
@@ -960,7 +962,7 @@ struct Case {
     f.write(reinterpret_cast<const char*>(&nh), sizeof(nh));
     f.write(reinterpret_cast<const char*>(h.data()), sizeof(int64_t) * h.size());
     std::vector<char> buf;
-    for (auto& a : stateArrays()) {
+    for (auto& a : stateArrays(refine)) {
       buf.resize(a.second);
       VLM_CUDA(cudaMemcpy(buf.data(), a.first, a.second, cudaMemcpyDeviceToHost));
       const int64_t nb = (int64_t)a.second;
@@ -982,20 +984,37 @@ struct Case {
     std::vector<int64_t> h((size_t)nh);
     f.read(reinterpret_cast<char*>(h.data()), sizeof(int64_t) * nh);
     if (!f || h[0] != (int64_t)kCkptMagic) throw StatusError(VLM_ERR_INVALID, "not a checkpoint: " + path);
-    for (size_t i = 2; i < h.size(); ++i)
-      if (h[i] != mine[i])
-        throw StatusError(VLM_ERR_INVALID, "checkpoint of a different case or options: " + path);
+    // the case's dimensions must agree; the arithmetic options (precision,
+    // summation blocks, solve mode) may differ: the state is FP64 in every
+    // precision, so a state saved by one precision continues in another
+    for (size_t i = 2; i <= 7; ++i)
+      if (h[i] != mine[i]) throw StatusError(VLM_ERR_INVALID, "checkpoint of a different case: " + path);
     if (h[1] < 0 || h[1] > W.nt) throw StatusError(VLM_ERR_INVALID, "checkpoint step out of range");
+    const bool fileRefined = h[10] != 0;
     VLM_CUDA(cudaStreamSynchronize(stream));
     std::vector<char> buf;
-    for (auto& a : stateArrays()) {
+    // (the FP32 factors of a case that does not refine are not allocated:
+    // only their sizes are used, to read past them)
+    const auto arrays = stateArrays(true);
+    const size_t common = stateArrays(false).size();
+    const size_t nread = fileRefined ? arrays.size() : common;
+    for (size_t i = 0; i < nread; ++i) {
+      const auto& a = arrays[i];
       int64_t nb = 0;
       f.read(reinterpret_cast<char*>(&nb), sizeof(nb));
       if (!f || nb != (int64_t)a.second) throw StatusError(VLM_ERR_INVALID, "checkpoint arrays do not match: " + path);
       buf.resize(a.second);
       f.read(buf.data(), (std::streamsize)buf.size());
       if (!f) throw StatusError(VLM_ERR_IO, "truncated checkpoint: " + path);
-      VLM_CUDA(cudaMemcpy(a.first, buf.data(), a.second, cudaMemcpyHostToDevice));
+      // the FP32 factors only matter to a case that refines
+      if (i < common || refine) VLM_CUDA(cudaMemcpy(a.first, buf.data(), a.second, cudaMemcpyHostToDevice));
+    }
+    // a refining case restored from a state without FP32 factors factors the
+    // restored AIC itself (the same FP32 LU its start would have made)
+    if (refine && !fileRefined) {
+      launch_lu32(d, s, stream);
+      VLM_CUDA(cudaGetLastError());
+      VLM_CUDA(cudaStreamSynchronize(stream));
     }
     // the frame of the restored step (later steps upload their own)
     iter = (int)h[1];
@@ -1161,6 +1180,10 @@ struct Case {
     else if (bok && k == "vr_rvc") v = dget(s.wRvc + 4 * b * npan, 4 * npan);
     else if (bok && k == "velN") v = dget(s.vN[0] + 3 * b * NW * (ns + 1), 3 * NW * (ns + 1));
     else if (bok && k == "velF") v = dget(s.vF[0] + 3 * b * NF, 3 * NF);
+    else if (bok && (k == "velN1" || k == "velN2" || k == "velN3"))
+      v = dget(s.vN[k[4] - '0'] + 3 * b * NW * (ns + 1), 3 * NW * (ns + 1));
+    else if (bok && (k == "velF1" || k == "velF2" || k == "velF3")) v = dget(s.vF[k[4] - '0'] + 3 * b * NF, 3 * NF);
+    else if (bok && k == "gamPrev") v = dget(s.gamPrev + b * npan, npan);
     else if (bok && k == "secCL") v = dget(s.secCL + b * ns, ns);
     else if (bok && k == "secLiftDir") v = dget(s.secLiftDir + 3 * b * ns, 3 * ns);
     else if (bok && k == "secChordwiseResVel") v = dget(s.secResVel + 3 * b * ns, 3 * ns);
@@ -1289,7 +1312,7 @@ static void grow(void** p, size_t& cap, size_t need) {
 static int ring_chunk(int64_t N, int64_t M, int precision) {
   // enough (target block x chunk) work items to fill the GPU several times
   const int64_t blocks = precision == VLM_PREC_FP64 ? (M + 127) / 128 : (M + 255) / 256;
-  const int64_t want = 4 * 152;
+  const int64_t want = 4 * (int64_t)device_sm_count();
   int64_t q = std::max<int64_t>(1, (want + blocks - 1) / blocks);
   q = std::min<int64_t>(q, std::max<int64_t>(1, N / 64));
   return (int)((N + q - 1) / q);

@@ -37,8 +37,8 @@ constexpr size_t kOffTables = kOffNacc + align256(kMaxPoints * 3 * sizeof(long l
 constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words
 
 // One fixed scratch area per device that loads the library, held until exit.
-// It starts zeroed; the near-field accumulators in it are left zero by every
-// call.
+// Every FP32 + FP64-near call clears the near-field accumulators it uses
+// before its launch, so a call that failed half-way leaves nothing behind.
 // In host code this name is only a stand-in for the device object: kernels
 // get its device address from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -128,6 +128,10 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
       launch_partial64(rec64, chunks, 1, P, (int)M, part, st);
     } else {
       const bool nearOn = precision == VLM_PREC_FP32_NEAR64;
+      if (nearOn) {
+        e = cudaMemsetAsync(nacc, 0, (size_t)M * 3 * sizeof(long long), st);
+        if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+      }
       launch_pack32(rec64, (int)N, nearOn ? 4.0 : 0.0, rec32, st);
       launch_partial32(rec32, rec64, chunks, 1, P, (int)M, part, ctl, nearOn ? near : nullptr, (int)kMaxNear, nacc, st);
     }

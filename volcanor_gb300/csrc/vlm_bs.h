@@ -105,6 +105,8 @@ int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, i
 // Resident block slots of the FP32 kernel on the current device
 // (SMs x resident blocks per SM).
 int partial32_slots();
+// Streaming multiprocessors of the current device (cached per device).
+int device_sm_count();
 
 
 // FP64 reference-arithmetic partial sums: part[(q * M + m) * 3 + k].

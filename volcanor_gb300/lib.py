@@ -65,6 +65,7 @@ SIGNATURES = {
     "vlm_kernel_launch_count": (_i64, []),
     "vlm_device_info": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                        ctypes.POINTER(ctypes.c_int)]),
+    "vlm_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "vlm_biot_savart_rings": (ctypes.c_int, [_dp, _dp, _dp, _i64, _dp, _i64, _dp, ctypes.c_int]),
     "vlm_biot_savart_rings_device": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _vp, ctypes.c_int, _vp]),
     "vlm_biot_savart_rings_scratch_bytes": (_i64, [_i64, _i64, ctypes.c_int]),
@@ -178,6 +179,13 @@ def device_info(device: int = 0):
     sm, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     _err(load().vlm_device_info(device, ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)))
     return sm.value, ma.value, mi.value
+
+
+def measure_fp32_peak(device: int = 0, reps: int = 20):
+    """(TFLOP/s, ms per launch) of the library's FP32 FMA-chain kernel on all SMs."""
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    _err(load().vlm_measure_fp32_peak(device, reps, ctypes.byref(tf), ctypes.byref(ms)))
+    return tf.value, ms.value
 
 
 def params_json(config_text: str, geom_text: str, base_dir: str | os.PathLike = "") -> str:
