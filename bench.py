@@ -278,7 +278,7 @@ def run_ours(args):
     case.checkpoint_save(ck)
     if dist:
         dist.barrier()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk, nvtx_range("timed_steps"):
         l0 = lib.launch_count()
         t0 = time.perf_counter()
         rows = case.step(K)

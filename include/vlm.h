@@ -121,11 +121,11 @@ int vlm_biot_savart_filaments_device(const double* fc, const double* rvc, const 
  * device memory when they call it (a host solver that reserves its device
  * memory once at start-up, a process under a hard device-memory cap, or a
  * caller that must not trigger the device-wide synchronisation an allocation
- * may cause): its scratch is one fixed 9.25 MiB array compiled into the library,
+ * may cause): its scratch is one fixed 9.5 MiB array compiled into the library,
  * held on every device that loads the library until the process exits.
- * Limits: N <= 16384 rings, M <= 65536 points, at most 65536 near-field
- * pairs (VLM_PREC_FP32_NEAR64); larger sizes return VLM_ERR_INVALID with a
- * message.  The rings are summed in one block, i.e. in the reference's order.
+ * Limits: N <= 16384 rings, M <= 65536 points; larger sizes return
+ * VLM_ERR_INVALID with a message.  The rings are summed in one block, i.e.
+ * in the reference's order.
  * The first call on a device looks up the scratch array's device address
  * and keeps it for the life of the process, so make that first call before
  * any CUDA stream capture, and do not reset the device (cudaDeviceReset)
@@ -155,6 +155,43 @@ int vlm_case_start(vlm_case* c);
  * receives nsteps x 10 rows (iter, CL/CT, CD/CQ, CLu, CDi, CD0, CDu, CFx, CFy,
  * CFz) -- the rXXForceNonDim.csv columns (src/libPostprocess.f90:814-838). */
 int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows);
+/* ---- the time step as separate calls ---------------------------------------
+ * For a host that keeps its own time loop and replaces the reference's
+ * procedures one by one.  vlm_case_aic_factor replaces rotor%calcAIC + inv2
+ * + isInverse at start-up (src/main.f90:62-81; vlm_case_start calls it when
+ * the host has not).  One iteration k = iter + 1 is then
+ *   vlm_case_solve_circulation  -- the RHS loop + matmulAX + map_gam
+ *       (src/main.f90:466-603: leading-edge shedding, wake ageing and
+ *       dissipation, wake-induced velocity at the collocation points, RHS,
+ *       gamVec); kinematic_vel (3 x n, the RHS rows' order ic + nc(is-1) +
+ *       nc ns(ib-1); NULL = the library's own prescribed kinematics) is the
+ *       kinematic part of velCP the reference computes at main.f90:522-560;
+ *       gam_out (n, or NULL) receives gamVec;
+ *   vlm_case_loads (optional)   -- calc_force + the CT row of force2file
+ *       (src/main.f90:623-764); ct_row (10, or NULL) receives the
+ *       rXXForceNonDim.csv row.  The reference computes loads only on
+ *       iterations that are multiples of rotorForcePlot, and so does
+ *       vlm_case_step; the loads carry the unsteady term's previous
+ *       circulation from one call to the next;
+ *   vlm_case_wake_step          -- wake-node velocities, the FD scheme,
+ *       strain, roll-up / truncation, trailing-edge shedding
+ *       (src/main.f90:799-1439); the case is then at iteration k.
+ * Between vlm_case_loads and vlm_case_wake_step the case holds the state the
+ * reference writes its per-step files from (filaments2file, probes2file,
+ * src/main.f90:788,795): vlm_case_get / vlm_case_get_wake /
+ * vlm_case_vind_points read it there.  The three calls in sequence produce
+ * the same bits as vlm_case_step(c, 1, row) (loads called on the iterations
+ * vlm_case_step computes them). */
+int vlm_case_aic_factor(vlm_case* c);
+int vlm_case_solve_circulation(vlm_case* c, const double* kinematic_vel, double* gam_out);
+int vlm_case_loads(vlm_case* c, double* ct_row);
+int vlm_case_wake_step(vlm_case* c);
+/* The wake of blade (1-based) as the reference stores it (waN, waF of
+ * blade_class): near-wake ring corners (3, 4, nNwake, ns), their
+ * circulations (nNwake, ns), far-wake filament nodes (3, 2, nFwake), their
+ * circulations (nFwake).  Any pointer may be NULL. */
+int vlm_case_get_wake(vlm_case* c, int blade, double* waN, double* waN_gam, double* waF, double* waF_gam);
+
 /* Integer state: nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter,
  * nbConvect, wakeTruncateNt, rotorForcePlot; nearPairs (near-field filament-target pairs of the
  * last FP32 evaluation) and nodeChunks (chunks of the next step's wake-node
@@ -180,6 +217,8 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *   velN, velF (blade)              (3, nNwake, ns+1), (3, nFwake) node velocities
  *   velN1..velN3, velF1..velF3 (blade)  the same shapes: the velocity history of the
  *                                   multi-step schemes (velNwake1..3, velFwake1..3)
+ *   velKin (blade)                  (3, nc, ns) the kinematic velocity at the collocation points
+ *                                   of the current iteration (during an open step, of that step)
  *   gamPrev (blade)                 (nc, ns) the previous step's trapezoidal circulation
  *                                   (the unsteady term of the loads)
  *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section

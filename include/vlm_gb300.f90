@@ -108,6 +108,47 @@ module vlm_gb300
       real(c_double), intent(out) :: V(3, *)
       integer(c_int), value :: prec
     end function
+    ! the time step as separate calls (include/vlm.h): a host that keeps its
+    ! own loop replaces calcAIC + inv2, the RHS loop + matmulAX + map_gam,
+    ! calc_force, and the wake update one by one
+    integer(c_int) function vlm_case_aic_factor(cs) bind(c, name='vlm_case_aic_factor')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: cs
+    end function
+    integer(c_int) function vlm_case_solve_circulation(cs, kinematic_vel, gam_out) &
+        bind(c, name='vlm_case_solve_circulation')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: cs
+      ! absent optional arguments pass NULL (Fortran 2018 interoperability)
+      real(c_double), intent(in), optional :: kinematic_vel(3, *)
+      real(c_double), intent(out), optional :: gam_out(*)
+    end function
+    integer(c_int) function vlm_case_loads(cs, ct_row) bind(c, name='vlm_case_loads')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: cs
+      real(c_double), intent(out), optional :: ct_row(10)
+    end function
+    integer(c_int) function vlm_case_wake_step(cs) bind(c, name='vlm_case_wake_step')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: cs
+    end function
+    integer(c_int) function vlm_case_get_wake(cs, blade, waN, waN_gam, waF, waF_gam) &
+        bind(c, name='vlm_case_get_wake')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: cs
+      integer(c_int), value :: blade
+      real(c_double), intent(out) :: waN(3, 4, *), waN_gam(*), waF(3, 2, *), waF_gam(*)
+    end function
+    integer(c_int) function vlm_case_checkpoint_save(cs, path) bind(c, name='vlm_case_checkpoint_save')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: cs
+      character(kind=c_char), intent(in) :: path(*)
+    end function
+    integer(c_int) function vlm_case_checkpoint_load(cs, path) bind(c, name='vlm_case_checkpoint_load')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: cs
+      character(kind=c_char), intent(in) :: path(*)
+    end function
   end interface
 
 contains

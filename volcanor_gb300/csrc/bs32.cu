@@ -20,15 +20,18 @@
 // zero; the reference's eps^2 cut-off needs no separate test.  FP32 partial sums are promoted to
 // the FP64 accumulator after every tile.
 //
-// Near field: one compare per target and ring (distance to the record's
-// centre against its reach) and a warp vote select the records some lane of
-// the warp may be near; for those the warp evaluates the record with a per-
-// filament near-zone test that leaves near filaments out of the FP32 sum and
-// appends one (target, record, filament) entry per near filament to a list
-// (staged per warp in shared memory).  k_near64 evaluates the list
-// coherently in FP64 into order-independent fixed-point accumulators, and
-// k_near_apply adds them to the chunk partial sums, so the result does not
-// depend on the order of the list.
+// Near field (VLM_PREC_FP32_NEAR64): the FP32 kernel sums every pair; the
+// pairs within near_factor core radii of a filament segment -- where the
+// FP32 cross product and Vatistas denominator lose digits -- are then
+// corrected to FP64 outside the hot loop.  A hash grid over the records'
+// near-zone bounding boxes (cell size = the largest box, so a box covers at
+// most 2 x 2 x 2 cells) gives each target the few records whose zones can
+// contain it; for every near filament of those, k_near_fix recomputes the
+// FP32 kernel's own contribution bit for bit (same inline arithmetic, same
+// FP32 inputs) and adds FP64 value - FP32 contribution to order-independent
+// fixed-point accumulators, which k_near_apply folds into the chunk partial
+// sums.  The result equals summing the far pairs in FP32 and the near pairs
+// in FP64, up to the FP32 rounding of the tile sums that held the near terms.
 #include <stdint.h>
 
 #include <algorithm>
@@ -82,75 +85,6 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// Near-list entries are staged per warp in shared memory and written to the
-// global list in batches, one atomic per batch (a single global counter
-// shared by every warp would otherwise put its latency on every append).
-constexpr int kNearStage = 128;  // entries staged per warp
-
-// Writes the warp's staged entries to the global list.
-__device__ __forceinline__ void near_flush(NearPair* __restrict__ stage, int& staged, int lane, int* __restrict__ ctl,
-                                           NearPair* __restrict__ near, int near_cap) {
-  if (staged == 0) return;
-  int base = 0;
-  if (lane == 0) base = atomicAdd(ctl + 1, staged);
-  base = __shfl_sync(kFull, base, 0);
-  __syncwarp();
-  for (int i = lane; i < staged; i += 32) {
-    if (base + i < near_cap) near[base + i] = stage[i];
-    else atomicExch(ctl, 3);
-  }
-  __syncwarp();
-  staged = 0;
-}
-
-// Appends one entry per near filament (bits of msk, at most 4) of this
-// warp's lanes.  Slots come from one ballot per filament index, no shuffles:
-// filament k of lane l goes to P_k + popc(ballot_k & lanes below l), P_k the
-// entries of the filament indices below k.
-__device__ __forceinline__ void near_append(unsigned msk, int m, int q, int rec, int lane, int* __restrict__ ctl,
-                                            NearPair* __restrict__ near, int near_cap, NearPair* __restrict__ stage,
-                                            int& staged) {
-  if (!__ballot_sync(kFull, msk != 0u)) return;
-  const unsigned lt = (1u << lane) - 1u;
-  unsigned bk[4];
-  int pk[4], total = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    bk[k] = __ballot_sync(kFull, (msk >> k) & 1u);
-    pk[k] = total;
-    total += __popc(bk[k]);
-  }
-  int base;
-  NearPair* dst;
-  if (total <= kNearStage) {
-    if (staged + total > kNearStage) near_flush(stage, staged, lane, ctl, near, near_cap);
-    base = staged;
-    dst = stage;
-  } else {
-    // more than a stage holds (up to 32 lanes x 4 filaments): straight out
-    int b0 = 0;
-    if (lane == 0) b0 = atomicAdd(ctl + 1, total);
-    base = __shfl_sync(kFull, b0, 0);
-    dst = nullptr;
-  }
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if ((msk >> k) & 1u) {
-      const int slot = base + pk[k] + __popc(bk[k] & lt);
-      NearPair np;
-      np.m = m;
-      np.q = q;
-      np.rec = rec;
-      np.k = k;
-      if (dst) dst[slot] = np;
-      else if (slot < near_cap) near[slot] = np;
-      else atomicExch(ctl, 3);
-    }
-  }
-  __syncwarp();
-  if (dst) staged += total;
-}
-
 // Corner vector r = P - c and 1/|r| (|r|^2 + 1e-30: a target on a corner
 // gets a finite 1/|r|, times r = 0).
 __device__ __forceinline__ void corner_vector(float px, float py, float pz, float cx, float cy, float cz, float& rx,
@@ -175,37 +109,36 @@ __device__ __forceinline__ void load_view(const float4* __restrict__ R4, RecView
   v.a4v[0] = a4.x, v.a4v[1] = a4.y, v.a4v[2] = a4.z, v.a4v[3] = a4.w;
 }
 
-// Adds the FP32 velocity of filament K (c_K -> c_{K+1}) at one target, from
-// the corner vectors (r, 1/|r|) of its two ends.  CHECK: also tests the
-// filament against its near zone (record fields [32+K], [36+K], [40+K]); a
-// near filament is left out and reported through the return value.
-template <int K, bool CHECK>
-__device__ __forceinline__ bool fil_fp32(const float4* __restrict__ R4, const RecView& v, float rxk, float ryk,
-                                         float rzk, float invk, float rxj, float ryj, float rzj, float invj, float& ax,
-                                         float& ay, float& az, bool mine) {
-  const float kx = fmaf(ryk, rzj, -rzk * ryj);
-  const float ky = fmaf(rzk, rxj, -rxk * rzj);
-  const float kz = fmaf(rxk, ryj, -ryk * rxj);
-  const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
+// FP32 velocity of filament K (c_K -> c_{K+1}) at one target, from the
+// corner vectors (r, 1/|r|) of its two ends: the factor f and the cross
+// product r_K x r_{K+1}; the contribution is f (kx, ky, kz).  The near-field
+// correction recomputes exactly this (k_near_fix), so keep every operation
+// explicit (no expression the compiler could contract differently).
+struct Fil32 {
+  float f, kx, ky, kz, c2, tt;
+};
+__device__ __forceinline__ Fil32 fil_terms(float ex, float ey, float ez, float eev, float a4, float rxk, float ryk,
+                                           float rzk, float invk, float rxj, float ryj, float rzj, float invj) {
+  Fil32 o;
+  o.kx = fmaf(ryk, rzj, -rzk * ryj);
+  o.ky = fmaf(rzk, rxj, -rxk * rzj);
+  o.kz = fmaf(rxk, ryj, -ryk * rxj);
+  o.c2 = fmaf(o.kx, o.kx, fmaf(o.ky, o.ky, o.kz * o.kz));
   // w (e.r_k/|r_k| - e.r_j/|r_j|) with the weight folded into e
-  const float tt = fmaf(v.ex[K], rxk, fmaf(v.ey[K], ryk, v.ez[K] * rzk));
-  const float d = fmaf(tt, invk, -(tt - v.eev[K]) * invj);
-  float f = d * rsqrtf(fmaf(c2, c2, v.a4v[K]));
-  bool nr = false;
-  if (CHECK) {
-    const float thr = reinterpret_cast<const float*>(R4)[32 + K];
-    const float lo = reinterpret_cast<const float*>(R4)[36 + K];
-    const float hi = reinterpret_cast<const float*>(R4)[40 + K];
-    // exact zeros (target on the filament line) stay in the FP32 sum; only
-    // a target inside the record's sphere can flag (so that which pairs are
-    // near does not depend on the other lanes of its warp)
-    nr = mine && c2 < thr && c2 > kS2Min && tt > lo && tt < hi;
-    f = nr ? 0.f : f;
-  }
-  ax = fmaf(f, kx, ax);
-  ay = fmaf(f, ky, ay);
-  az = fmaf(f, kz, az);
-  return nr;
+  o.tt = fmaf(ex, rxk, fmaf(ey, ryk, ez * rzk));
+  const float d = fmaf(o.tt, invk, -(o.tt - eev) * invj);
+  o.f = d * rsqrtf(fmaf(o.c2, o.c2, a4));
+  return o;
+}
+
+// Adds the FP32 velocity of filament K at one target.
+template <int K>
+__device__ __forceinline__ void fil_fp32(const RecView& v, float rxk, float ryk, float rzk, float invk, float rxj,
+                                         float ryj, float rzj, float invj, float& ax, float& ay, float& az) {
+  const Fil32 t = fil_terms(v.ex[K], v.ey[K], v.ez[K], v.eev[K], v.a4v[K], rxk, ryk, rzk, invk, rxj, ryj, rzj, invj);
+  ax = fmaf(t.f, t.kx, ax);
+  ay = fmaf(t.f, t.ky, ay);
+  az = fmaf(t.f, t.kz, az);
 }
 
 // A whole ring (all four edges active): the four corner vectors r_k = P - c_k
@@ -223,75 +156,21 @@ __device__ __forceinline__ void corner_vectors(float px, float py, float pz, con
 }
 
 // Adds the FP32 velocity of a whole ring at one target (corner vectors r_k
-// and rsqrt norms given).  CHECK: also tests every filament against its near
-// zone, leaves the near ones out and returns their bit mask.
-template <bool CHECK>
-__device__ __forceinline__ unsigned ring_fp32(const float4* __restrict__ R4, const float (&rx)[4], const float (&ry)[4],
-                                              const float (&rz)[4], const float (&inv)[4], float& ax, float& ay,
-                                              float& az, bool mine = false) {
-  const float4 q3 = R4[3], q4 = R4[4], q5 = R4[5];  // weighted edges
-  const float4 ee = R4[6], a4 = R4[7];
-  const float ex[4] = {q3.x, q3.w, q4.z, q5.y};
-  const float ey[4] = {q3.y, q4.x, q4.w, q5.z};
-  const float ez[4] = {q3.z, q4.y, q5.x, q5.w};
-  const float eev[4] = {ee.x, ee.y, ee.z, ee.w};
-  const float a4v[4] = {a4.x, a4.y, a4.z, a4.w};
-  float thr[4], lo[4], hi[4];
-  if (CHECK) {
-    const float4 t = R4[8], l = R4[9], h = R4[10];
-    thr[0] = t.x, thr[1] = t.y, thr[2] = t.z, thr[3] = t.w;
-    lo[0] = l.x, lo[1] = l.y, lo[2] = l.z, lo[3] = l.w;
-    hi[0] = h.x, hi[1] = h.y, hi[2] = h.z, hi[3] = h.w;
-  }
-  unsigned msk = 0u;
+// and rsqrt norms given).
+__device__ __forceinline__ void ring_fp32(const float4* __restrict__ R4, const float (&rx)[4], const float (&ry)[4],
+                                          const float (&rz)[4], const float (&inv)[4], float& ax, float& ay,
+                                          float& az) {
+  RecView v;
+  load_view(R4, v);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int j = (k + 1) & 3;
-    const float kx = fmaf(ry[k], rz[j], -rz[k] * ry[j]);
-    const float ky = fmaf(rz[k], rx[j], -rx[k] * rz[j]);
-    const float kz = fmaf(rx[k], ry[j], -ry[k] * rx[j]);
-    const float c2 = fmaf(kx, kx, fmaf(ky, ky, kz * kz));
-    // w (e.r_k/|r_k| - e.r_j/|r_j|) with the weight folded into e
-    const float tt = fmaf(ex[k], rx[k], fmaf(ey[k], ry[k], ez[k] * rz[k]));
-    const float d = fmaf(tt, inv[k], -(tt - eev[k]) * inv[j]);
-    float f = d * rsqrtf(fmaf(c2, c2, a4v[k]));
-    if (CHECK) {
-      // exact zeros (target on the filament line) stay in the FP32 sum
-      // only a target inside the record's sphere can flag (so that which
-      // pairs are near does not depend on the other lanes of its warp)
-      const bool nr = mine && c2 < thr[k] && c2 > kS2Min && tt > lo[k] && tt < hi[k];
-      f = nr ? 0.f : f;
-      msk |= nr ? (1u << k) : 0u;
-    }
-    ax = fmaf(f, kx, ax);
-    ay = fmaf(f, ky, ay);
-    az = fmaf(f, kz, az);
+    const Fil32 t = fil_terms(v.ex[k], v.ey[k], v.ez[k], v.eev[k], v.a4v[k], rx[k], ry[k], rz[k], inv[k], rx[j], ry[j],
+                              rz[j], inv[j]);
+    ax = fmaf(t.f, t.kx, ax);
+    ay = fmaf(t.f, t.ky, ay);
+    az = fmaf(t.f, t.kz, az);
   }
-  return msk;
-}
-
-// One lattice-form record at one target: corners c0..c2 and edges 0 and 1,
-// then c3 and the border edges 2 / 3 only where they carry circulation
-// (a whole ring takes all four).  CHECK: returns the mask of near filaments.
-template <bool CHECK>
-__device__ __forceinline__ unsigned rec_lat(const float4* __restrict__ R4, const RecView& v, const float (&cx)[4],
-                                            const float (&cy)[4], const float (&cz)[4], float px, float py, float pz,
-                                            float& ax, float& ay, float& az, bool mine = false) {
-  float rx[4], ry[4], rz[4], inv[4];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) corner_vector(px, py, pz, cx[k], cy[k], cz[k], rx[k], ry[k], rz[k], inv[k]);
-  unsigned msk = 0u;
-  if (fil_fp32<0, CHECK>(R4, v, rx[0], ry[0], rz[0], inv[0], rx[1], ry[1], rz[1], inv[1], ax, ay, az, mine)) msk |= 1u;
-  if (fil_fp32<1, CHECK>(R4, v, rx[1], ry[1], rz[1], inv[1], rx[2], ry[2], rz[2], inv[2], ax, ay, az, mine)) msk |= 2u;
-  const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
-  if (t2 || t3) {
-    corner_vector(px, py, pz, cx[3], cy[3], cz[3], rx[3], ry[3], rz[3], inv[3]);
-    if (t2 && fil_fp32<2, CHECK>(R4, v, rx[2], ry[2], rz[2], inv[2], rx[3], ry[3], rz[3], inv[3], ax, ay, az, mine))
-      msk |= 4u;
-    if (t3 && fil_fp32<3, CHECK>(R4, v, rx[3], ry[3], rz[3], inv[3], rx[0], ry[0], rz[0], inv[0], ax, ay, az, mine))
-      msk |= 8u;
-  }
-  return msk;
 }
 
 // Both targets of a thread, one lattice-form record, no near test: both
@@ -312,10 +191,10 @@ __device__ __forceinline__ void rec_lat_pair(const float4* __restrict__ R4, cons
       corner_vector(px[u], py[u], pz[u], cx[k], cy[k], cz[k], rx[u][k], ry[u][k], rz[u][k], inv[u][k]);
 #pragma unroll
   for (int u = 0; u < T; ++u) {
-    fil_fp32<0, false>(R4, v, rx[u][0], ry[u][0], rz[u][0], inv[u][0], rx[u][1], ry[u][1], rz[u][1], inv[u][1], ax[u],
-                       ay[u], az[u], false);
-    fil_fp32<1, false>(R4, v, rx[u][1], ry[u][1], rz[u][1], inv[u][1], rx[u][2], ry[u][2], rz[u][2], inv[u][2], ax[u],
-                       ay[u], az[u], false);
+    fil_fp32<0>(v, rx[u][0], ry[u][0], rz[u][0], inv[u][0], rx[u][1], ry[u][1], rz[u][1], inv[u][1], ax[u], ay[u],
+                az[u]);
+    fil_fp32<1>(v, rx[u][1], ry[u][1], rz[u][1], inv[u][1], rx[u][2], ry[u][2], rz[u][2], inv[u][2], ax[u], ay[u],
+                az[u]);
   }
   const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
   if (t2 || t3) {
@@ -325,14 +204,14 @@ __device__ __forceinline__ void rec_lat_pair(const float4* __restrict__ R4, cons
     if (t2) {
 #pragma unroll
       for (int u = 0; u < T; ++u)
-        fil_fp32<2, false>(R4, v, rx[u][2], ry[u][2], rz[u][2], inv[u][2], rx[u][3], ry[u][3], rz[u][3], inv[u][3],
-                           ax[u], ay[u], az[u], false);
+        fil_fp32<2>(v, rx[u][2], ry[u][2], rz[u][2], inv[u][2], rx[u][3], ry[u][3], rz[u][3], inv[u][3], ax[u],
+                    ay[u], az[u]);
     }
     if (t3) {
 #pragma unroll
       for (int u = 0; u < T; ++u)
-        fil_fp32<3, false>(R4, v, rx[u][3], ry[u][3], rz[u][3], inv[u][3], rx[u][0], ry[u][0], rz[u][0], inv[u][0],
-                           ax[u], ay[u], az[u], false);
+        fil_fp32<3>(v, rx[u][3], ry[u][3], rz[u][3], inv[u][3], rx[u][0], ry[u][0], rz[u][0], inv[u][0], ax[u],
+                    ay[u], az[u]);
     }
   }
 }
@@ -349,12 +228,11 @@ static_assert(kConsumerWarps * 32 * kTPT == kTargetsPerBlock32, "targets per blo
 
 // LAT: the records are in lattice form (edges 2 and 3 marked when they carry
 // no circulation); otherwise every record is evaluated as a whole ring.
-template <bool NEAR, bool LAT>
+template <bool LAT>
 __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restrict__ rec32,
                                                          const Chunk* __restrict__ chunks,
                                                          const double* __restrict__ P, int M,
-                                                         double* __restrict__ part, int* __restrict__ ctl,
-                                                         NearPair* __restrict__ near, int near_cap) {
+                                                         double* __restrict__ part, int* __restrict__ ctl) {
   extern __shared__ __align__(16) float stage[];  // [kStages][kTileW * kRec32]
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ __align__(8) uint64_t empty[kStages];
@@ -399,9 +277,6 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   }
 
   // ---- consumers ----
-  __shared__ NearPair nstage_all[NEAR ? kConsumerWarps * kNearStage : 1];
-  NearPair* nstage = nstage_all + (NEAR ? warp * kNearStage : 0);
-  int staged = 0;
   int mt[kTPT];
   bool valid[kTPT];
   float px[kTPT], py[kTPT], pz[kTPT];
@@ -440,58 +315,13 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
         const float cx[4] = {q0.x, q0.w, q1.z, q2.y};
         const float cy[4] = {q0.y, q1.x, q1.w, q2.z};
         const float cz[4] = {q0.z, q1.y, q2.x, q2.w};
-        if (NEAR) {
-          // candidate test first (distance to the record's centre against
-          // its reach), so that only one target's corner vectors are live in
-          // either path below
-          const float4 zone = R4[11];  // reach^2, centre of the near zones
-          bool candu[kTPT], cand = false;
-#pragma unroll
-          for (int u = 0; u < kTPT; ++u) {
-            const float dx = px[u] - zone.y, dy = py[u] - zone.z, dz = pz[u] - zone.w;
-            candu[u] = valid[u] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < zone.x;
-            cand |= candu[u];
-          }
-          if (__any_sync(kFull, cand)) {
-            // some lane of the warp is within reach of this record
-            const int rec = ch.rec_begin + t * kTileW + r;
-            if (LAT) {
-              RecView v;
-              load_view(R4, v);
-              unsigned msk[kTPT];
-#pragma unroll
-              for (int u = 0; u < kTPT; ++u)
-                msk[u] = rec_lat<true>(R4, v, cx, cy, cz, px[u], py[u], pz[u], ax[u], ay[u], az[u], candu[u]);
-#pragma unroll
-              for (int u = 0; u < kTPT; ++u) near_append(msk[u], mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
-            } else {
-#pragma unroll
-              for (int u = 0; u < kTPT; ++u) {
-                float rx[4], ry[4], rz[4], inv[4];
-                corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-                const unsigned msk = ring_fp32<true>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u], candu[u]);
-                near_append(msk, mt[u], q, rec, lane, ctl, near, near_cap, nstage, staged);
-              }
-            }
-            continue;
-          }
-          if (LAT) {
-            rec_lat_pair<kTPT>(R4, cx, cy, cz, px, py, pz, ax, ay, az);
-            continue;
-          }
-#pragma unroll
-          for (int u = 0; u < kTPT; ++u) {
-            float rx[4], ry[4], rz[4], inv[4];
-            corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx, ry, rz, inv);
-            ring_fp32<false>(R4, rx, ry, rz, inv, ax[u], ay[u], az[u]);
-          }
-        } else if (!LAT) {
+        if (!LAT) {
           // both targets' corner vectors first: more independent work in flight
           float rx[kTPT][4], ry[kTPT][4], rz[kTPT][4], inv[kTPT][4];
 #pragma unroll
           for (int u = 0; u < kTPT; ++u) corner_vectors(px[u], py[u], pz[u], cx, cy, cz, rx[u], ry[u], rz[u], inv[u]);
 #pragma unroll
-          for (int u = 0; u < kTPT; ++u) ring_fp32<false>(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
+          for (int u = 0; u < kTPT; ++u) ring_fp32(R4, rx[u], ry[u], rz[u], inv[u], ax[u], ay[u], az[u]);
         } else {
           rec_lat_pair<kTPT>(R4, cx, cy, cz, px, py, pz, ax, ay, az);
         }
@@ -506,7 +336,6 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
-  if (NEAR) near_flush(nstage, staged, lane, ctl, near, near_cap);
 #pragma unroll
   for (int u = 0; u < kTPT; ++u) {
     if (valid[u]) {
@@ -516,6 +345,148 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
       o[2] = acc64[u][2];
     }
   }
+}
+
+
+// ---- near field: hash grid over the records' near zones -----------------
+// Scratch layout: grid_layout (vlm_bs.h).  The box of record r is [8 r ..]:
+// min xyz, max xyz (min > max: no near zone); the bucket counts become the
+// fill cursors after the scan.
+__device__ __forceinline__ unsigned cell_hash(int ix, int iy, int iz, int T) {
+  return ((unsigned)ix * 73856093u ^ (unsigned)iy * 19349663u ^ (unsigned)iz * 83492791u) & (unsigned)(T - 1);
+}
+__device__ __forceinline__ int cell_of(float x, float invh) { return (int)floorf(x * invh); }
+
+// Bounding box of the record's active near zones: every filament k with a
+// near threshold ([32 + k] >= 0) contributes its segment grown by 1.5 x its
+// zone radius near_factor rvc_k = sqrt([32 + k]) / |e_k| (the zone is the
+// segment's cylinder of that radius, extended by it at both ends), in FP64
+// from the record's corners, rounded outwards to FP32.
+__global__ void k_grid_bbox(const float* __restrict__ rec32, const double* __restrict__ rec64, int nrec,
+                            unsigned char* __restrict__ scratch) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  GridHdr* H = reinterpret_cast<GridHdr*>(scratch);
+  const GridLayout L = grid_layout(nrec);
+  float* bb = reinterpret_cast<float*>(scratch + L.bbox) + 8 * (size_t)i;
+  const float* R = rec32 + (size_t)i * kRec32;
+  const double* D = rec64 + (size_t)i * kRec64;
+  const bool fil = (int)D[17] & REC_FIL;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  bool any = false;
+  for (int k = 0; k < 4; ++k) {
+    const float thr = R[32 + k];
+    if (!(thr >= 0.f)) continue;
+    const int j = (k + 1) & 3;
+    const int sk = fil ? (k == 1 || k == 2 ? 1 : 0) : k, sj = fil ? (j == 1 || j == 2 ? 1 : 0) : j;
+    const double ax = D[3 * sk], ay = D[3 * sk + 1], az = D[3 * sk + 2];
+    const double bx = D[3 * sj], by = D[3 * sj + 1], bz = D[3 * sj + 2];
+    const double ee = (bx - ax) * (bx - ax) + (by - ay) * (by - ay) + (bz - az) * (bz - az);
+    if (!(ee > 0.0)) continue;
+    const double z = 1.5 * sqrt((double)thr / ee) + 1e-7;
+    lo[0] = fmin(lo[0], fmin(ax, bx) - z), hi[0] = fmax(hi[0], fmax(ax, bx) + z);
+    lo[1] = fmin(lo[1], fmin(ay, by) - z), hi[1] = fmax(hi[1], fmax(ay, by) + z);
+    lo[2] = fmin(lo[2], fmin(az, bz) - z), hi[2] = fmax(hi[2], fmax(az, bz) + z);
+    any = true;
+  }
+  if (!any) {
+    bb[0] = 1.f, bb[3] = -1.f;
+    return;
+  }
+  float ext = 0.f;
+  for (int a = 0; a < 3; ++a) {
+    bb[a] = __double2float_rd(lo[a]);
+    bb[3 + a] = __double2float_ru(hi[a]);
+    ext = fmaxf(ext, bb[3 + a] - bb[a]);
+  }
+  atomicMax(&H->hbits, __float_as_uint(ext));  // non-negative floats order as their bits
+}
+
+// The buckets of the cells a box overlaps, each once.  The cell size is 1 %
+// above the largest box, so a box overlaps at most 2 cells per axis; the
+// enumeration allows 3 (FP32 rounding of coordinates more than ~10^5 cells
+// from the origin) and the fill checks the entry capacity.
+constexpr int kMaxBoxBuckets = 27;
+__device__ __forceinline__ int box_buckets(const float* bb, float invh, int T, unsigned (&out)[kMaxBoxBuckets]) {
+  const int x0 = cell_of(bb[0], invh), x1 = min(cell_of(bb[3], invh), x0 + 2);
+  const int y0 = cell_of(bb[1], invh), y1 = min(cell_of(bb[4], invh), y0 + 2);
+  const int z0 = cell_of(bb[2], invh), z1 = min(cell_of(bb[5], invh), z0 + 2);
+  int n = 0;
+  for (int x = x0; x <= x1; ++x)
+    for (int y = y0; y <= y1; ++y)
+      for (int z = z0; z <= z1; ++z) {
+        const unsigned h = cell_hash(x, y, z, T);
+        bool dup = false;
+        for (int k = 0; k < n; ++k) dup |= out[k] == h;
+        if (!dup) out[n++] = h;
+      }
+  return n;
+}
+
+__device__ __forceinline__ float grid_invh(const GridHdr* H) {
+  const float h = __uint_as_float(H->hbits) * 1.01f;
+  return h > 0.f ? 1.f / h : 0.f;
+}
+
+// FILL = false: count the records per bucket; true: write them
+template <bool FILL>
+__global__ void k_grid_insert(int nrec, unsigned char* __restrict__ scratch) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
+  const GridLayout L = grid_layout(nrec);
+  const float* bb = reinterpret_cast<const float*>(scratch + L.bbox) + 8 * (size_t)i;
+  if (!(bb[0] <= bb[3])) return;
+  int* count = reinterpret_cast<int*>(scratch + L.count);
+  unsigned b[kMaxBoxBuckets];
+  const int n = box_buckets(bb, grid_invh(H), H->T, b);
+  for (int k = 0; k < n; ++k) {
+    if (!FILL) {
+      atomicAdd(count + b[k], 1);
+    } else {
+      const int slot = atomicAdd(count + b[k], 1);
+      if (slot < 8 * nrec) reinterpret_cast<int*>(scratch + L.entry)[slot] = i;
+    }
+  }
+}
+
+// Exclusive scan of the bucket counts into start[0..T]; the counts become
+// the fill cursors (= start).  One block.
+__global__ void k_grid_scan(int nrec, unsigned char* __restrict__ scratch) {
+  const GridLayout L = grid_layout(nrec);
+  const int T = reinterpret_cast<const GridHdr*>(scratch)->T;
+  int* count = reinterpret_cast<int*>(scratch + L.count);
+  int* start = reinterpret_cast<int*>(scratch + L.start);
+  __shared__ int part[1024];
+  const int per = (T + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per, b1 = min(T, b0 + per);
+  int sum = 0;
+  for (int b = b0; b < b1; ++b) sum += count[b];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      const int v = part[t];
+      part[t] = acc;
+      acc += v;
+    }
+    start[T] = acc;
+  }
+  __syncthreads();
+  int acc = part[threadIdx.x];
+  for (int b = b0; b < b1; ++b) {
+    const int c = count[b];
+    start[b] = acc;
+    count[b] = acc;
+    acc += c;
+  }
+}
+
+__global__ void k_grid_init(unsigned char* scratch, int T) {
+  GridHdr* H = reinterpret_cast<GridHdr*>(scratch);
+  H->hbits = 0u;
+  H->T = T;
 }
 
 // FP64 filament velocity (src/classdef.f90:476-503: the Vatistas n=2 kernel
@@ -532,37 +503,87 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
   return c * (d * rsqrt(s2 * s2 + c2 * c2) * kInv4Pi);
 }
 
-// FP64 evaluation of the listed near-field filament-target pairs (filament
-// velocity times the circulation), added in fixed point to the accumulators
-// of their (chunk, target).
-__global__ void k_near64(const NearPair* __restrict__ near, int* __restrict__ ctl, int near_cap,
-                         const double* __restrict__ rec64, const double* __restrict__ ew,
-                         const double* __restrict__ P, int M, unsigned long long* __restrict__ nacc) {
-  const int n = min(ctl[1], near_cap);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const NearPair np = near[i];
-    const double* R = rec64 + (size_t)np.rec * kRec64;
-    const d3 p = mk3(P[3 * (size_t)np.m], P[3 * (size_t)np.m + 1], P[3 * (size_t)np.m + 2]);
-    d3 v;
-    if ((int)R[17] & REC_FIL) {
-      v = fil_near64(p, mk3(R[0], R[1], R[2]), mk3(R[3], R[4], R[5]), R[12]);
-    } else {
-      const int k = np.k, j = (k + 1) & 3;
-      v = fil_near64(p, mk3(R[3 * k], R[3 * k + 1], R[3 * k + 2]), mk3(R[3 * j], R[3 * j + 1], R[3 * j + 2]),
-                     R[12 + k]);
-    }
-    v = v * (ew ? ew[4 * (size_t)np.rec + np.k] : R[16]);
-    unsigned long long* o = nacc + ((size_t)np.q * M + np.m) * 3;
-    const double c[3] = {v.x, v.y, v.z};
-    for (int a = 0; a < 3; ++a) {
-      if (!(fabs(c[a]) < kNearMax)) {
-        atomicExch(ctl, 4);
-        continue;
+// One thread per target: the records of the target's bucket whose near-zone
+// box holds it; for each of their filaments with the target inside the near
+// zone -- |r_k x r_j|^2 < (near_factor rvc |e|)^2 and the projection within
+// the segment extended by near_factor rvc, tested on the FP32 kernel's own
+// FP32 values -- the correction FP64 velocity x weight - the FP32 kernel's
+// contribution f (r_k x r_j) (recomputed with the same FP32 operations, the
+// product taken exactly in FP64) goes to the fixed-point accumulator of the
+// target and the record's chunk.  ctl[1] counts the corrected pairs, ctl[0]
+// = 4 flags a correction outside the fixed-point range.
+__global__ void k_near_fix(const float* __restrict__ rec32, const double* __restrict__ rec64, int nrec,
+                           const double* __restrict__ ew, const Chunk* __restrict__ chunks, int nchunks,
+                           const double* __restrict__ P, int M, const unsigned char* __restrict__ scratch,
+                           unsigned long long* __restrict__ nacc, int* __restrict__ ctl) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
+  const float invh = grid_invh(H);
+  if (!(invh > 0.f)) return;  // no near zone anywhere
+  const GridLayout L = grid_layout(nrec);
+  const float* bbox = reinterpret_cast<const float*>(scratch + L.bbox);
+  const int* start = reinterpret_cast<const int*>(scratch + L.start);
+  const int* entry = reinterpret_cast<const int*>(scratch + L.entry);
+  const double p64x = P[3 * (size_t)m], p64y = P[3 * (size_t)m + 1], p64z = P[3 * (size_t)m + 2];
+  const float px = (float)p64x, py = (float)p64y, pz = (float)p64z;  // as the FP32 kernel
+  if (start[H->T] > 8 * nrec) {  // more bucket entries than the scratch holds
+    if (m == 0) atomicExch(ctl, 3);
+    return;
+  }
+  const unsigned b = cell_hash(cell_of(px, invh), cell_of(py, invh), cell_of(pz, invh), H->T);
+  int found = 0;
+  for (int e = start[b]; e < start[b + 1]; ++e) {
+    const int r = entry[e];
+    const float* bb = bbox + 8 * (size_t)r;
+    if (!(px >= bb[0] && px <= bb[3] && py >= bb[1] && py <= bb[4] && pz >= bb[2] && pz <= bb[5])) continue;
+    const float* R = rec32 + (size_t)r * kRec32;
+    RecView v;
+    load_view(reinterpret_cast<const float4*>(R), v);
+    for (int k = 0; k < 4; ++k) {
+      const float thr = R[32 + k];
+      if (!(thr >= 0.f)) continue;
+      const int j = (k + 1) & 3;
+      float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
+      corner_vector(px, py, pz, R[3 * k], R[3 * k + 1], R[3 * k + 2], rxk, ryk, rzk, invk);
+      corner_vector(px, py, pz, R[3 * j], R[3 * j + 1], R[3 * j + 2], rxj, ryj, rzj, invj);
+      const Fil32 t = fil_terms(v.ex[k], v.ey[k], v.ez[k], v.eev[k], v.a4v[k], rxk, ryk, rzk, invk, rxj, ryj, rzj, invj);
+      if (!(t.c2 < thr && t.c2 > kS2Min && t.tt > R[36 + k] && t.tt < R[40 + k])) continue;
+      // FP64 value of the same filament pair
+      const double* D = rec64 + (size_t)r * kRec64;
+      const d3 p = mk3(p64x, p64y, p64z);
+      d3 v64;
+      if ((int)D[17] & REC_FIL) {
+        v64 = fil_near64(p, mk3(D[0], D[1], D[2]), mk3(D[3], D[4], D[5]), D[12]);
+      } else {
+        v64 = fil_near64(p, mk3(D[3 * k], D[3 * k + 1], D[3 * k + 2]), mk3(D[3 * j], D[3 * j + 1], D[3 * j + 2]),
+                         D[12 + k]);
       }
-      atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
+      v64 = v64 * (ew ? ew[4 * (size_t)r + k] : D[16]);
+      const double c[3] = {v64.x - (double)t.f * (double)t.kx, v64.y - (double)t.f * (double)t.ky,
+                           v64.z - (double)t.f * (double)t.kz};
+      // the record's chunk (chunks are in record order)
+      int lo = 0, hi = nchunks - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (chunks[mid].rec_begin <= r) lo = mid;
+        else hi = mid - 1;
+      }
+      unsigned long long* o = nacc + ((size_t)lo * M + m) * 3;
+      for (int a = 0; a < 3; ++a) {
+        if (!(fabs(c[a]) < kNearMax)) {
+          atomicExch(ctl, 4);
+          continue;
+        }
+        atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
+      }
+      ++found;
     }
   }
+  if (found) atomicAdd(ctl + 1, found);
 }
+
+__global__ void k_set_flag(int* ctl, int code) { atomicExch(ctl, code); }
 
 // part += nacc / 2^44, and nacc back to zero for the next evaluation.
 __global__ void k_near_apply(double* __restrict__ part, long long* __restrict__ nacc, size_t n) {
@@ -615,18 +636,6 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
   }
   const float nf = (float)near_factor;
   const float w = (float)(g * kInv4Pi);
-  // centre of the near zones: mean of the active filaments' end points
-  double mx = 0.0, my = 0.0, mz = 0.0;
-  for (int k = 0; k < 4; ++k) {
-    mx += cx[k];
-    my += cy[k];
-    mz += cz[k];
-  }
-  mx *= 0.25;
-  my *= 0.25;
-  mz *= 0.25;
-  float reach = 0.f;
-  bool anyNear = false;
   for (int k = 0; k < 4; ++k) {
     const int j = (k + 1) & 3;
     const bool act = EW ? EW[k] != 0.0 : (!fil || k == 0) && !skipped;
@@ -650,22 +659,8 @@ __global__ void k_pack32(const double* __restrict__ rec64, int nrec, double near
     const float blo = -nfs * wk, bhi = (ee + nfs) * wk;
     o[36 + k] = on ? fminf(blo, bhi) : 0.f;
     o[40 + k] = on ? fmaxf(blo, bhi) : 0.f;
-    if (on) {
-      anyNear = true;
-      // farthest point of this filament's near zone from the centre
-      const float ax = (float)(cx[k] - mx), ay = (float)(cy[k] - my), az = (float)(cz[k] - mz);
-      const float bx = (float)(cx[j] - mx), by = (float)(cy[j] - my), bz = (float)(cz[j] - mz);
-      const float da = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-      const float db = sqrtf(fmaf(bx, bx, fmaf(by, by, bz * bz)));
-      reach = fmaxf(reach, fmaxf(da, db) + nf * rv[k]);
-    }
   }
-  // margin for the FP32 rounding of corners and of this sum
-  const float r = reach * 1.0001f + 1e-6f;
-  o[44] = anyNear ? r * r : -1.f;
-  o[45] = (float)mx;
-  o[46] = (float)my;
-  o[47] = (float)mz;
+  o[44] = o[45] = o[46] = o[47] = 0.f;
 }
 
 }  // namespace
@@ -677,9 +672,9 @@ void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec
   k_pack32<<<(nrec + 255) / 256, 256, 0, s>>>(rec64, nrec, near_factor, rec32, ew);
 }
 
-void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
-                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s,
-                      const double* ew) {
+void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
+                      const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
+                      long long* nacc, cudaStream_t s, const double* ew) {
   if (M <= 0 || nchunks <= 0) return;
   const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
   // the dynamic shared-memory opt-in is per device; set it once on each
@@ -687,29 +682,39 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || !attr[dev].load(std::memory_order_acquire)) {
-    cudaFuncSetAttribute(k_partial32<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_partial32<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_partial32<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_partial32<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (dev >= 0 && dev < 64) attr[dev].store(true, std::memory_order_release);
   }
   dim3 grid((M + kTargetsPerBlock32 - 1) / kTargetsPerBlock32, nchunks);
   count_launch();
-  if (near) {
-    if (ew) k_partial32<true, true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
-    else k_partial32<true, false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
-    const int sms = device_sm_count();
+  if (ew) k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
+  else k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
+  if (!near_scratch || nrec <= 0) return;
+  // near field: grid over the records' near zones, FP64 corrections of the
+  // near pairs, corrections folded into the partial sums
+  if (near_bytes < near_grid_bytes(nrec)) {
     count_launch();
-    k_near64<<<4 * sms, 128, 0, s>>>(near, ctl, near_cap, rec64, ew, P, M,
-                                     reinterpret_cast<unsigned long long*>(nacc));
-    const size_t n = (size_t)M * nchunks * 3;
-    count_launch();
-    k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * sms), 256, 0, s>>>(part, nacc, n);
-  } else if (ew) {
-    k_partial32<false, true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
-  } else {
-    k_partial32<false, false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl, near, near_cap);
+    k_set_flag<<<1, 1, 0, s>>>(ctl, 3);
+    return;
   }
+  unsigned char* g = static_cast<unsigned char*>(near_scratch);
+  const GridLayout L = grid_layout(nrec);
+  const int T = grid_buckets(nrec);
+  const int rb = (nrec + 255) / 256;
+  count_launches(6);
+  k_grid_init<<<1, 1, 0, s>>>(g, T);
+  k_grid_bbox<<<rb, 256, 0, s>>>(rec32, rec64, nrec, g);
+  cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), s);
+  k_grid_insert<false><<<rb, 256, 0, s>>>(nrec, g);
+  k_grid_scan<<<1, 1024, 0, s>>>(nrec, g);
+  k_grid_insert<true><<<rb, 256, 0, s>>>(nrec, g);
+  k_near_fix<<<(M + 127) / 128, 128, 0, s>>>(rec32, rec64, nrec, ew, chunks, nchunks, P, M, g,
+                                             reinterpret_cast<unsigned long long*>(nacc), ctl);
+  const size_t n = (size_t)M * nchunks * 3;
+  count_launch();
+  k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * device_sm_count()), 256, 0, s>>>(part, nacc,
+                                                                                                            n);
 }
 
 // A host without a usable device still plans (sizes are queried before any
@@ -736,8 +741,8 @@ int partial32_slots() {
   if (!cache[dev]) {
     int per = 0;
     const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
-    cudaFuncSetAttribute(k_partial32<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true, false>, kBlockW, smem);
+    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<false>, kBlockW, smem);
     cache[dev] = device_sm_count() * std::max(1, per);
   }
   return cache[dev];

@@ -368,8 +368,8 @@ struct Case {
     s.targets = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.outv = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.part = dalloc<double>((size_t)maxPart * 3, scratchOwned);
-    s.nearCap = opt.precision == VLM_PREC_FP32_NEAR64 ? 256 * maxTargets : 1;
-    s.near = dalloc<NearPair>((size_t)s.nearCap, scratchOwned);
+    s.nearBytes = opt.precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes(maxRecords) : 0;
+    s.nearScratch = s.nearBytes ? dalloc<unsigned char>(s.nearBytes, scratchOwned) : nullptr;
     // zero here; every near-field evaluation leaves them zero
     s.nacc = dalloc<long long>(opt.precision == VLM_PREC_FP32_NEAR64 ? (size_t)maxPart * 3 : 1, scratchOwned);
     dGroups = dalloc<Group>(std::max<size_t>(hGroups.size(), 1), scratchOwned);
@@ -455,8 +455,8 @@ struct Case {
       const bool nearOn = prec == VLM_PREC_FP32_NEAR64;
       launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream, s.edgeW);
       VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
-      launch_partial32(s.rec32, s.rec64, ch, e.nchunks, P, M, s.part, s.err + 2, nearOn ? s.near : nullptr,
-                       s.nearCap, s.nacc, stream, s.edgeW);
+      launch_partial32(s.rec32, s.rec64, ch, e.nchunks, e.nrec, P, M, s.part, s.err + 2,
+                       nearOn ? s.nearScratch : nullptr, s.nearBytes, s.nacc, stream, s.edgeW);
     }
     if (e.nchunks == 0) {
       VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M, stream));
@@ -720,9 +720,14 @@ struct Case {
     launch_scatter_nodes(d, s, stepFrame(k), pl.rowNear, pl.rowFar, pred, iwv, stream);
   }
 
-  void start() {
+  // The AIC of the initial geometry, its FP64 LU and explicit inverse, the
+  // inverse check, and (refined solves) its FP32 LU (src/main.f90:62-81:
+  // rotor%calcAIC, inv2, isInverse).  Once per case.
+  bool factored = false;
+  void aicFactor() {
     useDevice();
     if (started) throw StatusError(VLM_ERR_STATE, "case already started");
+    if (factored) return;
     launch_aic(d, s, frame(0), stream);
     launch_lu_inverse(d, s, stream);
     launch_is_inverse(d, s, stream);
@@ -732,6 +737,14 @@ struct Case {
     if (err == 10) throw StatusError(VLM_ERR_SINGULAR, "Matrix is numerically singular!");
     if (err == 11) throw StatusError(VLM_ERR_SINGULAR, "Computed AIC_inv does not seem to be correct within given tolerance");
     if (refine) launch_lu32(d, s, stream);
+    VLM_CUDA(cudaGetLastError());
+    factored = true;
+  }
+
+  void start() {
+    useDevice();
+    if (started) throw StatusError(VLM_ERR_STATE, "case already started");
+    aicFactor();
     launch_solve(d, s, frame(0), false, stream);
     if (d.NW > 0) launch_shed(d, s, frame(0), d.NW + 1, false, stream);
     if (W.sw.rotorForcePlot != 0) launch_loads(d, s, frame(0), chunk64, 0, stream);
@@ -748,6 +761,21 @@ struct Case {
   }
 
   void enqueueStepBody(int k) {
+    enqueueSolvePhase(k);
+    if (W.sw.rotorForcePlot != 0 && k % W.sw.rotorForcePlot == 0) {
+      VLM_CUDA(cudaEventRecord(evFork, stream));
+      VLM_CUDA(cudaStreamWaitEvent(side, evFork, 0));
+      launch_loads(d, s, stepFrame(k), chunk64, replaying ? -1 : k, side);
+      VLM_CUDA(cudaEventRecord(evJoin, side));
+      loadsForked = true;
+    }
+    enqueueWakePhase(k);
+  }
+
+  // Phase 1 of step k (src/main.f90:466-603): shedding of the leading-edge
+  // row, wake ageing and dissipation, the wake-induced velocity at the
+  // collocation points, the RHS, the circulation solve.
+  void enqueueSolvePhase(int k) {
     const StepPlan& pl = plans[k];
     const int rN = pl.rowNear, rF = pl.rowFar;
     const double* fr = stepFrame(k);
@@ -776,13 +804,17 @@ struct Case {
     } else {
       launch_solve(d, s, fr, false, stream);
     }
-    if (W.sw.rotorForcePlot != 0 && k % W.sw.rotorForcePlot == 0) {
-      VLM_CUDA(cudaEventRecord(evFork, stream));
-      VLM_CUDA(cudaStreamWaitEvent(side, evFork, 0));
-      launch_loads(d, s, fr, chunk64, replaying ? -1 : k, side);
-      VLM_CUDA(cudaEventRecord(evJoin, side));
-      loadsForked = true;
-    }
+  }
+
+  // Phase 3 of step k (src/main.f90:799-1439): wake-node velocities, the
+  // finite-difference scheme (predictor, predicted-wake velocities,
+  // corrector), strain, roll-up / far-wake shift, trailing-edge shedding.
+  // (Phase 2, the loads, only reads the solution.)
+  void enqueueWakePhase(int k) {
+    const StepPlan& pl = plans[k];
+    const int rN = pl.rowNear, rF = pl.rowFar;
+    const double* fr = stepFrame(k);
+    const bool wake = d.NW > 0 && W.sw.wakeSuppress == 0;
     if (!wake) return;
     evalNodes(k, false);
     switch (W.sw.fdScheme) {
@@ -857,6 +889,7 @@ struct Case {
   // ---- the time loop: inputs in, steps enqueued, results out ---------------
   void checkSteps(int nsteps) const {
     if (!started) throw StatusError(VLM_ERR_STATE, "vlm_case_start must be called before vlm_case_step");
+    if (phase != 0) throw StatusError(VLM_ERR_STATE, "a step opened by vlm_case_solve_circulation is not finished");
     if (nsteps < 0 || iter + nsteps > W.nt)
       throw StatusError(VLM_ERR_INVALID, "nsteps runs past the case's nt timesteps");
   }
@@ -885,7 +918,7 @@ struct Case {
     VLM_CUDA(cudaStreamSynchronize(stream));
     iter += nsteps;
     const int err = errs[2];
-    if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
+    if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field scratch too small");
     if (err == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
     if (err) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
     if (errs[1]) throw StatusError(VLM_ERR_SINGULAR, "FP32 LU iterative refinement left a relative residual above 1e-9");
@@ -907,6 +940,64 @@ struct Case {
     VLM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     lastMs = ms;
     finishSteps(nsteps, ctRows);
+  }
+
+  // ---- the step as three calls (a host that drives its own time loop) -------
+  // phase: 0 between steps; 1 after the circulation solve of step iter + 1;
+  // 2 after its loads.  The three phases enqueue exactly the kernels of
+  // vlm_case_step in the same order on the case stream (the loads on the
+  // stream itself instead of the side stream: they only read the solution),
+  // so the results are the same bits.
+  int phase = 0;
+  void phaseSolve(const double* kinVel, double* gamOut) {
+    useDevice();
+    if (phase != 0) throw StatusError(VLM_ERR_STATE, "step already open: finish it with vlm_case_wake_step");
+    checkSteps(1);
+    const int k = iter + 1;
+    double* hf = hFrames + (size_t)k * d.fl.size;
+    if (kinVel) {
+      // the caller's kinematic velocity at the collocation points replaces the
+      // frame's (same panel order as the reference's RHS rows)
+      for (int p = 0; p < d.nb * d.npan; ++p)
+        for (int a = 0; a < 3; ++a) hf[d.fl.pan + (size_t)p * kPan + 24 + a] = kinVel[3 * (size_t)p + a];
+    }
+    uploadFrames(1);
+    iterSynced = false;
+    if (surr.on) surrPreStep(k);
+    enqueueSolvePhase(k);
+    VLM_CUDA(cudaGetLastError());
+    if (gamOut) VLM_CUDA(cudaMemcpyAsync(gamOut, s.gamVec, sizeof(double) * d.n, cudaMemcpyDeviceToHost, stream));
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    int errs[4] = {0, 0, 0, 0};
+    VLM_CUDA(cudaMemcpy(errs, s.err, sizeof(errs), cudaMemcpyDeviceToHost));
+    if (errs[1]) throw StatusError(VLM_ERR_SINGULAR, "FP32 LU iterative refinement left a relative residual above 1e-9");
+    if (gamOut)
+      for (int i = 0; i < d.n; ++i)
+        if (!std::isfinite(gamOut[i])) throw StatusError(VLM_ERR_NONFINITE, "non-finite circulation");
+    phase = 1;
+  }
+  void phaseLoads(double* row) {
+    useDevice();
+    if (phase != 1) throw StatusError(VLM_ERR_STATE, "vlm_case_loads needs a solved step (vlm_case_solve_circulation)");
+    const int k = iter + 1;
+    launch_loads(d, s, frame(k), chunk64, k, stream);
+    VLM_CUDA(cudaGetLastError());
+    double r[10];
+    VLM_CUDA(cudaMemcpyAsync(r, s.ctHist + (size_t)k * 10, sizeof(r), cudaMemcpyDeviceToHost, stream));
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    for (double x : r)
+      if (!std::isfinite(x)) throw StatusError(VLM_ERR_NONFINITE, "non-finite load in the CT row");
+    if (row) std::memcpy(row, r, sizeof(r));
+    phase = 2;
+  }
+  void phaseWake() {
+    useDevice();
+    if (phase == 0) throw StatusError(VLM_ERR_STATE, "vlm_case_wake_step needs a solved step (vlm_case_solve_circulation)");
+    const int k = iter + 1;
+    enqueueWakePhase(k);
+    VLM_CUDA(cudaGetLastError());
+    phase = 0;
+    finishSteps(1, nullptr);
   }
 
   // ---- checkpoint / resume (the reference's Restart/restartNNNNN.dat:
@@ -1018,6 +1109,8 @@ struct Case {
     }
     // the frame of the restored step (later steps upload their own)
     iter = (int)h[1];
+    factored = true;
+    phase = 0;
     VLM_CUDA(cudaMemcpy(s.frames + (size_t)iter * d.fl.size, hFrames + (size_t)iter * d.fl.size,
                         sizeof(double) * d.fl.size, cudaMemcpyHostToDevice));
     started = true;
@@ -1065,9 +1158,9 @@ struct Case {
       if (opt.precision == VLM_PREC_FP64) launch_partial64(s.rec64, ch, pl.node.nchunks, s.targets, M, s.part, stream);
       else {
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
-        launch_partial32(s.rec32, s.rec64, ch, pl.node.nchunks, s.targets, M, s.part, s.err + 2,
-                         opt.precision == VLM_PREC_FP32_NEAR64 ? s.near : nullptr, s.nearCap, s.nacc, stream,
-                         s.edgeW);
+        launch_partial32(s.rec32, s.rec64, ch, pl.node.nchunks, pl.node.nrec, s.targets, M, s.part, s.err + 2,
+                         opt.precision == VLM_PREC_FP32_NEAR64 ? s.nearScratch : nullptr, s.nearBytes, s.nacc,
+                         stream, s.edgeW);
       }
     };
     launch();  // warm
@@ -1184,6 +1277,15 @@ struct Case {
       v = dget(s.vN[k[4] - '0'] + 3 * b * NW * (ns + 1), 3 * NW * (ns + 1));
     else if (bok && (k == "velF1" || k == "velF2" || k == "velF3")) v = dget(s.vF[k[4] - '0'] + 3 * b * NF, 3 * NF);
     else if (bok && k == "gamPrev") v = dget(s.gamPrev + b * npan, npan);
+    else if (bok && k == "velKin") {
+      // the prescribed kinematic velocity at the collocation points of the
+      // current iteration (of the open step between its phases)
+      const double* f = hFrames + (size_t)(phase != 0 ? iter + 1 : iter) * d.fl.size;
+      for (size_t q = 0; q < npan; ++q) {
+        const double* r = f + d.fl.pan + (b * npan + q) * kPan + 24;
+        v.insert(v.end(), r, r + 3);
+      }
+    }
     else if (bok && k == "secCL") v = dget(s.secCL + b * ns, ns);
     else if (bok && k == "secLiftDir") v = dget(s.secLiftDir + 3 * b * ns, 3 * ns);
     else if (bok && k == "secChordwiseResVel") v = dget(s.secResVel + 3 * b * ns, 3 * ns);
@@ -1263,11 +1365,12 @@ struct Case {
       } else {
         const bool nearOn = opt.precision == VLM_PREC_FP32_NEAR64;
         launch_pack32(rec64, rec, nearOn ? opt.near_factor : 0.0, rec32, stream);
-        const int cap = nearOn ? (int)std::min<int64_t>(64 * M + (1 << 16), 1 << 26) : 1;
-        NearPair* np = dalloc<NearPair>(cap, tmpOwned);
+        const size_t nb = nearOn ? near_grid_bytes(rec) : 1;
+        unsigned char* ns = dalloc<unsigned char>(nb, tmpOwned);
         long long* nacc = dalloc<long long>(nearOn ? (size_t)M * nq * 3 : 1, tmpOwned);
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
-        launch_partial32(rec32, rec64, dc, nq, dP, (int)M, part, s.err + 2, nearOn ? np : nullptr, cap, nacc, stream);
+        launch_partial32(rec32, rec64, dc, nq, rec, dP, (int)M, part, s.err + 2, nearOn ? ns : nullptr, nb, nacc,
+                         stream);
       }
       if (opt.precision == VLM_PREC_FP64) launch_combine(part, (int)M, dg, (int)g.size(), 2, dV, stream);
       else {
@@ -1295,7 +1398,7 @@ struct RingScratch {
   Chunk* chunks = nullptr;
   Group* group = nullptr;
   int* err = nullptr;
-  NearPair* near = nullptr;
+  unsigned char* near = nullptr;
   long long* nacc = nullptr;  // zero between calls
   size_t cap64 = 0, cap32 = 0, capPart = 0, capChunks = 0, capNear = 0, capNacc = 0;
 };
@@ -1340,7 +1443,6 @@ static int ring_plan(int64_t N, int64_t M, int precision, Group& g, std::vector<
   return nq;
 }
 
-static int64_t ring_near_cap(int64_t M) { return std::min<int64_t>(16 * M + (1 << 20), 1 << 27); }
 
 int64_t ring_scratch_bytes(int64_t N, int64_t M, int precision) {
   Group g;
@@ -1348,7 +1450,7 @@ int64_t ring_scratch_bytes(int64_t N, int64_t M, int precision) {
   const int64_t Q = std::max(1, ring_plan(N, M, precision, g, ch));
   int64_t b = N * kRec64 * 8 + M * Q * 3 * 8 + Q * (int64_t)sizeof(Chunk) + 64;
   if (precision != VLM_PREC_FP64) b += N * kRec32 * 4;
-  if (precision == VLM_PREC_FP32_NEAR64) b += ring_near_cap(M) * (int64_t)sizeof(NearPair) + M * Q * 3 * 8;
+  if (precision == VLM_PREC_FP32_NEAR64) b += (int64_t)near_grid_bytes((int)N) + M * Q * 3 * 8;
   return b;
 }
 
@@ -1383,8 +1485,8 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   grow((void**)&R.chunks, R.capChunks, (size_t)Q * sizeof(Chunk) + sizeof(Group) + 64);
   R.group = reinterpret_cast<Group*>(R.chunks + Q);
   if (!R.err) VLM_CUDA(cudaMalloc(&R.err, 4 * sizeof(int)));
-  const int nearCap = precision == VLM_PREC_FP32_NEAR64 ? (int)ring_near_cap(M) : 1;
-  grow((void**)&R.near, R.capNear, (size_t)nearCap * sizeof(NearPair));
+  const size_t nearBytes = precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes((int)std::max<int64_t>(N, 1)) : 1;
+  grow((void**)&R.near, R.capNear, nearBytes);
   if (precision == VLM_PREC_FP32_NEAR64 && (size_t)M * Q * 3 * 8 > R.capNacc) {
     grow((void**)&R.nacc, R.capNacc, (size_t)M * Q * 3 * 8);
     VLM_CUDA(cudaMemset(R.nacc, 0, R.capNacc));
@@ -1402,7 +1504,8 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
     } else {
       const bool nearOn = precision == VLM_PREC_FP32_NEAR64;
       launch_pack32(R.rec64, (int)N, nearOn ? 4.0 : 0.0, R.rec32, st);
-      launch_partial32(R.rec32, R.rec64, R.chunks, nq, P, (int)M, R.part, R.err, nearOn ? R.near : nullptr, nearCap,
+      launch_partial32(R.rec32, R.rec64, R.chunks, nq, (int)N, P, (int)M, R.part, R.err, nearOn ? R.near : nullptr,
+                       nearBytes,
                        R.nacc, st);
     }
     if (precision == VLM_PREC_FP64) launch_combine(R.part, (int)M, R.group, 1, 2, V, st);
@@ -1416,7 +1519,7 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   int ctl[2] = {0, 0};
   VLM_CUDA(cudaMemcpyAsync(ctl, R.err, sizeof(ctl), cudaMemcpyDeviceToHost, st));
   VLM_CUDA(cudaStreamSynchronize(st));
-  if (ctl[0] == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
+  if (ctl[0] == 3) throw StatusError(VLM_ERR_CUDA, "near-field scratch too small");
   if (ctl[0] == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
   if (ctl[0]) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
 }
@@ -1784,6 +1887,39 @@ int vlm_case_start(vlm_case* c) {
 int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows) {
   if (!c) return VLM_ERR_INVALID;
   return guard([&]() { c->c.step(nsteps, ct_rows); });
+}
+
+int vlm_case_aic_factor(vlm_case* c) {
+  if (!c) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.aicFactor(); });
+}
+
+int vlm_case_solve_circulation(vlm_case* c, const double* kinematic_vel, double* gam_out) {
+  if (!c) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.phaseSolve(kinematic_vel, gam_out); });
+}
+
+int vlm_case_loads(vlm_case* c, double* ct_row) {
+  if (!c) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.phaseLoads(ct_row); });
+}
+
+int vlm_case_wake_step(vlm_case* c) {
+  if (!c) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.phaseWake(); });
+}
+
+int vlm_case_get_wake(vlm_case* c, int blade, double* waN, double* waN_gam, double* waF, double* waF_gam) {
+  if (!c) return VLM_ERR_INVALID;
+  return guard([&]() {
+    Case& C = c->c;
+    if (blade < 1 || blade > C.d.nb) throw StatusError(VLM_ERR_INVALID, "blade out of range");
+    const size_t NW = C.d.NW, NF = C.d.NF, ns = C.d.ns;
+    const std::pair<const char*, std::pair<double*, size_t>> parts[] = {
+        {"waN", {waN, 12 * NW * ns}}, {"waN_gam", {waN_gam, NW * ns}}, {"waF", {waF, 6 * NF}}, {"waF_gam", {waF_gam, NF}}};
+    for (const auto& q : parts)
+      if (q.second.first) C.get(q.first, blade, q.second.first, (int64_t)q.second.second);
+  });
 }
 
 int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value) {

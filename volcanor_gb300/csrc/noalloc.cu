@@ -25,14 +25,14 @@ namespace {
 // Limits of the fixed scratch (see include/vlm.h).
 constexpr int64_t kMaxRings = 16384;
 constexpr int64_t kMaxPoints = 65536;
-constexpr int64_t kMaxNear = 65536;
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kOffRec64 = 0;
 constexpr size_t kOffRec32 = kOffRec64 + align256(kMaxRings * kRec64 * sizeof(double));
 constexpr size_t kOffPart = kOffRec32 + align256(kMaxRings * kRec32 * sizeof(float));
 constexpr size_t kOffNear = kOffPart + align256(kMaxPoints * 3 * sizeof(double));
-constexpr size_t kOffNacc = kOffNear + align256(kMaxNear * sizeof(NearPair));
+constexpr size_t kNearBytes = near_grid_bytes((int)kMaxRings);  // near-field grid for the largest N
+constexpr size_t kOffNacc = kOffNear + align256(kNearBytes);
 constexpr size_t kOffTables = kOffNacc + align256(kMaxPoints * 3 * sizeof(long long));
 constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words
 
@@ -114,7 +114,7 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   double* rec64 = reinterpret_cast<double*>(base + kOffRec64);
   float* rec32 = reinterpret_cast<float*>(base + kOffRec32);
   double* part = reinterpret_cast<double*>(base + kOffPart);
-  NearPair* near = reinterpret_cast<NearPair*>(base + kOffNear);
+  unsigned char* near = base + kOffNear;
   long long* nacc = reinterpret_cast<long long*>(base + kOffNacc);
   Chunk* chunks = reinterpret_cast<Chunk*>(base + kOffTables);
   Group* group = reinterpret_cast<Group*>(base + kOffTables + 64);
@@ -133,7 +133,8 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
         if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
       }
       launch_pack32(rec64, (int)N, nearOn ? 4.0 : 0.0, rec32, st);
-      launch_partial32(rec32, rec64, chunks, 1, P, (int)M, part, ctl, nearOn ? near : nullptr, (int)kMaxNear, nacc, st);
+      launch_partial32(rec32, rec64, chunks, 1, (int)N, P, (int)M, part, ctl, nearOn ? near : nullptr, kNearBytes, nacc,
+                       st);
     }
     launch_combine(part, (int)M, group, 1, 2, V, st);
   } else {
@@ -148,7 +149,7 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   e = cudaMemcpyAsync(flags, ctl, sizeof(flags), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
-  if (flags[0] == 3) return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc: more than 65536 near-field pairs");
+  if (flags[0] == 3) return fail(VLM_ERR_CUDA, "vlm_biot_savart_rings_noalloc: near-field scratch too small");
   if (flags[0] == 4) return fail(VLM_ERR_NONFINITE, "vlm_biot_savart_rings_noalloc: near-field velocity outside the fixed-point range");
   if (flags[0]) return fail(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
   return VLM_OK;

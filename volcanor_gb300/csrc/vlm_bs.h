@@ -40,9 +40,7 @@ constexpr int REC_SKIP = 2;
 //   [32..35] near-field threshold on |r1 x r2|^2: (near_factor rvc_k |e_k|)^2, -1 if off
 //   [36..39] lower near-field bound on (w_k e_k).r1
 //   [40..43] upper near-field bound on (w_k e_k).r1
-//   [44]     squared radius about [45..47] outside which no filament of the
-//            record can be near (-1 when the near-field path is off)
-//   [45..47] centre of the near zones (mean of the four corners)
+//   [44..47] unused (zero; pads the record to 192 B)
 // A pair is near when the target lies within near_factor core radii of the
 // filament SEGMENT: |r1 x r2|^2 < [32+k] and -s < e.r1 < |e|^2 + s with
 // s = near_factor rvc_k |e_k|; the second test is stored multiplied by w_k,
@@ -60,11 +58,41 @@ constexpr int kRec32 = 48;
 // filament evaluations and three corner vectors instead of four and four.
 // Records outside lattices get ew = gam on their active filaments.
 
-// One near-field filament-target pair found by the FP32 kernel: target m,
-// chunk q (partial sum to correct), global record index, filament k.
-struct NearPair {
-  int32_t m, q, rec, k;
+#ifdef __CUDACC__
+#define VLM_BS_HD __host__ __device__
+#else
+#define VLM_BS_HD
+#endif
+
+// Near-field scratch of an evaluation over nrec records (a hash grid over
+// the records' near-zone boxes, carved from one caller buffer):
+//   header (cell size, bucket count), [nrec][8] box floats, [T] bucket
+//   counts, [T + 1] bucket starts, [8 nrec] entries (record indices),
+// T = the smallest power of two >= max(1024, 2 nrec).
+struct GridHdr {
+  unsigned int hbits;  // cell size (the largest box extent) as float bits
+  int T;               // bucket count
+  int pad[2];
 };
+VLM_BS_HD constexpr int grid_buckets(int nrec) {
+  int T = 1024;
+  while (T < 2 * nrec && T < (1 << 28)) T <<= 1;
+  return T;
+}
+VLM_BS_HD constexpr size_t grid_align(size_t b) { return (b + 255) & ~size_t(255); }
+struct GridLayout {
+  size_t bbox, count, start, entry, total;
+};
+VLM_BS_HD constexpr GridLayout grid_layout(int nrec) {
+  const size_t T = (size_t)grid_buckets(nrec);
+  const size_t bbox = grid_align(sizeof(GridHdr));
+  const size_t count = bbox + grid_align((size_t)nrec * 8 * sizeof(float));
+  const size_t start = count + grid_align(T * sizeof(int));
+  const size_t entry = start + grid_align((T + 1) * sizeof(int));
+  return GridLayout{bbox, count, start, entry, entry + grid_align((size_t)nrec * 8 * sizeof(int))};
+}
+// Bytes of near-field scratch an evaluation over nrec records needs.
+VLM_BS_HD constexpr size_t near_grid_bytes(int nrec) { return grid_layout(nrec).total; }
 
 // Fixed-point scale of the near-field accumulators: FP64 near-field
 // velocities are added as integers (v * 2^44, |v| < 2^18) so that their sum
@@ -112,19 +140,19 @@ int device_sm_count();
 // FP64 reference-arithmetic partial sums: part[(q * M + m) * 3 + k].
 void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,
                       cudaStream_t s);
-// FP32 pairs with FP64 accumulation.  When near is non-null, pairs inside the
-// records' near-field thresholds are left out of the FP32 sums, listed in
-// near (capacity near_cap, count in ctl[1]), evaluated in FP64 from rec64 by
-// a second kernel into the fixed-point accumulators nacc (M x nchunks x 3,
-// zero on entry and left zero on return) and added to their partial sums by
-// a third.  ctl[0] receives a nonzero code if a bounded wait on the tile
-// pipeline expired (1, 2), the near list overflowed (3) or a near-field
-// velocity left the fixed-point range (4).  ctl must be zeroed before the call.
+// FP32 pairs with FP64 accumulation over the nrec records the chunks cover.
+// When near_scratch is non-null (near_bytes >= near_grid_bytes(nrec)), the
+// pairs inside the records' near-field thresholds are then corrected to FP64
+// through the fixed-point accumulators nacc (M x nchunks x 3, zero on entry
+// and left zero on return).  ctl[0] receives a nonzero code if a bounded wait
+// on the tile pipeline expired (1, 2), the near-field scratch was too small
+// (3) or a near-field correction left the fixed-point range (4); ctl[1]
+// counts the corrected near pairs.  ctl must be zeroed before the call.
 // ew: the records' edge weights in lattice form (FP64 near field multiplies
 // by ew[4 rec + k] instead of the record's circulation), or null.
-void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, const double* P,
-                      int M, double* part, int* ctl, NearPair* near, int near_cap, long long* nacc, cudaStream_t s,
-                      const double* ew = nullptr);
+void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
+                      const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
+                      long long* nacc, cudaStream_t s, const double* ew = nullptr);
 // Converts FP64 records to FP32 records (near_factor <= 0 disables near-field);
 // ew as above (null: every active filament of a record carries its gam).
 void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s,

@@ -84,9 +84,9 @@ struct DevState {
   // lattice-form edge weights of the gathered records ([rec][4]; null: the
   // records are evaluated ring by ring), written by the gather
   double* edgeW;
-  NearPair* near;
+  void* nearScratch;  // near-field grid scratch (null unless FP32 + FP64 near field)
+  size_t nearBytes;
   long long* nacc;  // fixed-point near-field accumulators, zero between evaluations
-  int nearCap;
   // step replay by a CUDA graph: the step counter on the device and the
   // frame of the step being computed (filled by launch_step_begin)
   int* devIter;

@@ -79,6 +79,11 @@ SIGNATURES = {
     "vlm_case_destroy": (ctypes.c_int, [_vp]),
     "vlm_case_start": (ctypes.c_int, [_vp]),
     "vlm_case_step": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "vlm_case_aic_factor": (ctypes.c_int, [_vp]),
+    "vlm_case_solve_circulation": (ctypes.c_int, [_vp, _dp, _dp]),
+    "vlm_case_loads": (ctypes.c_int, [_vp, _dp]),
+    "vlm_case_wake_step": (ctypes.c_int, [_vp]),
+    "vlm_case_get_wake": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp]),
     "vlm_case_get_int": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_i64)]),
     "vlm_case_get": (_i64, [_vp, ctypes.c_char_p, ctypes.c_int, _dp, _i64]),
     "vlm_case_vind_points": (ctypes.c_int, [_vp, _dp, _i64, _dp]),
@@ -304,6 +309,37 @@ class Case:
         rows = np.zeros((n, 10)) if with_ct else None
         _err(load().vlm_case_step(self._h, int(n), _ptr(rows) if with_ct else None))
         return rows
+
+    # the step as separate calls (include/vlm.h): solve -> [loads] -> wake
+    def aic_factor(self):
+        _err(load().vlm_case_aic_factor(self._h))
+
+    def solve_circulation(self, kinematic_vel=None) -> np.ndarray:
+        """Opens iteration iter+1: RHS + solve; returns gamVec (n).
+        kinematic_vel (n x 3) replaces the library's kinematic velocity."""
+        n = self.geti("n")
+        gam = np.zeros(n)
+        kv = None if kinematic_vel is None else _c64(kinematic_vel).reshape(-1)
+        if kv is not None and kv.size != 3 * n:
+            raise ValueError("kinematic_vel must have 3 x n values")
+        _err(load().vlm_case_solve_circulation(self._h, _ptr(kv) if kv is not None else None, _ptr(gam)))
+        return gam
+
+    def loads(self) -> np.ndarray:
+        row = np.zeros(10)
+        _err(load().vlm_case_loads(self._h, _ptr(row)))
+        return row
+
+    def wake_step(self):
+        _err(load().vlm_case_wake_step(self._h))
+
+    def get_wake(self, blade: int = 1):
+        """(waN (nNwake*ns, 4, 3), waN_gam, waF (nFwake, 2, 3), waF_gam) of a blade."""
+        NW, NF, ns = self.geti("nNwake"), self.geti("nFwake"), self.geti("ns")
+        wn, wg = np.zeros(12 * NW * ns), np.zeros(max(NW * ns, 1))
+        fn, fg = np.zeros(max(6 * NF, 1)), np.zeros(max(NF, 1))
+        _err(load().vlm_case_get_wake(self._h, blade, _ptr(wn), _ptr(wg), _ptr(fn), _ptr(fg)))
+        return wn.reshape(-1, 4, 3), wg[:NW * ns], fn[:6 * NF].reshape(-1, 2, 3), fg[:NF]
 
     def geti(self, name: str) -> int:
         v = _i64()
