@@ -58,27 +58,47 @@ def test_fp32_variants_error_vs_fp64(prec, tol, tol_rms):
     assert np.sqrt(np.mean(err ** 2)) / scale < tol_rms
 
 
-def test_near_field_pairs_are_fp64():
-    """Targets 1-3 core radii from filament midpoints: the FP32 kernel's own
-    position rounding (6e-8 absolute at |x| ~ 1) is a large relative error at
-    a few core radii; the FP64 near-field correction recomputes those pairs
-    from FP64 positions, leaving the far pairs' FP32 rounding only."""
-    rng = np.random.default_rng(11)
-    corners, rvc, gam = random_rings(rng, 4096)
-    n = 600
-    i = rng.integers(0, 4096, n)
+def _near_targets(rng, corners, n, lo=1.0, hi=3.0, core=0.002):
+    """Targets lo..hi core radii from points 20-80 % along random filaments."""
+    i = rng.integers(0, corners.shape[0], n)
     k = rng.integers(0, 4, n)
     a, b = corners[i, k], corners[i, (k + 1) % 4]
     e = b - a
     u = np.cross(e, rng.normal(size=(n, 3)))
     u /= np.linalg.norm(u, axis=1, keepdims=True)
-    P = a + rng.uniform(0.2, 0.8, (n, 1)) * e + u * (rng.uniform(1.0, 3.0, (n, 1)) * 0.002)
+    return a + rng.uniform(0.2, 0.8, (n, 1)) * e + u * (rng.uniform(lo, hi, (n, 1)) * core)
+
+
+def test_near_field_pairs_are_fp64():
+    """Targets 1-3 core radii from filaments.  The FP32 kernel's own position
+    rounding (6e-8 absolute at |x| ~ 1) is a ~1e-5 relative error at a few
+    core radii; the FP64 near-field correction recomputes those pairs from
+    FP64 positions.  What remains is the FP32 rounding of the other pairs and
+    of the tile sums that held the near terms (~1e-7 of the near term,
+    visible only where the target's total velocity cancels far below it).
+    (a) one ring: the near terms dominate the velocity; the error left is the
+        FP32 position rounding of the ring's other filaments (~1e-6 of the
+        total), several times below FP32's;
+    (b) 4096 random rings: typical errors well below FP32's, all below 1e-4."""
+    rng = np.random.default_rng(11)
+    corners, rvc, gam = random_rings(rng, 1)
+    corners = corners * 0 + np.array([[0.3, 0.4, 0.5], [0.33, 0.4, 0.5], [0.33, 0.43, 0.5], [0.3, 0.43, 0.5]])
+    P = _near_targets(rng, corners, 400)
+    V64 = O.vind_rings(corners, rvc, gam, P)
+    scale = np.linalg.norm(V64, axis=1)
+    err32 = np.linalg.norm(lib.biot_savart_rings(corners, rvc, gam, P, lib.PREC_FP32) - V64, axis=1) / scale
+    errn = np.linalg.norm(lib.biot_savart_rings(corners, rvc, gam, P, lib.PREC_FP32_NEAR64) - V64, axis=1) / scale
+    assert errn.max() < 5e-6, errn.max()
+    assert err32.max() > 5 * errn.max(), (err32.max(), errn.max())
+
+    corners, rvc, gam = random_rings(rng, 4096)
+    P = _near_targets(rng, corners, 600)
     V64 = O.vind_rings(corners, rvc, gam, P)
     scale = np.linalg.norm(V64, axis=1)
     err32 = np.linalg.norm(lib.biot_savart_rings(corners, rvc, gam, P, lib.PREC_FP32) - V64, axis=1) / scale
     errn = np.linalg.norm(lib.biot_savart_rings(corners, rvc, gam, P, lib.PREC_FP32_NEAR64) - V64, axis=1) / scale
     assert errn.max() < 1e-4, errn.max()
-    assert errn.max() < 0.25 * err32.max(), (errn.max(), err32.max())
+    assert np.median(errn) < 0.5 * np.median(err32), (np.median(errn), np.median(err32))
 
 
 def test_edge_cases():
