@@ -23,15 +23,16 @@
 // Near field (VLM_PREC_FP32_NEAR64): the FP32 kernel sums every pair; the
 // pairs within near_factor core radii of a filament segment -- where the
 // FP32 cross product and Vatistas denominator lose digits -- are then
-// corrected to FP64 outside the hot loop.  A hash grid over the records'
-// near-zone bounding boxes (cell size = the largest box, so a box covers at
-// most 2 x 2 x 2 cells) gives each target the few records whose zones can
-// contain it; for every near filament of those, k_near_fix recomputes the
-// FP32 kernel's own contribution bit for bit (same inline arithmetic, same
-// FP32 inputs) and adds FP64 value - FP32 contribution to order-independent
-// fixed-point accumulators, which k_near_apply folds into the chunk partial
-// sums.  The result equals summing the far pairs in FP32 and the near pairs
-// in FP64, up to the FP32 rounding of the tile sums that held the near terms.
+// corrected to FP64 outside the hot loop.  The targets are binned into a
+// hashed uniform grid (cell size twice the mean near-zone radius); every
+// near-zone filament, cut into pieces no longer than a cell, visits the
+// cells around each piece and tests their targets.  For every near pair
+// k_near_fix recomputes the FP32 kernel's own contribution bit for bit (same
+// inline arithmetic, same FP32 inputs) and adds FP64 value - FP32
+// contribution to order-independent fixed-point accumulators, which
+// k_near_apply folds into the chunk partial sums.  The result equals summing
+// the far pairs in FP32 and the near pairs in FP64, up to the FP32 rounding
+// of the tile sums that held the near terms.
 #include <stdint.h>
 
 #include <algorithm>
@@ -348,112 +349,79 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
 }
 
 
-// ---- near field: hash grid over the records' near zones -----------------
-// Scratch layout: grid_layout (vlm_bs.h).  The box of record r is [8 r ..]:
-// min xyz, max xyz (min > max: no near zone); the bucket counts become the
-// fill cursors after the scan.
+// ---- near field: hashed uniform grid over the targets ---------------------
+// Scratch layout: grid_layout (vlm_bs.h): header, [T] bucket counts (the
+// fill cursors after the scan), [T + 1] bucket starts, [M] target indices.
+
 __device__ __forceinline__ unsigned cell_hash(int ix, int iy, int iz, int T) {
   return ((unsigned)ix * 73856093u ^ (unsigned)iy * 19349663u ^ (unsigned)iz * 83492791u) & (unsigned)(T - 1);
 }
-__device__ __forceinline__ int cell_of(float x, float invh) { return (int)floorf(x * invh); }
+// saturating conversion: coordinates far outside the grid stay finite ints
+__device__ __forceinline__ int cell_of(float x, float invh) { return __float2int_rd(x * invh); }
 
-// Bounding box of the record's active near zones: every filament k with a
-// near threshold ([32 + k] >= 0) contributes its segment grown by 1.5 x its
-// zone radius near_factor rvc_k = sqrt([32 + k]) / |e_k| (the zone is the
-// segment's cylinder of that radius, extended by it at both ends), in FP64
-// from the record's corners, rounded outwards to FP32.
-__global__ void k_grid_bbox(const float* __restrict__ rec32, const double* __restrict__ rec64, int nrec,
-                            unsigned char* __restrict__ scratch) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nrec) return;
+__global__ void k_grid_init(unsigned char* scratch, int T) {
   GridHdr* H = reinterpret_cast<GridHdr*>(scratch);
-  const GridLayout L = grid_layout(nrec);
-  float* bb = reinterpret_cast<float*>(scratch + L.bbox) + 8 * (size_t)i;
-  const float* R = rec32 + (size_t)i * kRec32;
-  const double* D = rec64 + (size_t)i * kRec64;
-  const bool fil = (int)D[17] & REC_FIL;
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  bool any = false;
-  for (int k = 0; k < 4; ++k) {
-    const float thr = R[32 + k];
-    if (!(thr >= 0.f)) continue;
-    const int j = (k + 1) & 3;
-    const int sk = fil ? (k == 1 || k == 2 ? 1 : 0) : k, sj = fil ? (j == 1 || j == 2 ? 1 : 0) : j;
-    const double ax = D[3 * sk], ay = D[3 * sk + 1], az = D[3 * sk + 2];
-    const double bx = D[3 * sj], by = D[3 * sj + 1], bz = D[3 * sj + 2];
-    const double ee = (bx - ax) * (bx - ax) + (by - ay) * (by - ay) + (bz - az) * (bz - az);
-    if (!(ee > 0.0)) continue;
-    const double z = 1.5 * sqrt((double)thr / ee) + 1e-7;
-    lo[0] = fmin(lo[0], fmin(ax, bx) - z), hi[0] = fmax(hi[0], fmax(ax, bx) + z);
-    lo[1] = fmin(lo[1], fmin(ay, by) - z), hi[1] = fmax(hi[1], fmax(ay, by) + z);
-    lo[2] = fmin(lo[2], fmin(az, bz) - z), hi[2] = fmax(hi[2], fmax(az, bz) + z);
-    any = true;
-  }
-  if (!any) {
-    bb[0] = 1.f, bb[3] = -1.f;
-    return;
-  }
-  float ext = 0.f;
-  for (int a = 0; a < 3; ++a) {
-    bb[a] = __double2float_rd(lo[a]);
-    bb[3 + a] = __double2float_ru(hi[a]);
-    ext = fmaxf(ext, bb[3 + a] - bb[a]);
-  }
-  atomicMax(&H->hbits, __float_as_uint(ext));  // non-negative floats order as their bits
+  H->zsum = 0.0;
+  H->zcount = 0u;
+  H->T = T;
 }
 
-// The buckets of the cells a box overlaps, each once.  The cell size is 1 %
-// above the largest box, so a box overlaps at most 2 cells per axis; the
-// enumeration allows 3 (FP32 rounding of coordinates more than ~10^5 cells
-// from the origin) and the fill checks the entry capacity.
-constexpr int kMaxBoxBuckets = 27;
-__device__ __forceinline__ int box_buckets(const float* bb, float invh, int T, unsigned (&out)[kMaxBoxBuckets]) {
-  const int x0 = cell_of(bb[0], invh), x1 = min(cell_of(bb[3], invh), x0 + 2);
-  const int y0 = cell_of(bb[1], invh), y1 = min(cell_of(bb[4], invh), y0 + 2);
-  const int z0 = cell_of(bb[2], invh), z1 = min(cell_of(bb[5], invh), z0 + 2);
-  int n = 0;
-  for (int x = x0; x <= x1; ++x)
-    for (int y = y0; y <= y1; ++y)
-      for (int z = z0; z <= z1; ++z) {
-        const unsigned h = cell_hash(x, y, z, T);
-        bool dup = false;
-        for (int k = 0; k < n; ++k) dup |= out[k] == h;
-        if (!dup) out[n++] = h;
-      }
-  return n;
-}
-
-__device__ __forceinline__ float grid_invh(const GridHdr* H) {
-  const float h = __uint_as_float(H->hbits) * 1.01f;
-  return h > 0.f ? 1.f / h : 0.f;
-}
-
-// FILL = false: count the records per bucket; true: write them
-template <bool FILL>
-__global__ void k_grid_insert(int nrec, unsigned char* __restrict__ scratch) {
+// Sum and count of the near-zone radii near_factor rvc_k = sqrt([32 + k]) /
+// |e_k| of the active filaments (the cell size is twice their mean).
+__global__ void k_zone_mean(const float* __restrict__ rec32, int nrec, unsigned char* __restrict__ scratch) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nrec) return;
-  const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
-  const GridLayout L = grid_layout(nrec);
-  const float* bb = reinterpret_cast<const float*>(scratch + L.bbox) + 8 * (size_t)i;
-  if (!(bb[0] <= bb[3])) return;
-  int* count = reinterpret_cast<int*>(scratch + L.count);
-  unsigned b[kMaxBoxBuckets];
-  const int n = box_buckets(bb, grid_invh(H), H->T, b);
-  for (int k = 0; k < n; ++k) {
-    if (!FILL) {
-      atomicAdd(count + b[k], 1);
-    } else {
-      const int slot = atomicAdd(count + b[k], 1);
-      if (slot < 8 * nrec) reinterpret_cast<int*>(scratch + L.entry)[slot] = i;
+  double z = 0.0;
+  unsigned c = 0u;
+  if (i < nrec) {
+    const float* R = rec32 + (size_t)i * kRec32;
+    for (int k = 0; k < 4; ++k) {
+      const float thr = R[32 + k];
+      if (!(thr >= 0.f)) continue;
+      const int j = (k + 1) & 3;
+      const float ex = R[3 * j] - R[3 * k], ey = R[3 * j + 1] - R[3 * k + 1], ez = R[3 * j + 2] - R[3 * k + 2];
+      const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+      if (!(ee > 0.f)) continue;
+      z += sqrt((double)thr / (double)ee);
+      ++c;
     }
   }
+  // one atomic pair per warp
+  for (int o = 16; o > 0; o >>= 1) {
+    z += __shfl_down_sync(kFull, z, o);
+    c += __shfl_down_sync(kFull, c, o);
+  }
+  if ((threadIdx.x & 31) == 0 && c) {
+    GridHdr* H = reinterpret_cast<GridHdr*>(scratch);
+    atomicAdd(&H->zsum, z);
+    atomicAdd(&H->zcount, c);
+  }
+}
+
+__device__ __forceinline__ float grid_h(const GridHdr* H) {
+  return H->zcount ? (float)(2.0 * H->zsum / (double)H->zcount) : 0.f;
+}
+
+// FILL = false: count the targets per bucket; true: write their indices
+template <bool FILL>
+__global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned char* __restrict__ scratch) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
+  const float h = grid_h(H);
+  if (!(h > 0.f)) return;
+  const float invh = 1.f / h;
+  const GridLayout L = grid_layout(M);
+  int* count = reinterpret_cast<int*>(scratch + L.count);
+  const unsigned b = cell_hash(cell_of((float)P[3 * (size_t)m], invh), cell_of((float)P[3 * (size_t)m + 1], invh),
+                               cell_of((float)P[3 * (size_t)m + 2], invh), H->T);
+  const int slot = atomicAdd(count + b, 1);
+  if (FILL) reinterpret_cast<int*>(scratch + L.entry)[slot] = m;
 }
 
 // Exclusive scan of the bucket counts into start[0..T]; the counts become
-// the fill cursors (= start).  One block.
-__global__ void k_grid_scan(int nrec, unsigned char* __restrict__ scratch) {
-  const GridLayout L = grid_layout(nrec);
+// the fill cursors (= start).  One block of 1024 threads.
+__global__ void k_grid_scan(int M, unsigned char* __restrict__ scratch) {
+  const GridLayout L = grid_layout(M);
   const int T = reinterpret_cast<const GridHdr*>(scratch)->T;
   int* count = reinterpret_cast<int*>(scratch + L.count);
   int* start = reinterpret_cast<int*>(scratch + L.start);
@@ -464,29 +432,21 @@ __global__ void k_grid_scan(int nrec, unsigned char* __restrict__ scratch) {
   for (int b = b0; b < b1; ++b) sum += count[b];
   part[threadIdx.x] = sum;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int t = 0; t < (int)blockDim.x; ++t) {
-      const int v = part[t];
-      part[t] = acc;
-      acc += v;
-    }
-    start[T] = acc;
+  // Hillis-Steele inclusive scan of the per-thread sums
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
   }
-  __syncthreads();
-  int acc = part[threadIdx.x];
+  int acc = part[threadIdx.x] - sum;
+  if (threadIdx.x == blockDim.x - 1) start[T] = part[threadIdx.x];
   for (int b = b0; b < b1; ++b) {
     const int c = count[b];
     start[b] = acc;
     count[b] = acc;
     acc += c;
   }
-}
-
-__global__ void k_grid_init(unsigned char* scratch, int T) {
-  GridHdr* H = reinterpret_cast<GridHdr*>(scratch);
-  H->hbits = 0u;
-  H->T = T;
 }
 
 // FP64 filament velocity (src/classdef.f90:476-503: the Vatistas n=2 kernel
@@ -503,81 +463,113 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
   return c * (d * rsqrt(s2 * s2 + c2 * c2) * kInv4Pi);
 }
 
-// One thread per target: the records of the target's bucket whose near-zone
-// box holds it; for each of their filaments with the target inside the near
-// zone -- |r_k x r_j|^2 < (near_factor rvc |e|)^2 and the projection within
-// the segment extended by near_factor rvc, tested on the FP32 kernel's own
-// FP32 values -- the correction FP64 velocity x weight - the FP32 kernel's
-// contribution f (r_k x r_j) (recomputed with the same FP32 operations, the
-// product taken exactly in FP64) goes to the fixed-point accumulator of the
-// target and the record's chunk.  ctl[1] counts the corrected pairs, ctl[0]
-// = 4 flags a correction outside the fixed-point range.
+// One warp per record.  Every filament k with a near zone (radius
+// z = near_factor rvc_k, from [32 + k]) is cut into np pieces no longer than
+// a cell; the lanes visit the cells of each piece's box (grown by 1.42 z,
+// which holds the zone's cylinder and its extensions past the ends) and test
+// the targets binned there.  A target is taken only in its own cell (not a
+// hash collision) and only by the piece that holds its projection on the
+// filament, so every (target, filament) pair is tested once.  A near pair --
+// |r_k x r_j|^2 < (near_factor rvc |e|)^2 and the projection within the
+// segment extended by near_factor rvc, on the FP32 kernel's own FP32 values
+// -- adds FP64 velocity x weight - the FP32 kernel's contribution
+// f (r_k x r_j) (recomputed with the same FP32 operations, the product taken
+// exactly in FP64) to the fixed-point accumulator of the target and the
+// record's chunk.  ctl[1] counts the corrected pairs, ctl[0] = 4 flags a
+// correction outside the fixed-point range.
 __global__ void k_near_fix(const float* __restrict__ rec32, const double* __restrict__ rec64, int nrec,
                            const double* __restrict__ ew, const Chunk* __restrict__ chunks, int nchunks,
                            const double* __restrict__ P, int M, const unsigned char* __restrict__ scratch,
                            unsigned long long* __restrict__ nacc, int* __restrict__ ctl) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= M) return;
+  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= nrec) return;
   const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
-  const float invh = grid_invh(H);
-  if (!(invh > 0.f)) return;  // no near zone anywhere
-  const GridLayout L = grid_layout(nrec);
-  const float* bbox = reinterpret_cast<const float*>(scratch + L.bbox);
+  const float h = grid_h(H);
+  if (!(h > 0.f)) return;
+  const float invh = 1.f / h;
+  const int T = H->T;
+  const GridLayout L = grid_layout(M);
   const int* start = reinterpret_cast<const int*>(scratch + L.start);
   const int* entry = reinterpret_cast<const int*>(scratch + L.entry);
-  const double p64x = P[3 * (size_t)m], p64y = P[3 * (size_t)m + 1], p64z = P[3 * (size_t)m + 2];
-  const float px = (float)p64x, py = (float)p64y, pz = (float)p64z;  // as the FP32 kernel
-  if (start[H->T] > 8 * nrec) {  // more bucket entries than the scratch holds
-    if (m == 0) atomicExch(ctl, 3);
-    return;
+  const float* R = rec32 + (size_t)r * kRec32;
+  const double* D = rec64 + (size_t)r * kRec64;
+  const bool fil = (int)D[17] & REC_FIL;
+  RecView v;
+  load_view(reinterpret_cast<const float4*>(R), v);
+  // the record's chunk (chunks are in record order)
+  int q = 0;
+  {
+    int hi = nchunks - 1;
+    while (q < hi) {
+      const int mid = (q + hi + 1) >> 1;
+      if (chunks[mid].rec_begin <= r) q = mid;
+      else hi = mid - 1;
+    }
   }
-  const unsigned b = cell_hash(cell_of(px, invh), cell_of(py, invh), cell_of(pz, invh), H->T);
   int found = 0;
-  for (int e = start[b]; e < start[b + 1]; ++e) {
-    const int r = entry[e];
-    const float* bb = bbox + 8 * (size_t)r;
-    if (!(px >= bb[0] && px <= bb[3] && py >= bb[1] && py <= bb[4] && pz >= bb[2] && pz <= bb[5])) continue;
-    const float* R = rec32 + (size_t)r * kRec32;
-    RecView v;
-    load_view(reinterpret_cast<const float4*>(R), v);
-    for (int k = 0; k < 4; ++k) {
-      const float thr = R[32 + k];
-      if (!(thr >= 0.f)) continue;
-      const int j = (k + 1) & 3;
-      float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
-      corner_vector(px, py, pz, R[3 * k], R[3 * k + 1], R[3 * k + 2], rxk, ryk, rzk, invk);
-      corner_vector(px, py, pz, R[3 * j], R[3 * j + 1], R[3 * j + 2], rxj, ryj, rzj, invj);
-      const Fil32 t = fil_terms(v.ex[k], v.ey[k], v.ez[k], v.eev[k], v.a4v[k], rxk, ryk, rzk, invk, rxj, ryj, rzj, invj);
-      if (!(t.c2 < thr && t.c2 > kS2Min && t.tt > R[36 + k] && t.tt < R[40 + k])) continue;
-      // FP64 value of the same filament pair
-      const double* D = rec64 + (size_t)r * kRec64;
-      const d3 p = mk3(p64x, p64y, p64z);
-      d3 v64;
-      if ((int)D[17] & REC_FIL) {
-        v64 = fil_near64(p, mk3(D[0], D[1], D[2]), mk3(D[3], D[4], D[5]), D[12]);
-      } else {
-        v64 = fil_near64(p, mk3(D[3 * k], D[3 * k + 1], D[3 * k + 2]), mk3(D[3 * j], D[3 * j + 1], D[3 * j + 2]),
-                         D[12 + k]);
-      }
-      v64 = v64 * (ew ? ew[4 * (size_t)r + k] : D[16]);
-      const double c[3] = {v64.x - (double)t.f * (double)t.kx, v64.y - (double)t.f * (double)t.ky,
-                           v64.z - (double)t.f * (double)t.kz};
-      // the record's chunk (chunks are in record order)
-      int lo = 0, hi = nchunks - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (chunks[mid].rec_begin <= r) lo = mid;
-        else hi = mid - 1;
-      }
-      unsigned long long* o = nacc + ((size_t)lo * M + m) * 3;
-      for (int a = 0; a < 3; ++a) {
-        if (!(fabs(c[a]) < kNearMax)) {
-          atomicExch(ctl, 4);
-          continue;
+  for (int k = 0; k < 4; ++k) {
+    const float thr = R[32 + k];
+    if (!(thr >= 0.f)) continue;
+    const int j = (k + 1) & 3;
+    const float ax = R[3 * k], ay = R[3 * k + 1], az = R[3 * k + 2];
+    const float ex = R[3 * j] - ax, ey = R[3 * j + 1] - ay, ez = R[3 * j + 2] - az;
+    const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    if (!(ee > 0.f) || !(v.eev[k] != 0.f)) continue;
+    const float len = sqrtf(ee);
+    const float z = sqrtf(thr) / len;
+    const int np = max(1, min(4096, (int)ceilf(len * invh)));
+    const float amax = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az)) + len;
+    const float grow = 1.42f * z * 1.0001f + 1e-6f + 4e-7f * amax;
+    for (int pc = 0; pc < np; ++pc) {
+      const float t0 = (float)pc / np, t1 = (float)(pc + 1) / np;
+      const float qx0 = fmaf(ex, t0, ax), qy0 = fmaf(ey, t0, ay), qz0 = fmaf(ez, t0, az);
+      const float qx1 = fmaf(ex, t1, ax), qy1 = fmaf(ey, t1, ay), qz1 = fmaf(ez, t1, az);
+      const int x0 = cell_of(fminf(qx0, qx1) - grow, invh), x1 = cell_of(fmaxf(qx0, qx1) + grow, invh);
+      const int y0 = cell_of(fminf(qy0, qy1) - grow, invh), y1 = cell_of(fmaxf(qy0, qy1) + grow, invh);
+      const int z0 = cell_of(fminf(qz0, qz1) - grow, invh), z1 = cell_of(fmaxf(qz0, qz1) + grow, invh);
+      const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+      const long long ncell = (long long)nx * ny * nz;
+      for (long long ci = lane; ci < ncell; ci += 32) {
+        const int cx = x0 + (int)(ci % nx), cy = y0 + (int)((ci / nx) % ny), cz = z0 + (int)(ci / ((long long)nx * ny));
+        const unsigned b = cell_hash(cx, cy, cz, T);
+        for (int e = start[b]; e < start[b + 1]; ++e) {
+          const int m = entry[e];
+          const double p64x = P[3 * (size_t)m], p64y = P[3 * (size_t)m + 1], p64z = P[3 * (size_t)m + 2];
+          const float px = (float)p64x, py = (float)p64y, pz = (float)p64z;  // as the FP32 kernel
+          if (cell_of(px, invh) != cx || cell_of(py, invh) != cy || cell_of(pz, invh) != cz) continue;
+          float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
+          corner_vector(px, py, pz, ax, ay, az, rxk, ryk, rzk, invk);
+          corner_vector(px, py, pz, R[3 * j], R[3 * j + 1], R[3 * j + 2], rxj, ryj, rzj, invj);
+          const Fil32 t = fil_terms(v.ex[k], v.ey[k], v.ez[k], v.eev[k], v.a4v[k], rxk, ryk, rzk, invk, rxj, ryj, rzj,
+                                    invj);
+          // the piece that holds the target's projection takes the pair
+          const int own = max(0, min(np - 1, __float2int_rd(t.tt / v.eev[k] * (float)np)));
+          if (own != pc) continue;
+          if (!(t.c2 < thr && t.c2 > kS2Min && t.tt > R[36 + k] && t.tt < R[40 + k])) continue;
+          // FP64 value of the same filament pair
+          const d3 p = mk3(p64x, p64y, p64z);
+          d3 v64;
+          if (fil) {
+            v64 = fil_near64(p, mk3(D[0], D[1], D[2]), mk3(D[3], D[4], D[5]), D[12]);
+          } else {
+            v64 = fil_near64(p, mk3(D[3 * k], D[3 * k + 1], D[3 * k + 2]), mk3(D[3 * j], D[3 * j + 1], D[3 * j + 2]),
+                             D[12 + k]);
+          }
+          v64 = v64 * (ew ? ew[4 * (size_t)r + k] : D[16]);
+          const double c[3] = {v64.x - (double)t.f * (double)t.kx, v64.y - (double)t.f * (double)t.ky,
+                               v64.z - (double)t.f * (double)t.kz};
+          unsigned long long* o = nacc + ((size_t)q * M + m) * 3;
+          for (int a = 0; a < 3; ++a) {
+            if (!(fabs(c[a]) < kNearMax)) {
+              atomicExch(ctl, 4);
+              continue;
+            }
+            atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
+          }
+          ++found;
         }
-        atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
       }
-      ++found;
     }
   }
   if (found) atomicAdd(ctl + 1, found);
@@ -691,26 +683,26 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   if (ew) k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
   else k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
   if (!near_scratch || nrec <= 0) return;
-  // near field: grid over the records' near zones, FP64 corrections of the
-  // near pairs, corrections folded into the partial sums
-  if (near_bytes < near_grid_bytes(nrec)) {
+  // near field: targets binned in a grid, FP64 corrections of the near
+  // pairs, corrections folded into the partial sums
+  if (near_bytes < near_grid_bytes(M)) {
     count_launch();
     k_set_flag<<<1, 1, 0, s>>>(ctl, 3);
     return;
   }
   unsigned char* g = static_cast<unsigned char*>(near_scratch);
-  const GridLayout L = grid_layout(nrec);
-  const int T = grid_buckets(nrec);
-  const int rb = (nrec + 255) / 256;
+  const GridLayout L = grid_layout(M);
+  const int T = grid_buckets(M);
   count_launches(6);
   k_grid_init<<<1, 1, 0, s>>>(g, T);
-  k_grid_bbox<<<rb, 256, 0, s>>>(rec32, rec64, nrec, g);
+  k_zone_mean<<<(nrec + 255) / 256, 256, 0, s>>>(rec32, nrec, g);
   cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), s);
-  k_grid_insert<false><<<rb, 256, 0, s>>>(nrec, g);
-  k_grid_scan<<<1, 1024, 0, s>>>(nrec, g);
-  k_grid_insert<true><<<rb, 256, 0, s>>>(nrec, g);
-  k_near_fix<<<(M + 127) / 128, 128, 0, s>>>(rec32, rec64, nrec, ew, chunks, nchunks, P, M, g,
-                                             reinterpret_cast<unsigned long long*>(nacc), ctl);
+  k_tgrid_insert<false><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
+  k_grid_scan<<<1, 1024, 0, s>>>(M, g);
+  k_tgrid_insert<true><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
+  k_near_fix<<<(unsigned)(((size_t)nrec * 32 + 255) / 256), 256, 0, s>>>(rec32, rec64, nrec, ew, chunks, nchunks, P, M,
+                                                                         g, reinterpret_cast<unsigned long long*>(nacc),
+                                                                         ctl);
   const size_t n = (size_t)M * nchunks * 3;
   count_launch();
   k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * device_sm_count()), 256, 0, s>>>(part, nacc,

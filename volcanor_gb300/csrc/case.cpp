@@ -368,7 +368,7 @@ struct Case {
     s.targets = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.outv = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.part = dalloc<double>((size_t)maxPart * 3, scratchOwned);
-    s.nearBytes = opt.precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes(maxRecords) : 0;
+    s.nearBytes = opt.precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes(maxTargets) : 0;
     s.nearScratch = s.nearBytes ? dalloc<unsigned char>(s.nearBytes, scratchOwned) : nullptr;
     // zero here; every near-field evaluation leaves them zero
     s.nacc = dalloc<long long>(opt.precision == VLM_PREC_FP32_NEAR64 ? (size_t)maxPart * 3 : 1, scratchOwned);
@@ -1365,7 +1365,7 @@ struct Case {
       } else {
         const bool nearOn = opt.precision == VLM_PREC_FP32_NEAR64;
         launch_pack32(rec64, rec, nearOn ? opt.near_factor : 0.0, rec32, stream);
-        const size_t nb = nearOn ? near_grid_bytes(rec) : 1;
+        const size_t nb = nearOn ? near_grid_bytes((int)M) : 1;
         unsigned char* ns = dalloc<unsigned char>(nb, tmpOwned);
         long long* nacc = dalloc<long long>(nearOn ? (size_t)M * nq * 3 : 1, tmpOwned);
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
@@ -1450,7 +1450,7 @@ int64_t ring_scratch_bytes(int64_t N, int64_t M, int precision) {
   const int64_t Q = std::max(1, ring_plan(N, M, precision, g, ch));
   int64_t b = N * kRec64 * 8 + M * Q * 3 * 8 + Q * (int64_t)sizeof(Chunk) + 64;
   if (precision != VLM_PREC_FP64) b += N * kRec32 * 4;
-  if (precision == VLM_PREC_FP32_NEAR64) b += (int64_t)near_grid_bytes((int)N) + M * Q * 3 * 8;
+  if (precision == VLM_PREC_FP32_NEAR64) b += (int64_t)near_grid_bytes((int)M) + M * Q * 3 * 8;
   return b;
 }
 
@@ -1485,7 +1485,7 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   grow((void**)&R.chunks, R.capChunks, (size_t)Q * sizeof(Chunk) + sizeof(Group) + 64);
   R.group = reinterpret_cast<Group*>(R.chunks + Q);
   if (!R.err) VLM_CUDA(cudaMalloc(&R.err, 4 * sizeof(int)));
-  const size_t nearBytes = precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes((int)std::max<int64_t>(N, 1)) : 1;
+  const size_t nearBytes = precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes((int)M) : 1;
   grow((void**)&R.near, R.capNear, nearBytes);
   if (precision == VLM_PREC_FP32_NEAR64 && (size_t)M * Q * 3 * 8 > R.capNacc) {
     grow((void**)&R.nacc, R.capNacc, (size_t)M * Q * 3 * 8);

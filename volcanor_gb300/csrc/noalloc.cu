@@ -31,7 +31,7 @@ constexpr size_t kOffRec64 = 0;
 constexpr size_t kOffRec32 = kOffRec64 + align256(kMaxRings * kRec64 * sizeof(double));
 constexpr size_t kOffPart = kOffRec32 + align256(kMaxRings * kRec32 * sizeof(float));
 constexpr size_t kOffNear = kOffPart + align256(kMaxPoints * 3 * sizeof(double));
-constexpr size_t kNearBytes = near_grid_bytes((int)kMaxRings);  // near-field grid for the largest N
+constexpr size_t kNearBytes = near_grid_bytes((int)kMaxPoints);  // near-field grid for the largest M
 constexpr size_t kOffNacc = kOffNear + align256(kNearBytes);
 constexpr size_t kOffTables = kOffNacc + align256(kMaxPoints * 3 * sizeof(long long));
 constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words

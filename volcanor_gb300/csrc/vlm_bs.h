@@ -64,35 +64,33 @@ constexpr int kRec32 = 48;
 #define VLM_BS_HD
 #endif
 
-// Near-field scratch of an evaluation over nrec records (a hash grid over
-// the records' near-zone boxes, carved from one caller buffer):
-//   header (cell size, bucket count), [nrec][8] box floats, [T] bucket
-//   counts, [T + 1] bucket starts, [8 nrec] entries (record indices),
-// T = the smallest power of two >= max(1024, 2 nrec).
+// Near-field scratch of an evaluation at M targets (a hashed uniform grid of
+// the targets, carved from one caller buffer): header, [T] bucket counts,
+// [T + 1] bucket starts, [M] target indices, T = the smallest power of two
+// >= max(1024, 2 M).
 struct GridHdr {
-  unsigned int hbits;  // cell size (the largest box extent) as float bits
+  double zsum;         // sum of the near-zone radii (the cell size is twice their mean)
+  unsigned int zcount;
   int T;               // bucket count
-  int pad[2];
 };
-VLM_BS_HD constexpr int grid_buckets(int nrec) {
+VLM_BS_HD constexpr int grid_buckets(int M) {
   int T = 1024;
-  while (T < 2 * nrec && T < (1 << 28)) T <<= 1;
+  while (T < 2 * M && T < (1 << 28)) T <<= 1;
   return T;
 }
 VLM_BS_HD constexpr size_t grid_align(size_t b) { return (b + 255) & ~size_t(255); }
 struct GridLayout {
-  size_t bbox, count, start, entry, total;
+  size_t count, start, entry, total;
 };
-VLM_BS_HD constexpr GridLayout grid_layout(int nrec) {
-  const size_t T = (size_t)grid_buckets(nrec);
-  const size_t bbox = grid_align(sizeof(GridHdr));
-  const size_t count = bbox + grid_align((size_t)nrec * 8 * sizeof(float));
+VLM_BS_HD constexpr GridLayout grid_layout(int M) {
+  const size_t T = (size_t)grid_buckets(M);
+  const size_t count = grid_align(sizeof(GridHdr));
   const size_t start = count + grid_align(T * sizeof(int));
   const size_t entry = start + grid_align((T + 1) * sizeof(int));
-  return GridLayout{bbox, count, start, entry, entry + grid_align((size_t)nrec * 8 * sizeof(int))};
+  return GridLayout{count, start, entry, entry + grid_align((size_t)M * sizeof(int))};
 }
-// Bytes of near-field scratch an evaluation over nrec records needs.
-VLM_BS_HD constexpr size_t near_grid_bytes(int nrec) { return grid_layout(nrec).total; }
+// Bytes of near-field scratch an evaluation at M targets needs.
+VLM_BS_HD constexpr size_t near_grid_bytes(int M) { return grid_layout(M).total; }
 
 // Fixed-point scale of the near-field accumulators: FP64 near-field
 // velocities are added as integers (v * 2^44, |v| < 2^18) so that their sum
@@ -141,7 +139,7 @@ int device_sm_count();
 void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,
                       cudaStream_t s);
 // FP32 pairs with FP64 accumulation over the nrec records the chunks cover.
-// When near_scratch is non-null (near_bytes >= near_grid_bytes(nrec)), the
+// When near_scratch is non-null (near_bytes >= near_grid_bytes(M)), the
 // pairs inside the records' near-field thresholds are then corrected to FP64
 // through the fixed-point accumulators nacc (M x nchunks x 3, zero on entry
 // and left zero on return).  ctl[0] receives a nonzero code if a bounded wait
