@@ -349,15 +349,41 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
 }
 
 
-// ---- near field: hashed uniform grid over the targets ---------------------
-// Scratch layout: grid_layout (vlm_bs.h): header, [T] bucket counts (the
-// fill cursors after the scan), [T + 1] bucket starts, [M] target indices.
+// ---- near field: uniform grid over the targets, occupied cells hashed -----
+// Scratch layout: grid_layout (vlm_bs.h).  A cell's key packs its three
+// coordinates (21 bits each, offset by 2^20); kEmptyKey marks a free slot.
+// Every target's cell is inserted by linear probing (atomicCAS); the slot's
+// targets are then listed contiguously (count, scan, fill).  A lookup of a
+// cell probes until it finds the key (the cell is occupied) or a free slot
+// (it is not), so empty cells cost one or two reads and a slot holds the
+// targets of one cell only.
+constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr int kCellBias = 1 << 20;
 
+__device__ __forceinline__ unsigned long long cell_key(int ix, int iy, int iz) {
+  return ((unsigned long long)(unsigned)(ix + kCellBias) & 0x1FFFFFull) |
+         (((unsigned long long)(unsigned)(iy + kCellBias) & 0x1FFFFFull) << 21) |
+         (((unsigned long long)(unsigned)(iz + kCellBias) & 0x1FFFFFull) << 42);
+}
 __device__ __forceinline__ unsigned cell_hash(int ix, int iy, int iz, int T) {
   return ((unsigned)ix * 73856093u ^ (unsigned)iy * 19349663u ^ (unsigned)iz * 83492791u) & (unsigned)(T - 1);
 }
-// saturating conversion: coordinates far outside the grid stay finite ints
-__device__ __forceinline__ int cell_of(float x, float invh) { return __float2int_rd(x * invh); }
+// saturating conversion, clamped to the key's 21-bit range
+__device__ __forceinline__ int cell_of(float x, float invh) {
+  return max(-kCellBias + 1, min(kCellBias - 2, __float2int_rd(x * invh)));
+}
+// the slot of cell (ix, iy, iz), or -1 if no target lies in it
+__device__ __forceinline__ int cell_slot(const unsigned long long* __restrict__ key, int T, int ix, int iy, int iz) {
+  const unsigned long long k = cell_key(ix, iy, iz);
+  unsigned b = cell_hash(ix, iy, iz, T);
+  for (int n = 0; n < T; ++n) {
+    const unsigned long long v = key[b];
+    if (v == k) return (int)b;
+    if (v == kEmptyKey) return -1;
+    b = (b + 1) & (unsigned)(T - 1);
+  }
+  return -1;
+}
 
 __global__ void k_grid_init(unsigned char* scratch, int T) {
   GridHdr* H = reinterpret_cast<GridHdr*>(scratch);
@@ -401,8 +427,9 @@ __device__ __forceinline__ float grid_h(const GridHdr* H) {
   return H->zcount ? (float)(2.0 * H->zsum / (double)H->zcount) : 0.f;
 }
 
-// FILL = false: count the targets per bucket; true: write their indices
-template <bool FILL>
+// PASS 0: insert the target's cell key and count the target in its slot;
+// PASS 1: write the target's index at its slot's cursor.
+template <int PASS>
 __global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned char* __restrict__ scratch) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= M) return;
@@ -410,43 +437,73 @@ __global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned cha
   const float h = grid_h(H);
   if (!(h > 0.f)) return;
   const float invh = 1.f / h;
+  const int T = H->T;
   const GridLayout L = grid_layout(M);
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(scratch + L.key);
   int* count = reinterpret_cast<int*>(scratch + L.count);
-  const unsigned b = cell_hash(cell_of((float)P[3 * (size_t)m], invh), cell_of((float)P[3 * (size_t)m + 1], invh),
-                               cell_of((float)P[3 * (size_t)m + 2], invh), H->T);
-  const int slot = atomicAdd(count + b, 1);
-  if (FILL) reinterpret_cast<int*>(scratch + L.entry)[slot] = m;
+  const int ix = cell_of((float)P[3 * (size_t)m], invh), iy = cell_of((float)P[3 * (size_t)m + 1], invh),
+            iz = cell_of((float)P[3 * (size_t)m + 2], invh);
+  if (PASS == 0) {
+    const unsigned long long k = cell_key(ix, iy, iz);
+    unsigned b = cell_hash(ix, iy, iz, T);
+    // T >= 2 M: a free slot always exists
+    for (int n = 0; n < T; ++n) {
+      const unsigned long long old = atomicCAS(key + b, kEmptyKey, k);
+      if (old == kEmptyKey || old == k) {
+        atomicAdd(count + b, 1);
+        return;
+      }
+      b = (b + 1) & (unsigned)(T - 1);
+    }
+  } else {
+    const int b = cell_slot(key, T, ix, iy, iz);
+    const int slot = atomicAdd(count + b, 1);
+    reinterpret_cast<int*>(scratch + L.entry)[slot] = m;
+  }
 }
 
-// Exclusive scan of the bucket counts into start[0..T]; the counts become
-// the fill cursors (= start).  One block of 1024 threads.
+// Exclusive scan of the slot counts into start[0..T]; the counts become the
+// fill cursors (= start).  One block of 1024 threads: tiles of 1024 slots,
+// each scanned with warp shuffles, carried from tile to tile.
 __global__ void k_grid_scan(int M, unsigned char* __restrict__ scratch) {
   const GridLayout L = grid_layout(M);
   const int T = reinterpret_cast<const GridHdr*>(scratch)->T;
   int* count = reinterpret_cast<int*>(scratch + L.count);
   int* start = reinterpret_cast<int*>(scratch + L.start);
-  __shared__ int part[1024];
-  const int per = (T + blockDim.x - 1) / blockDim.x;
-  const int b0 = threadIdx.x * per, b1 = min(T, b0 + per);
-  int sum = 0;
-  for (int b = b0; b < b1; ++b) sum += count[b];
-  part[threadIdx.x] = sum;
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
   __syncthreads();
-  // Hillis-Steele inclusive scan of the per-thread sums
-  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-    const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+  for (int base = 0; base < T; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int c = i < T ? count[i] : 0;
+    int x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
     __syncthreads();
-    part[threadIdx.x] += v;
+    if (warp == 0) {
+      int w = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const int excl = carry + (warp ? wsum[warp - 1] : 0) + x - c;
+    if (i < T) {
+      start[i] = excl;
+      count[i] = excl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += wsum[31];
     __syncthreads();
   }
-  int acc = part[threadIdx.x] - sum;
-  if (threadIdx.x == blockDim.x - 1) start[T] = part[threadIdx.x];
-  for (int b = b0; b < b1; ++b) {
-    const int c = count[b];
-    start[b] = acc;
-    count[b] = acc;
-    acc += c;
-  }
+  if (threadIdx.x == 0) start[T] = carry;
 }
 
 // FP64 filament velocity (src/classdef.f90:476-503: the Vatistas n=2 kernel
@@ -467,8 +524,9 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
 // z = near_factor rvc_k, from [32 + k]) is cut into np pieces no longer than
 // a cell; the lanes visit the cells of each piece's box (grown by 1.42 z,
 // which holds the zone's cylinder and its extensions past the ends) and test
-// the targets binned there.  A target is taken only in its own cell (not a
-// hash collision) and only by the piece that holds its projection on the
+// the targets binned there (cells whose centre is farther from the piece than
+// sqrt(2) z + half a cell diagonal are skipped, empty cells cost one probe).
+// A target is taken only by the piece that holds its projection on the
 // filament, so every (target, filament) pair is tested once.  A near pair --
 // |r_k x r_j|^2 < (near_factor rvc |e|)^2 and the projection within the
 // segment extended by near_factor rvc, on the FP32 kernel's own FP32 values
@@ -490,6 +548,7 @@ __global__ void k_near_fix(const float* __restrict__ rec32, const double* __rest
   const float invh = 1.f / h;
   const int T = H->T;
   const GridLayout L = grid_layout(M);
+  const unsigned long long* key = reinterpret_cast<const unsigned long long*>(scratch + L.key);
   const int* start = reinterpret_cast<const int*>(scratch + L.start);
   const int* entry = reinterpret_cast<const int*>(scratch + L.entry);
   const float* R = rec32 + (size_t)r * kRec32;
@@ -521,10 +580,17 @@ __global__ void k_near_fix(const float* __restrict__ rec32, const double* __rest
     const int np = max(1, min(4096, (int)ceilf(len * invh)));
     const float amax = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az)) + len;
     const float grow = 1.42f * z * 1.0001f + 1e-6f + 4e-7f * amax;
+    // cells whose centre lies farther than sqrt(2) z (the zone's extension
+    // past the ends) + half a cell diagonal from the piece cannot hold a
+    // target of the zone
+    const float reach = 1.4143f * z * 1.0001f + 0.8661f * h + 1e-6f + 4e-7f * amax;
+    const float reach2 = reach * reach;
     for (int pc = 0; pc < np; ++pc) {
       const float t0 = (float)pc / np, t1 = (float)(pc + 1) / np;
       const float qx0 = fmaf(ex, t0, ax), qy0 = fmaf(ey, t0, ay), qz0 = fmaf(ez, t0, az);
       const float qx1 = fmaf(ex, t1, ax), qy1 = fmaf(ey, t1, ay), qz1 = fmaf(ez, t1, az);
+      const float sx = qx1 - qx0, sy = qy1 - qy0, sz = qz1 - qz0;
+      const float ss = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
       const int x0 = cell_of(fminf(qx0, qx1) - grow, invh), x1 = cell_of(fmaxf(qx0, qx1) + grow, invh);
       const int y0 = cell_of(fminf(qy0, qy1) - grow, invh), y1 = cell_of(fmaxf(qy0, qy1) + grow, invh);
       const int z0 = cell_of(fminf(qz0, qz1) - grow, invh), z1 = cell_of(fmaxf(qz0, qz1) + grow, invh);
@@ -532,12 +598,17 @@ __global__ void k_near_fix(const float* __restrict__ rec32, const double* __rest
       const long long ncell = (long long)nx * ny * nz;
       for (long long ci = lane; ci < ncell; ci += 32) {
         const int cx = x0 + (int)(ci % nx), cy = y0 + (int)((ci / nx) % ny), cz = z0 + (int)(ci / ((long long)nx * ny));
-        const unsigned b = cell_hash(cx, cy, cz, T);
+        // distance from the cell centre to the piece
+        const float gx = ((float)cx + 0.5f) * h - qx0, gy = ((float)cy + 0.5f) * h - qy0, gz = ((float)cz + 0.5f) * h - qz0;
+        const float tq = ss > 0.f ? fminf(fmaxf(fmaf(gx, sx, fmaf(gy, sy, gz * sz)) / ss, 0.f), 1.f) : 0.f;
+        const float dx = fmaf(-tq, sx, gx), dy = fmaf(-tq, sy, gy), dz = fmaf(-tq, sz, gz);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > reach2) continue;
+        const int b = cell_slot(key, T, cx, cy, cz);
+        if (b < 0) continue;
         for (int e = start[b]; e < start[b + 1]; ++e) {
           const int m = entry[e];
           const double p64x = P[3 * (size_t)m], p64y = P[3 * (size_t)m + 1], p64z = P[3 * (size_t)m + 2];
           const float px = (float)p64x, py = (float)p64y, pz = (float)p64z;  // as the FP32 kernel
-          if (cell_of(px, invh) != cx || cell_of(py, invh) != cy || cell_of(pz, invh) != cz) continue;
           float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
           corner_vector(px, py, pz, ax, ay, az, rxk, ryk, rzk, invk);
           corner_vector(px, py, pz, R[3 * j], R[3 * j + 1], R[3 * j + 2], rxj, ryj, rzj, invj);
@@ -696,10 +767,11 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   count_launches(6);
   k_grid_init<<<1, 1, 0, s>>>(g, T);
   k_zone_mean<<<(nrec + 255) / 256, 256, 0, s>>>(rec32, nrec, g);
+  cudaMemsetAsync(g + L.key, 0xFF, (size_t)T * sizeof(unsigned long long), s);
   cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), s);
-  k_tgrid_insert<false><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
+  k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
   k_grid_scan<<<1, 1024, 0, s>>>(M, g);
-  k_tgrid_insert<true><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
+  k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
   k_near_fix<<<(unsigned)(((size_t)nrec * 32 + 255) / 256), 256, 0, s>>>(rec32, rec64, nrec, ew, chunks, nchunks, P, M,
                                                                          g, reinterpret_cast<unsigned long long*>(nacc),
                                                                          ctl);

@@ -64,14 +64,15 @@ constexpr int kRec32 = 48;
 #define VLM_BS_HD
 #endif
 
-// Near-field scratch of an evaluation at M targets (a hashed uniform grid of
-// the targets, carved from one caller buffer): header, [T] bucket counts,
-// [T + 1] bucket starts, [M] target indices, T = the smallest power of two
-// >= max(1024, 2 M).
+// Near-field scratch of an evaluation at M targets: the targets binned in a
+// uniform grid whose occupied cells sit in an open-addressing hash table
+// (T slots, T = the smallest power of two >= max(1024, 2 M)), carved from
+// one caller buffer: header, [T] cell keys, [T] per-slot target counts (the
+// fill cursors after the scan), [T + 1] slot starts, [M] target indices.
 struct GridHdr {
   double zsum;         // sum of the near-zone radii (the cell size is twice their mean)
   unsigned int zcount;
-  int T;               // bucket count
+  int T;               // table slots
 };
 VLM_BS_HD constexpr int grid_buckets(int M) {
   int T = 1024;
@@ -80,14 +81,15 @@ VLM_BS_HD constexpr int grid_buckets(int M) {
 }
 VLM_BS_HD constexpr size_t grid_align(size_t b) { return (b + 255) & ~size_t(255); }
 struct GridLayout {
-  size_t count, start, entry, total;
+  size_t key, count, start, entry, total;
 };
 VLM_BS_HD constexpr GridLayout grid_layout(int M) {
   const size_t T = (size_t)grid_buckets(M);
-  const size_t count = grid_align(sizeof(GridHdr));
+  const size_t key = grid_align(sizeof(GridHdr));
+  const size_t count = key + grid_align(T * sizeof(unsigned long long));
   const size_t start = count + grid_align(T * sizeof(int));
   const size_t entry = start + grid_align((T + 1) * sizeof(int));
-  return GridLayout{count, start, entry, entry + grid_align((size_t)M * sizeof(int))};
+  return GridLayout{key, count, start, entry, entry + grid_align((size_t)M * sizeof(int))};
 }
 // Bytes of near-field scratch an evaluation at M targets needs.
 VLM_BS_HD constexpr size_t near_grid_bytes(int M) { return grid_layout(M).total; }
