@@ -121,11 +121,12 @@ int vlm_biot_savart_filaments_device(const double* fc, const double* rvc, const 
  * device memory when they call it (a host solver that reserves its device
  * memory once at start-up, a process under a hard device-memory cap, or a
  * caller that must not trigger the device-wide synchronisation an allocation
- * may cause): its scratch is one fixed 9.5 MiB array compiled into the library,
- * held on every device that loads the library until the process exits.
- * Limits: N <= 16384 rings, M <= 65536 points; larger sizes return
- * VLM_ERR_INVALID with a message.  The rings are summed in one block, i.e.
- * in the reference's order.
+ * may cause): its scratch is one fixed 11.5 MiB array compiled into the
+ * library, held on every device that loads the library until the process
+ * exits.  Limits: N <= 16384 rings, M <= 65536 points; larger sizes return
+ * VLM_ERR_INVALID with a message, as does a VLM_PREC_FP32_NEAR64 call with
+ * more than 65536 near-field pairs.  The rings are summed in one block,
+ * i.e. in the reference's order.
  * The first call on a device looks up the scratch array's device address
  * and keeps it for the life of the process, so make that first call before
  * any CUDA stream capture, and do not reset the device (cudaDeviceReset)

@@ -26,8 +26,9 @@
 // corrected to FP64 outside the hot loop.  The targets are binned into a
 // hashed uniform grid (cell size twice the mean near-zone radius); every
 // near-zone filament, cut into pieces no longer than a cell, visits the
-// cells around each piece and tests their targets.  For every near pair
-// k_near_fix recomputes the FP32 kernel's own contribution bit for bit (same
+// cells around each piece and tests their targets, listing the near pairs
+// (k_near_find).  For every listed pair k_near_fix recomputes the FP32
+// kernel's own contribution bit for bit (same
 // inline arithmetic, same FP32 inputs) and adds FP64 value - FP32
 // contribution to order-independent fixed-point accumulators, which
 // k_near_apply folds into the chunk partial sums.  The result equals summing
@@ -520,28 +521,27 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
   return c * (d * rsqrt(s2 * s2 + c2 * c2) * kInv4Pi);
 }
 
-// One warp per record.  Every filament k with a near zone (radius
-// z = near_factor rvc_k, from [32 + k]) is cut into np pieces no longer than
-// a cell; the lanes visit the cells of each piece's box (grown by 1.42 z,
-// which holds the zone's cylinder and its extensions past the ends) and test
-// the targets binned there (cells whose centre is farther from the piece than
-// sqrt(2) z + half a cell diagonal are skipped, empty cells cost one probe).
-// A target is taken only by the piece that holds its projection on the
-// filament, so every (target, filament) pair is tested once.  A near pair --
-// |r_k x r_j|^2 < (near_factor rvc |e|)^2 and the projection within the
-// segment extended by near_factor rvc, on the FP32 kernel's own FP32 values
-// -- adds FP64 velocity x weight - the FP32 kernel's contribution
-// f (r_k x r_j) (recomputed with the same FP32 operations, the product taken
-// exactly in FP64) to the fixed-point accumulator of the target and the
-// record's chunk.  ctl[1] counts the corrected pairs, ctl[0] = 4 flags a
-// correction outside the fixed-point range.
-__global__ void k_near_fix(const float* __restrict__ rec32, const double* __restrict__ rec64, int nrec,
-                           const double* __restrict__ ew, const Chunk* __restrict__ chunks, int nchunks,
-                           const double* __restrict__ P, int M, const unsigned char* __restrict__ scratch,
-                           unsigned long long* __restrict__ nacc, int* __restrict__ ctl) {
+// Detection, one warp per record.  Every filament k with a near zone
+// (radius z = near_factor rvc_k, from [32 + k]) is cut into np pieces no
+// longer than a cell; the lanes take the cells of each piece's box (grown by
+// 1.42 z, which holds the zone's cylinder and its extensions past the ends),
+// skip cells whose centre is farther from the piece than sqrt(2) z + half a
+// cell diagonal, look the rest up in the cell table, and then share out the
+// targets of the cells found, 32 at a time.  A target is taken only by the
+// piece that holds its projection on the filament, so every (target,
+// filament) pair is tested once.  A near pair -- |r_k x r_j|^2 <
+// (near_factor rvc |e|)^2 and the projection within the segment extended by
+// near_factor rvc, on the FP32 kernel's own FP32 values -- is appended to the
+// near list (one atomic per warp and batch; ctl[1] counts, ctl[0] = 3 if the
+// list is full).
+__global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ rec32, int nrec,
+                                                   const Chunk* __restrict__ chunks, int nchunks,
+                                                   const double* __restrict__ P, int M,
+                                                   const unsigned char* __restrict__ scratch,
+                                                   NearPair* __restrict__ near, int near_cap, int* __restrict__ ctl) {
   const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (r >= nrec) return;
+  if (r >= nrec) return;  // whole warps leave together
   const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
   const float h = grid_h(H);
   if (!(h > 0.f)) return;
@@ -552,10 +552,6 @@ __global__ void k_near_fix(const float* __restrict__ rec32, const double* __rest
   const int* start = reinterpret_cast<const int*>(scratch + L.start);
   const int* entry = reinterpret_cast<const int*>(scratch + L.entry);
   const float* R = rec32 + (size_t)r * kRec32;
-  const double* D = rec64 + (size_t)r * kRec64;
-  const bool fil = (int)D[17] & REC_FIL;
-  RecView v;
-  load_view(reinterpret_cast<const float4*>(R), v);
   // the record's chunk (chunks are in record order)
   int q = 0;
   {
@@ -566,23 +562,23 @@ __global__ void k_near_fix(const float* __restrict__ rec32, const double* __rest
       else hi = mid - 1;
     }
   }
-  int found = 0;
+  const unsigned lt = (1u << lane) - 1u;
   for (int k = 0; k < 4; ++k) {
     const float thr = R[32 + k];
     if (!(thr >= 0.f)) continue;
     const int j = (k + 1) & 3;
     const float ax = R[3 * k], ay = R[3 * k + 1], az = R[3 * k + 2];
-    const float ex = R[3 * j] - ax, ey = R[3 * j + 1] - ay, ez = R[3 * j + 2] - az;
+    const float bx = R[3 * j], by = R[3 * j + 1], bz = R[3 * j + 2];
+    const float wex = R[12 + 3 * k], wey = R[12 + 3 * k + 1], wez = R[12 + 3 * k + 2];
+    const float eev = R[24 + k], a4 = R[28 + k], lo = R[36 + k], hi = R[40 + k];
+    const float ex = bx - ax, ey = by - ay, ez = bz - az;
     const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-    if (!(ee > 0.f) || !(v.eev[k] != 0.f)) continue;
+    if (!(ee > 0.f) || !(eev != 0.f)) continue;
     const float len = sqrtf(ee);
     const float z = sqrtf(thr) / len;
     const int np = max(1, min(4096, (int)ceilf(len * invh)));
     const float amax = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az)) + len;
     const float grow = 1.42f * z * 1.0001f + 1e-6f + 4e-7f * amax;
-    // cells whose centre lies farther than sqrt(2) z (the zone's extension
-    // past the ends) + half a cell diagonal from the piece cannot hold a
-    // target of the zone
     const float reach = 1.4143f * z * 1.0001f + 0.8661f * h + 1e-6f + 4e-7f * amax;
     const float reach2 = reach * reach;
     for (int pc = 0; pc < np; ++pc) {
@@ -594,56 +590,124 @@ __global__ void k_near_fix(const float* __restrict__ rec32, const double* __rest
       const int x0 = cell_of(fminf(qx0, qx1) - grow, invh), x1 = cell_of(fmaxf(qx0, qx1) + grow, invh);
       const int y0 = cell_of(fminf(qy0, qy1) - grow, invh), y1 = cell_of(fmaxf(qy0, qy1) + grow, invh);
       const int z0 = cell_of(fminf(qz0, qz1) - grow, invh), z1 = cell_of(fmaxf(qz0, qz1) + grow, invh);
-      const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
-      const long long ncell = (long long)nx * ny * nz;
-      for (long long ci = lane; ci < ncell; ci += 32) {
-        const int cx = x0 + (int)(ci % nx), cy = y0 + (int)((ci / nx) % ny), cz = z0 + (int)(ci / ((long long)nx * ny));
-        // distance from the cell centre to the piece
-        const float gx = ((float)cx + 0.5f) * h - qx0, gy = ((float)cy + 0.5f) * h - qy0, gz = ((float)cz + 0.5f) * h - qz0;
-        const float tq = ss > 0.f ? fminf(fmaxf(fmaf(gx, sx, fmaf(gy, sy, gz * sz)) / ss, 0.f), 1.f) : 0.f;
-        const float dx = fmaf(-tq, sx, gx), dy = fmaf(-tq, sy, gy), dz = fmaf(-tq, sz, gz);
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > reach2) continue;
-        const int b = cell_slot(key, T, cx, cy, cz);
-        if (b < 0) continue;
-        for (int e = start[b]; e < start[b + 1]; ++e) {
-          const int m = entry[e];
-          const double p64x = P[3 * (size_t)m], p64y = P[3 * (size_t)m + 1], p64z = P[3 * (size_t)m + 2];
-          const float px = (float)p64x, py = (float)p64y, pz = (float)p64z;  // as the FP32 kernel
-          float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
-          corner_vector(px, py, pz, ax, ay, az, rxk, ryk, rzk, invk);
-          corner_vector(px, py, pz, R[3 * j], R[3 * j + 1], R[3 * j + 2], rxj, ryj, rzj, invj);
-          const Fil32 t = fil_terms(v.ex[k], v.ey[k], v.ez[k], v.eev[k], v.a4v[k], rxk, ryk, rzk, invk, rxj, ryj, rzj,
-                                    invj);
-          // the piece that holds the target's projection takes the pair
-          const int own = max(0, min(np - 1, __float2int_rd(t.tt / v.eev[k] * (float)np)));
-          if (own != pc) continue;
-          if (!(t.c2 < thr && t.c2 > kS2Min && t.tt > R[36 + k] && t.tt < R[40 + k])) continue;
-          // FP64 value of the same filament pair
-          const d3 p = mk3(p64x, p64y, p64z);
-          d3 v64;
-          if (fil) {
-            v64 = fil_near64(p, mk3(D[0], D[1], D[2]), mk3(D[3], D[4], D[5]), D[12]);
-          } else {
-            v64 = fil_near64(p, mk3(D[3 * k], D[3 * k + 1], D[3 * k + 2]), mk3(D[3 * j], D[3 * j + 1], D[3 * j + 2]),
-                             D[12 + k]);
-          }
-          v64 = v64 * (ew ? ew[4 * (size_t)r + k] : D[16]);
-          const double c[3] = {v64.x - (double)t.f * (double)t.kx, v64.y - (double)t.f * (double)t.ky,
-                               v64.z - (double)t.f * (double)t.kz};
-          unsigned long long* o = nacc + ((size_t)q * M + m) * 3;
-          for (int a = 0; a < 3; ++a) {
-            if (!(fabs(c[a]) < kNearMax)) {
-              atomicExch(ctl, 4);
-              continue;
+      const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
+      const long long ncell = (long long)nx * ny * (z1 - z0 + 1);
+      for (long long base = 0; base < ncell; base += 32) {
+        // each lane one cell: culled by distance, then looked up
+        const long long ci = base + lane;
+        int s0 = 0, cnt = 0;
+        if (ci < ncell) {
+          const int cx = x0 + (int)(ci % nx), cy = y0 + (int)((ci / nx) % ny), cz = z0 + (int)(ci / ((long long)nx * ny));
+          const float gx = ((float)cx + 0.5f) * h - qx0, gy = ((float)cy + 0.5f) * h - qy0,
+                      gz = ((float)cz + 0.5f) * h - qz0;
+          const float tq = ss > 0.f ? fminf(fmaxf(fmaf(gx, sx, fmaf(gy, sy, gz * sz)) / ss, 0.f), 1.f) : 0.f;
+          const float dx = fmaf(-tq, sx, gx), dy = fmaf(-tq, sy, gy), dz = fmaf(-tq, sz, gz);
+          if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= reach2) {
+            const int b = cell_slot(key, T, cx, cy, cz);
+            if (b >= 0) {
+              s0 = start[b];
+              cnt = start[b + 1] - s0;
             }
-            atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
           }
-          ++found;
+        }
+        // the found cells' targets, shared out 32 at a time
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        for (int tb = 0; tb < total; tb += 32) {
+          const int idx = tb + lane;
+          // the lane whose cell holds target idx: the first with incl > idx
+          int own = 0;
+          for (int step = 16; step >= 1; step >>= 1) {
+            const int v = __shfl_sync(kFull, incl, own + step - 1);
+            if (v <= idx) own += step;
+          }
+          own = min(own, 31);
+          const int os0 = __shfl_sync(kFull, s0, own);
+          const int oex = __shfl_sync(kFull, incl - cnt, own);
+          bool isnear = false;
+          int m = 0;
+          if (idx < total) {
+            m = entry[os0 + idx - oex];
+            const float px = (float)P[3 * (size_t)m], py = (float)P[3 * (size_t)m + 1], pz = (float)P[3 * (size_t)m + 2];
+            float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
+            corner_vector(px, py, pz, ax, ay, az, rxk, ryk, rzk, invk);
+            corner_vector(px, py, pz, bx, by, bz, rxj, ryj, rzj, invj);
+            const Fil32 t = fil_terms(wex, wey, wez, eev, a4, rxk, ryk, rzk, invk, rxj, ryj, rzj, invj);
+            // the piece that holds the target's projection takes the pair
+            const int piece = max(0, min(np - 1, __float2int_rd(t.tt / eev * (float)np)));
+            isnear = piece == pc && t.c2 < thr && t.c2 > kS2Min && t.tt > lo && t.tt < hi;
+          }
+          const unsigned mask = __ballot_sync(kFull, isnear);
+          if (mask) {
+            int base_slot = 0;
+            if (lane == 0) base_slot = atomicAdd(ctl + 1, __popc(mask));
+            base_slot = __shfl_sync(kFull, base_slot, 0);
+            if (isnear) {
+              const int slot = base_slot + __popc(mask & lt);
+              if (slot < near_cap) {
+                NearPair np_;
+                np_.m = m;
+                np_.q = q;
+                np_.rec = r;
+                np_.k = k;
+                near[slot] = np_;
+              } else {
+                atomicExch(ctl, 3);
+              }
+            }
+          }
         }
       }
     }
   }
-  if (found) atomicAdd(ctl + 1, found);
+}
+
+// Correction, one thread per listed near pair: FP64 velocity x weight - the
+// FP32 kernel's contribution f (r_k x r_j) (recomputed with the same FP32
+// operations, the product taken exactly in FP64), added in fixed point to the
+// accumulator of the target and the record's chunk (order-independent).
+// ctl[0] = 4 flags a correction outside the fixed-point range.
+__global__ void k_near_fix(const NearPair* __restrict__ near, int near_cap, const float* __restrict__ rec32,
+                           const double* __restrict__ rec64, const double* __restrict__ ew,
+                           const double* __restrict__ P, int M, unsigned long long* __restrict__ nacc,
+                           int* __restrict__ ctl) {
+  const int n = min(ctl[1], near_cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const NearPair np_ = near[i];
+    const int r = np_.rec, k = np_.k, j = (k + 1) & 3, m = np_.m;
+    const float* R = rec32 + (size_t)r * kRec32;
+    const double* D = rec64 + (size_t)r * kRec64;
+    const double p64x = P[3 * (size_t)m], p64y = P[3 * (size_t)m + 1], p64z = P[3 * (size_t)m + 2];
+    const float px = (float)p64x, py = (float)p64y, pz = (float)p64z;  // as the FP32 kernel
+    float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
+    corner_vector(px, py, pz, R[3 * k], R[3 * k + 1], R[3 * k + 2], rxk, ryk, rzk, invk);
+    corner_vector(px, py, pz, R[3 * j], R[3 * j + 1], R[3 * j + 2], rxj, ryj, rzj, invj);
+    const Fil32 t = fil_terms(R[12 + 3 * k], R[12 + 3 * k + 1], R[12 + 3 * k + 2], R[24 + k], R[28 + k], rxk, ryk, rzk,
+                              invk, rxj, ryj, rzj, invj);
+    const d3 p = mk3(p64x, p64y, p64z);
+    d3 v64;
+    if ((int)D[17] & REC_FIL) {
+      v64 = fil_near64(p, mk3(D[0], D[1], D[2]), mk3(D[3], D[4], D[5]), D[12]);
+    } else {
+      v64 = fil_near64(p, mk3(D[3 * k], D[3 * k + 1], D[3 * k + 2]), mk3(D[3 * j], D[3 * j + 1], D[3 * j + 2]),
+                       D[12 + k]);
+    }
+    v64 = v64 * (ew ? ew[4 * (size_t)r + k] : D[16]);
+    const double c[3] = {v64.x - (double)t.f * (double)t.kx, v64.y - (double)t.f * (double)t.ky,
+                         v64.z - (double)t.f * (double)t.kz};
+    unsigned long long* o = nacc + ((size_t)np_.q * M + m) * 3;
+    for (int a = 0; a < 3; ++a) {
+      if (!(fabs(c[a]) < kNearMax)) {
+        atomicExch(ctl, 4);
+        continue;
+      }
+      atomicAdd(o + a, (unsigned long long)__double2ll_rn(c[a] * kNearScale));
+    }
+  }
 }
 
 __global__ void k_set_flag(int* ctl, int code) { atomicExch(ctl, code); }
@@ -754,17 +818,20 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   if (ew) k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
   else k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
   if (!near_scratch || nrec <= 0) return;
-  // near field: targets binned in a grid, FP64 corrections of the near
-  // pairs, corrections folded into the partial sums
-  if (near_bytes < near_grid_bytes(M)) {
+  // near field: targets binned in a grid, near pairs listed, FP64
+  // corrections of the listed pairs, corrections folded into the partials
+  const size_t gridBytes = near_grid_bytes(M);
+  if (near_bytes < gridBytes + (size_t)kNearAlign) {
     count_launch();
     k_set_flag<<<1, 1, 0, s>>>(ctl, 3);
     return;
   }
   unsigned char* g = static_cast<unsigned char*>(near_scratch);
+  NearPair* list = reinterpret_cast<NearPair*>(g + gridBytes);
+  const int cap = (int)std::min<size_t>((near_bytes - gridBytes) / sizeof(NearPair), (size_t)1 << 30);
   const GridLayout L = grid_layout(M);
   const int T = grid_buckets(M);
-  count_launches(6);
+  count_launches(7);
   k_grid_init<<<1, 1, 0, s>>>(g, T);
   k_zone_mean<<<(nrec + 255) / 256, 256, 0, s>>>(rec32, nrec, g);
   cudaMemsetAsync(g + L.key, 0xFF, (size_t)T * sizeof(unsigned long long), s);
@@ -772,13 +839,14 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
   k_grid_scan<<<1, 1024, 0, s>>>(M, g);
   k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
-  k_near_fix<<<(unsigned)(((size_t)nrec * 32 + 255) / 256), 256, 0, s>>>(rec32, rec64, nrec, ew, chunks, nchunks, P, M,
-                                                                         g, reinterpret_cast<unsigned long long*>(nacc),
-                                                                         ctl);
+  k_near_find<<<(unsigned)(((size_t)nrec * 32 + 255) / 256), 256, 0, s>>>(rec32, nrec, chunks, nchunks, P, M, g, list,
+                                                                          cap, ctl);
+  const int sms = device_sm_count();
+  k_near_fix<<<4 * sms, 128, 0, s>>>(list, cap, rec32, rec64, ew, P, M, reinterpret_cast<unsigned long long*>(nacc),
+                                     ctl);
   const size_t n = (size_t)M * nchunks * 3;
   count_launch();
-  k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * device_sm_count()), 256, 0, s>>>(part, nacc,
-                                                                                                            n);
+  k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * sms), 256, 0, s>>>(part, nacc, n);
 }
 
 // A host without a usable device still plans (sizes are queried before any

@@ -368,7 +368,7 @@ struct Case {
     s.targets = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.outv = dalloc<double>((size_t)maxTargets * 3, scratchOwned);
     s.part = dalloc<double>((size_t)maxPart * 3, scratchOwned);
-    s.nearBytes = opt.precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes(maxTargets) : 0;
+    s.nearBytes = opt.precision == VLM_PREC_FP32_NEAR64 ? near_scratch_bytes(maxTargets, (size_t)256 * maxTargets) : 0;
     s.nearScratch = s.nearBytes ? dalloc<unsigned char>(s.nearBytes, scratchOwned) : nullptr;
     // zero here; every near-field evaluation leaves them zero
     s.nacc = dalloc<long long>(opt.precision == VLM_PREC_FP32_NEAR64 ? (size_t)maxPart * 3 : 1, scratchOwned);
@@ -918,7 +918,7 @@ struct Case {
     VLM_CUDA(cudaStreamSynchronize(stream));
     iter += nsteps;
     const int err = errs[2];
-    if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field scratch too small");
+    if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
     if (err == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
     if (err) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
     if (errs[1]) throw StatusError(VLM_ERR_SINGULAR, "FP32 LU iterative refinement left a relative residual above 1e-9");
@@ -1365,7 +1365,7 @@ struct Case {
       } else {
         const bool nearOn = opt.precision == VLM_PREC_FP32_NEAR64;
         launch_pack32(rec64, rec, nearOn ? opt.near_factor : 0.0, rec32, stream);
-        const size_t nb = nearOn ? near_grid_bytes((int)M) : 1;
+        const size_t nb = nearOn ? near_scratch_bytes((int)M, (size_t)std::min<int64_t>(64 * M + (1 << 16), 1 << 26)) : 1;
         unsigned char* ns = dalloc<unsigned char>(nb, tmpOwned);
         long long* nacc = dalloc<long long>(nearOn ? (size_t)M * nq * 3 : 1, tmpOwned);
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
@@ -1444,13 +1444,16 @@ static int ring_plan(int64_t N, int64_t M, int precision, Group& g, std::vector<
 }
 
 
+// near-pair list capacity of an isolated evaluation at M targets
+static size_t ring_near_cap(int64_t M) { return (size_t)std::min<int64_t>(16 * M + (1 << 20), 1 << 27); }
+
 int64_t ring_scratch_bytes(int64_t N, int64_t M, int precision) {
   Group g;
   std::vector<Chunk> ch;
   const int64_t Q = std::max(1, ring_plan(N, M, precision, g, ch));
   int64_t b = N * kRec64 * 8 + M * Q * 3 * 8 + Q * (int64_t)sizeof(Chunk) + 64;
   if (precision != VLM_PREC_FP64) b += N * kRec32 * 4;
-  if (precision == VLM_PREC_FP32_NEAR64) b += (int64_t)near_grid_bytes((int)M) + M * Q * 3 * 8;
+  if (precision == VLM_PREC_FP32_NEAR64) b += (int64_t)near_scratch_bytes((int)M, ring_near_cap(M)) + M * Q * 3 * 8;
   return b;
 }
 
@@ -1485,7 +1488,7 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   grow((void**)&R.chunks, R.capChunks, (size_t)Q * sizeof(Chunk) + sizeof(Group) + 64);
   R.group = reinterpret_cast<Group*>(R.chunks + Q);
   if (!R.err) VLM_CUDA(cudaMalloc(&R.err, 4 * sizeof(int)));
-  const size_t nearBytes = precision == VLM_PREC_FP32_NEAR64 ? near_grid_bytes((int)M) : 1;
+  const size_t nearBytes = precision == VLM_PREC_FP32_NEAR64 ? near_scratch_bytes((int)M, ring_near_cap(M)) : 1;
   grow((void**)&R.near, R.capNear, nearBytes);
   if (precision == VLM_PREC_FP32_NEAR64 && (size_t)M * Q * 3 * 8 > R.capNacc) {
     grow((void**)&R.nacc, R.capNacc, (size_t)M * Q * 3 * 8);
@@ -1519,7 +1522,7 @@ void rings_device(const double* corners, const double* rvc, const double* gam, i
   int ctl[2] = {0, 0};
   VLM_CUDA(cudaMemcpyAsync(ctl, R.err, sizeof(ctl), cudaMemcpyDeviceToHost, st));
   VLM_CUDA(cudaStreamSynchronize(st));
-  if (ctl[0] == 3) throw StatusError(VLM_ERR_CUDA, "near-field scratch too small");
+  if (ctl[0] == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
   if (ctl[0] == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
   if (ctl[0]) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
 }

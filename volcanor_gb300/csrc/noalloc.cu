@@ -25,13 +25,14 @@ namespace {
 // Limits of the fixed scratch (see include/vlm.h).
 constexpr int64_t kMaxRings = 16384;
 constexpr int64_t kMaxPoints = 65536;
+constexpr int64_t kMaxNear = 65536;
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kOffRec64 = 0;
 constexpr size_t kOffRec32 = kOffRec64 + align256(kMaxRings * kRec64 * sizeof(double));
 constexpr size_t kOffPart = kOffRec32 + align256(kMaxRings * kRec32 * sizeof(float));
 constexpr size_t kOffNear = kOffPart + align256(kMaxPoints * 3 * sizeof(double));
-constexpr size_t kNearBytes = near_grid_bytes((int)kMaxPoints);  // near-field grid for the largest M
+constexpr size_t kNearBytes = near_scratch_bytes((int)kMaxPoints, (size_t)kMaxNear);  // near-field grid + pair list
 constexpr size_t kOffNacc = kOffNear + align256(kNearBytes);
 constexpr size_t kOffTables = kOffNacc + align256(kMaxPoints * 3 * sizeof(long long));
 constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words
@@ -149,7 +150,7 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   e = cudaMemcpyAsync(flags, ctl, sizeof(flags), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
-  if (flags[0] == 3) return fail(VLM_ERR_CUDA, "vlm_biot_savart_rings_noalloc: near-field scratch too small");
+  if (flags[0] == 3) return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc: the near-field pair list overflowed (more than 65536 pairs)");
   if (flags[0] == 4) return fail(VLM_ERR_NONFINITE, "vlm_biot_savart_rings_noalloc: near-field velocity outside the fixed-point range");
   if (flags[0]) return fail(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
   return VLM_OK;

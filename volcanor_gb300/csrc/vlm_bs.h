@@ -64,6 +64,12 @@ constexpr int kRec32 = 48;
 #define VLM_BS_HD
 #endif
 
+// One near-field filament-target pair: target m, chunk q (partial sum to
+// correct), global record index, filament k.
+struct NearPair {
+  int32_t m, q, rec, k;
+};
+
 // Near-field scratch of an evaluation at M targets: the targets binned in a
 // uniform grid whose occupied cells sit in an open-addressing hash table
 // (T slots, T = the smallest power of two >= max(1024, 2 M)), carved from
@@ -91,8 +97,14 @@ VLM_BS_HD constexpr GridLayout grid_layout(int M) {
   const size_t entry = start + grid_align((T + 1) * sizeof(int));
   return GridLayout{key, count, start, entry, entry + grid_align((size_t)M * sizeof(int))};
 }
-// Bytes of near-field scratch an evaluation at M targets needs.
+// Bytes of the grid part of the near-field scratch of an evaluation at M
+// targets; the near-pair list (NearPair entries) follows it.
 VLM_BS_HD constexpr size_t near_grid_bytes(int M) { return grid_layout(M).total; }
+constexpr int kNearAlign = 256;
+// Near-field scratch for M targets and a list of cap near pairs.
+VLM_BS_HD constexpr size_t near_scratch_bytes(int M, size_t cap) {
+  return near_grid_bytes(M) + grid_align(cap * sizeof(NearPair));
+}
 
 // Fixed-point scale of the near-field accumulators: FP64 near-field
 // velocities are added as integers (v * 2^44, |v| < 2^18) so that their sum
@@ -141,13 +153,14 @@ int device_sm_count();
 void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const double* P, int M, double* part,
                       cudaStream_t s);
 // FP32 pairs with FP64 accumulation over the nrec records the chunks cover.
-// When near_scratch is non-null (near_bytes >= near_grid_bytes(M)), the
+// When near_scratch is non-null (near_bytes = near_scratch_bytes(M, cap) for a list of cap
+// near pairs), the
 // pairs inside the records' near-field thresholds are then corrected to FP64
 // through the fixed-point accumulators nacc (M x nchunks x 3, zero on entry
 // and left zero on return).  ctl[0] receives a nonzero code if a bounded wait
 // on the tile pipeline expired (1, 2), the near-field scratch was too small
-// (3) or a near-field correction left the fixed-point range (4); ctl[1]
-// counts the corrected near pairs.  ctl must be zeroed before the call.
+// or the near-pair list was too small (3) or a near-field correction left the
+// fixed-point range (4); ctl[1] counts the near pairs.  ctl must be zeroed before the call.
 // ew: the records' edge weights in lattice form (FP64 near field multiplies
 // by ew[4 rec + k] instead of the record's circulation), or null.
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
