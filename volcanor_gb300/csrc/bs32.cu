@@ -37,6 +37,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 
 #include "vlm_bs.h"
@@ -429,7 +430,7 @@ __device__ __forceinline__ float grid_h(const GridHdr* H) {
 }
 
 // PASS 0: insert the target's cell key and count the target in its slot;
-// PASS 1: write the target's index at its slot's cursor.
+// PASS 1: write the target's FP32 position and index at its slot's cursor.
 template <int PASS>
 __global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned char* __restrict__ scratch) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -447,7 +448,7 @@ __global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned cha
   if (PASS == 0) {
     const unsigned long long k = cell_key(ix, iy, iz);
     unsigned b = cell_hash(ix, iy, iz, T);
-    // T >= 2 M: a free slot always exists
+    // T >= M >= occupied cells: a free slot always exists
     for (int n = 0; n < T; ++n) {
       const unsigned long long old = atomicCAS(key + b, kEmptyKey, k);
       if (old == kEmptyKey || old == k) {
@@ -459,7 +460,9 @@ __global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned cha
   } else {
     const int b = cell_slot(key, T, ix, iy, iz);
     const int slot = atomicAdd(count + b, 1);
-    reinterpret_cast<int*>(scratch + L.entry)[slot] = m;
+    reinterpret_cast<float4*>(scratch + L.entry)[slot] =
+        make_float4((float)P[3 * (size_t)m], (float)P[3 * (size_t)m + 1], (float)P[3 * (size_t)m + 2],
+                    __int_as_float(m));
   }
 }
 
@@ -521,7 +524,7 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
   return c * (d * rsqrt(s2 * s2 + c2 * c2) * kInv4Pi);
 }
 
-// Detection, one warp per record.  Every filament k with a near zone
+// Detection, one warp per filament (record r, edge k).  A filament with a near zone
 // (radius z = near_factor rvc_k, from [32 + k]) is cut into np pieces no
 // longer than a cell; the lanes take the cells of each piece's box (grown by
 // 1.42 z, which holds the zone's cylinder and its extensions past the ends),
@@ -539,9 +542,13 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
                                                    const double* __restrict__ P, int M,
                                                    const unsigned char* __restrict__ scratch,
                                                    NearPair* __restrict__ near, int near_cap, int* __restrict__ ctl) {
-  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const size_t wid = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (r >= nrec) return;  // whole warps leave together
+  if (wid >= (size_t)nrec * 4) return;  // whole warps leave together
+  const int r = (int)(wid >> 2), k = (int)(wid & 3);
+  const float* R = rec32 + (size_t)r * kRec32;
+  const float thr = R[32 + k];
+  if (!(thr >= 0.f)) return;
   const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
   const float h = grid_h(H);
   if (!(h > 0.f)) return;
@@ -550,8 +557,7 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
   const GridLayout L = grid_layout(M);
   const unsigned long long* key = reinterpret_cast<const unsigned long long*>(scratch + L.key);
   const int* start = reinterpret_cast<const int*>(scratch + L.start);
-  const int* entry = reinterpret_cast<const int*>(scratch + L.entry);
-  const float* R = rec32 + (size_t)r * kRec32;
+  const float4* entry = reinterpret_cast<const float4*>(scratch + L.entry);
   // the record's chunk (chunks are in record order)
   int q = 0;
   {
@@ -563,9 +569,7 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
     }
   }
   const unsigned lt = (1u << lane) - 1u;
-  for (int k = 0; k < 4; ++k) {
-    const float thr = R[32 + k];
-    if (!(thr >= 0.f)) continue;
+  {
     const int j = (k + 1) & 3;
     const float ax = R[3 * k], ay = R[3 * k + 1], az = R[3 * k + 2];
     const float bx = R[3 * j], by = R[3 * j + 1], bz = R[3 * j + 2];
@@ -573,7 +577,7 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
     const float eev = R[24 + k], a4 = R[28 + k], lo = R[36 + k], hi = R[40 + k];
     const float ex = bx - ax, ey = by - ay, ez = bz - az;
     const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-    if (!(ee > 0.f) || !(eev != 0.f)) continue;
+    if (!(ee > 0.f) || !(eev != 0.f)) return;
     const float len = sqrtf(ee);
     const float z = sqrtf(thr) / len;
     const int np = max(1, min(4096, (int)ceilf(len * invh)));
@@ -590,14 +594,17 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
       const int x0 = cell_of(fminf(qx0, qx1) - grow, invh), x1 = cell_of(fmaxf(qx0, qx1) + grow, invh);
       const int y0 = cell_of(fminf(qy0, qy1) - grow, invh), y1 = cell_of(fmaxf(qy0, qy1) + grow, invh);
       const int z0 = cell_of(fminf(qz0, qz1) - grow, invh), z1 = cell_of(fmaxf(qz0, qz1) + grow, invh);
-      const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
-      const long long ncell = (long long)nx * ny * (z1 - z0 + 1);
-      for (long long base = 0; base < ncell; base += 32) {
+      const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nxy = nx * ny;
+      // (a piece's box spans a few cells per axis unless a zone is far larger
+      // than the mean; 2^31 cells would take hours, never an index overflow)
+      const int ncell = (int)min((long long)nxy * (z1 - z0 + 1), (long long)INT_MAX - 32);
+      for (int base = 0; base < ncell; base += 32) {
         // each lane one cell: culled by distance, then looked up
-        const long long ci = base + lane;
+        const int ci = base + lane;
         int s0 = 0, cnt = 0;
         if (ci < ncell) {
-          const int cx = x0 + (int)(ci % nx), cy = y0 + (int)((ci / nx) % ny), cz = z0 + (int)(ci / ((long long)nx * ny));
+          const int cz = z0 + ci / nxy, rem = ci % nxy;
+          const int cx = x0 + rem % nx, cy = y0 + rem / nx;
           const float gx = ((float)cx + 0.5f) * h - qx0, gy = ((float)cy + 0.5f) * h - qy0,
                       gz = ((float)cz + 0.5f) * h - qz0;
           const float tq = ss > 0.f ? fminf(fmaxf(fmaf(gx, sx, fmaf(gy, sy, gz * sz)) / ss, 0.f), 1.f) : 0.f;
@@ -631,8 +638,9 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
           bool isnear = false;
           int m = 0;
           if (idx < total) {
-            m = entry[os0 + idx - oex];
-            const float px = (float)P[3 * (size_t)m], py = (float)P[3 * (size_t)m + 1], pz = (float)P[3 * (size_t)m + 2];
+            const float4 e4 = entry[os0 + idx - oex];
+            m = __float_as_int(e4.w);
+            const float px = e4.x, py = e4.y, pz = e4.z;  // the FP32 kernel's target coordinates
             float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
             corner_vector(px, py, pz, ax, ay, az, rxk, ryk, rzk, invk);
             corner_vector(px, py, pz, bx, by, bz, rxj, ryj, rzj, invj);
@@ -839,8 +847,8 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
   k_grid_scan<<<1, 1024, 0, s>>>(M, g);
   k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
-  k_near_find<<<(unsigned)(((size_t)nrec * 32 + 255) / 256), 256, 0, s>>>(rec32, nrec, chunks, nchunks, P, M, g, list,
-                                                                          cap, ctl);
+  k_near_find<<<(unsigned)(((size_t)nrec * 4 * 32 + 255) / 256), 256, 0, s>>>(rec32, nrec, chunks, nchunks, P, M, g,
+                                                                              list, cap, ctl);
   const int sms = device_sm_count();
   k_near_fix<<<4 * sms, 128, 0, s>>>(list, cap, rec32, rec64, ew, P, M, reinterpret_cast<unsigned long long*>(nacc),
                                      ctl);

@@ -72,9 +72,11 @@ struct NearPair {
 
 // Near-field scratch of an evaluation at M targets: the targets binned in a
 // uniform grid whose occupied cells sit in an open-addressing hash table
-// (T slots, T = the smallest power of two >= max(1024, 2 M)), carved from
+// (T slots, T = the smallest power of two >= max(1024, M): at least two
+// targets per occupied cell on the wakes this serves), carved from
 // one caller buffer: header, [T] cell keys, [T] per-slot target counts (the
-// fill cursors after the scan), [T + 1] slot starts, [M] target indices.
+// fill cursors after the scan), [T + 1] slot starts, [M] float4 entries in
+// slot order (the target's FP32 position and, in w, its index's bits).
 struct GridHdr {
   double zsum;         // sum of the near-zone radii (the cell size is twice their mean)
   unsigned int zcount;
@@ -82,7 +84,7 @@ struct GridHdr {
 };
 VLM_BS_HD constexpr int grid_buckets(int M) {
   int T = 1024;
-  while (T < 2 * M && T < (1 << 28)) T <<= 1;
+  while (T < M && T < (1 << 28)) T <<= 1;
   return T;
 }
 VLM_BS_HD constexpr size_t grid_align(size_t b) { return (b + 255) & ~size_t(255); }
@@ -95,7 +97,7 @@ VLM_BS_HD constexpr GridLayout grid_layout(int M) {
   const size_t count = key + grid_align(T * sizeof(unsigned long long));
   const size_t start = count + grid_align(T * sizeof(int));
   const size_t entry = start + grid_align((T + 1) * sizeof(int));
-  return GridLayout{key, count, start, entry, entry + grid_align((size_t)M * sizeof(int))};
+  return GridLayout{key, count, start, entry, entry + grid_align((size_t)M * 4 * sizeof(float))};
 }
 // Bytes of the grid part of the near-field scratch of an evaluation at M
 // targets; the near-pair list (NearPair entries) follows it.
