@@ -24,7 +24,7 @@
 // pairs within near_factor core radii of a filament segment -- where the
 // FP32 cross product and Vatistas denominator lose digits -- are then
 // corrected to FP64 outside the hot loop.  The targets are binned into a
-// hashed uniform grid (cell size twice the mean near-zone radius); every
+// hashed uniform grid (cell size three times the mean near-zone radius); every
 // near-zone filament, cut into pieces no longer than a cell, visits the
 // cells around each piece and tests their targets, listing the near pairs
 // (k_near_find).  For every listed pair k_near_fix recomputes the FP32
@@ -360,6 +360,7 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
 // (it is not), so empty cells cost one or two reads and a slot holds the
 // targets of one cell only.
 constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr double kCellOverZone = 3.0;  // cell size / mean near-zone radius
 constexpr int kCellBias = 1 << 20;
 
 __device__ __forceinline__ unsigned long long cell_key(int ix, int iy, int iz) {
@@ -426,7 +427,7 @@ __global__ void k_zone_mean(const float* __restrict__ rec32, int nrec, unsigned 
 }
 
 __device__ __forceinline__ float grid_h(const GridHdr* H) {
-  return H->zcount ? (float)(2.0 * H->zsum / (double)H->zcount) : 0.f;
+  return H->zcount ? (float)(kCellOverZone * H->zsum / (double)H->zcount) : 0.f;
 }
 
 // PASS 0: insert the target's cell key and count the target in its slot;
@@ -573,13 +574,17 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
     const int j = (k + 1) & 3;
     const float ax = R[3 * k], ay = R[3 * k + 1], az = R[3 * k + 2];
     const float bx = R[3 * j], by = R[3 * j + 1], bz = R[3 * j + 2];
-    const float wex = R[12 + 3 * k], wey = R[12 + 3 * k + 1], wez = R[12 + 3 * k + 2];
-    const float eev = R[24 + k], a4 = R[28 + k], lo = R[36 + k], hi = R[40 + k];
+    const float eev = R[24 + k];
     const float ex = bx - ax, ey = by - ay, ez = bz - az;
     const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
     if (!(ee > 0.f) || !(eev != 0.f)) return;
     const float len = sqrtf(ee);
     const float z = sqrtf(thr) / len;
+    // near zone: distance to the line < z, projection within the segment
+    // extended by z at both ends (the FP32 kernel's own near test, in
+    // distance form; which pairs are corrected is an accuracy choice, the
+    // correction itself is exact)
+    const float iee = 1.f / ee, z2 = z * z, tlo = -z * len, thi = fmaf(z, len, ee);
     const int np = max(1, min(4096, (int)ceilf(len * invh)));
     const float amax = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az)) + len;
     const float grow = 1.42f * z * 1.0001f + 1e-6f + 4e-7f * amax;
@@ -595,6 +600,7 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
       const int y0 = cell_of(fminf(qy0, qy1) - grow, invh), y1 = cell_of(fmaxf(qy0, qy1) + grow, invh);
       const int z0 = cell_of(fminf(qz0, qz1) - grow, invh), z1 = cell_of(fmaxf(qz0, qz1) + grow, invh);
       const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nxy = nx * ny;
+      const float inx = 1.f / (float)nx, inxy = 1.f / (float)nxy;
       // (a piece's box spans a few cells per axis unless a zone is far larger
       // than the mean; 2^31 cells would take hours, never an index overflow)
       const int ncell = (int)min((long long)nxy * (z1 - z0 + 1), (long long)INT_MAX - 32);
@@ -603,8 +609,10 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
         const int ci = base + lane;
         int s0 = 0, cnt = 0;
         if (ci < ncell) {
-          const int cz = z0 + ci / nxy, rem = ci % nxy;
-          const int cx = x0 + rem % nx, cy = y0 + rem / nx;
+          // exact for the small cell counts of a piece (ci < 2^22)
+          const int iz = (int)(((float)ci + 0.5f) * inxy), rem = ci - iz * nxy;
+          const int iy = (int)(((float)rem + 0.5f) * inx);
+          const int cx = x0 + rem - iy * nx, cy = y0 + iy, cz = z0 + iz;
           const float gx = ((float)cx + 0.5f) * h - qx0, gy = ((float)cy + 0.5f) * h - qy0,
                       gz = ((float)cz + 0.5f) * h - qz0;
           const float tq = ss > 0.f ? fminf(fmaxf(fmaf(gx, sx, fmaf(gy, sy, gz * sz)) / ss, 0.f), 1.f) : 0.f;
@@ -640,14 +648,14 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
           if (idx < total) {
             const float4 e4 = entry[os0 + idx - oex];
             m = __float_as_int(e4.w);
-            const float px = e4.x, py = e4.y, pz = e4.z;  // the FP32 kernel's target coordinates
-            float rxk, ryk, rzk, invk, rxj, ryj, rzj, invj;
-            corner_vector(px, py, pz, ax, ay, az, rxk, ryk, rzk, invk);
-            corner_vector(px, py, pz, bx, by, bz, rxj, ryj, rzj, invj);
-            const Fil32 t = fil_terms(wex, wey, wez, eev, a4, rxk, ryk, rzk, invk, rxj, ryj, rzj, invj);
+            // projection on the filament and distance to its line
+            const float dx = e4.x - ax, dy = e4.y - ay, dz = e4.z - az;
+            const float tr = fmaf(dx, ex, fmaf(dy, ey, dz * ez));  // e.(p - a)
+            const float tn = tr * iee;
+            const float qx = fmaf(-tn, ex, dx), qy = fmaf(-tn, ey, dy), qz = fmaf(-tn, ez, dz);
             // the piece that holds the target's projection takes the pair
-            const int piece = max(0, min(np - 1, __float2int_rd(t.tt / eev * (float)np)));
-            isnear = piece == pc && t.c2 < thr && t.c2 > kS2Min && t.tt > lo && t.tt < hi;
+            const int piece = max(0, min(np - 1, __float2int_rd(tn * (float)np)));
+            isnear = piece == pc && fmaf(qx, qx, fmaf(qy, qy, qz * qz)) < z2 && tr > tlo && tr < thi;
           }
           const unsigned mask = __ballot_sync(kFull, isnear);
           if (mask) {

@@ -78,7 +78,7 @@ struct NearPair {
 // fill cursors after the scan), [T + 1] slot starts, [M] float4 entries in
 // slot order (the target's FP32 position and, in w, its index's bits).
 struct GridHdr {
-  double zsum;         // sum of the near-zone radii (the cell size is twice their mean)
+  double zsum;         // sum of the near-zone radii (the cell size is a multiple of their mean)
   unsigned int zcount;
   int T;               // table slots
 };
