@@ -220,6 +220,9 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *                                   multi-step schemes (velNwake1..3, velFwake1..3)
  *   velKin (blade)                  (3, nc, ns) the kinematic velocity at the collocation points
  *                                   of the current iteration (during an open step, of that step)
+ *   waP (blade)                     (3, 2, 240) the prescribed far wake's filaments (fc(:,1), fc(:,2)),
+ *                                   cases with prescWakeAfterTruncNt > 0 only (src/classdef.f90:222-236)
+ *   waP_gam, waP_rvc (blade)        scalars: its circulation and core radius
  *   gamPrev (blade)                 (nc, ns) the previous step's trapezoidal circulation
  *                                   (the unsteady term of the loads)
  *   secCL, secLift, secLiftDir, secChordwiseResVel (blade)  per section

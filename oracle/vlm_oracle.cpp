@@ -392,6 +392,14 @@ struct FW {            // classdef.f90:198-220
   double gam = 0;
 };
 
+// classdef.f90:222-236 -- prescribed far wake: a helix of 240 filaments (10
+// revolutions) fitted to the free far wake and attached at its oldest node
+struct PFwake {
+  std::vector<FW> waF = std::vector<FW>(240);
+  double nRevs = 10.0, helixPitch = 0.0, helixRadius = 0.0, relaxFactor = 0.5;
+  bool isClockwiseRotor = true, isPresent = false;
+};
+
 struct WingPanel {     // classdef.f90:106-179
   VR vr;
   double gamPrev = 0, gamTrapz = 0;
@@ -435,6 +443,7 @@ struct Blade {         // classdef.f90:238-358
   std::vector<WingPanel> wiP;     // [i + nc*j]
   std::vector<VR> waN, waNP;      // [i + NW*j]
   std::vector<FW> waF, waFP;
+  PFwake wapF, wapFP;  // prescribed far wake of the free wake and of the predicted wake
   double theta = 0, psi = 0, pivotLE = 0, preconeAngle = 0;
   double flap = 0, dflap = 0, flapPrev = 0, dflapPrev = 0, MflapLift = 0, MflapLiftPrev = 0;
   V3 flapOrigin, forceInertial, lift, drag, dragInduced, dragProfile, liftUnsteady, dragUnsteady;
@@ -997,7 +1006,15 @@ struct Sim {
           if (std::fabs(f.gam) > EPS) s.add(vf_vind(f.vf, P) * f.gam);
           else s.tick();
         }
-        // prescribed far wake: circulation stays 0 (not generated), so skipped
+        // the prescribed far wake (classdef.f90:1471-1476, 1501-1507): summed
+        // only by cases that generate one
+        if (R.prescWakeNt > 0) {
+          const PFwake& pf = pred ? b.wapFP : b.wapF;
+          for (const FW& f : pf.waF) {
+            if (std::fabs(f.gam) > EPS) s.add(vf_vind(f.vf, P) * f.gam);
+            else s.tick();
+          }
+        }
       }
       acc = acc + s.result();
     }
@@ -1169,7 +1186,82 @@ struct Sim {
         blade_rot_wake_axis(b, off, R.shaftAxis, R.hubCoords, pred);
       }
     }
-    if (R.prescWakeNt > 0 && iter > R.prescWakeNt) throw std::runtime_error("prescribed far wake not supported");
+    if (R.prescWakeNt > 0 && iter > R.prescWakeNt) updatePrescribedWake(pred);
+  }
+  // classdef.f90:998-1066 (pFwake_update) on the far-wake filaments i0..i1
+  void pFwake_update(PFwake& pf, const std::vector<FW>& waF, int i0, int i1, V3 hub, V3 shaft, double dpsi) {
+    if (std::fabs(shaft.x) > EPS || std::fabs(shaft.y) > EPS)
+      throw std::runtime_error("Prescribed far wake only implemented for shaft along Z-axis");
+    pf.isPresent = true;
+    const int n = i1 - i0 + 1;
+    const V3 anchor = waF[i1].vf.fc1;
+    double pitch = 0.0, radius = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const V3 c = waF[i0 + i].vf.fc1;
+      radius = radius + std::sqrt(c.y * c.y + c.x * c.x);
+      if (i < n - 1) pitch = pitch + c.z - waF[i0 + i + 1].vf.fc1.z;
+    }
+    pitch = std::fabs(pitch) * (-TWO_PI / dpsi) / double(n - 1);
+    radius = radius / double(n);
+    pf.helixPitch = pf.relaxFactor * pitch + (1.0 - pf.relaxFactor) * pf.helixPitch;
+    pf.helixRadius = pf.relaxFactor * radius + (1.0 - pf.relaxFactor) * pf.helixRadius;
+    const double dTheta = std::atan2(anchor.y, anchor.x);
+    const double deltaZ = anchor.z - hub.z;
+    const int nc = (int)pf.waF.size() + 1;
+    std::vector<double> theta = linspace(0.0, TWO_PI * pf.nRevs, nc);
+    if (pf.isClockwiseRotor)
+      for (auto& t : theta) t = -1.0 * t;
+    std::vector<V3> c(nc);
+    for (int i = 0; i < nc; ++i)
+      c[i] = mk(pf.helixRadius * std::cos(theta[i] + dTheta), pf.helixRadius * std::sin(theta[i] + dTheta),
+                pf.helixPitch * std::fabs(theta[i]) / TWO_PI + deltaZ);
+    for (size_t i = 0; i < pf.waF.size(); ++i) {
+      pf.waF[i].vf.fc2 = hub + c[i];
+      pf.waF[i].vf.fc1 = hub + c[i + 1];
+    }
+    pf.waF[0].vf.fc2 = anchor;
+    for (auto& f : pf.waF) {
+      f.gam = waF[i1].gam;
+      f.vf.rVc = waF[i1].vf.rVc;
+    }
+  }
+  // classdef.f90:5172-5217
+  void updatePrescribedWake(bool pred) {
+    const int rowStart = R.prescWakeGenNt == 0 ? R.rowFar : R.nFwake - R.prescWakeGenNt;
+    for (int ib = 0; ib < R.nbConvect; ++ib) {
+      Blade& b = R.blade[ib];
+      pFwake_update(pred ? b.wapFP : b.wapF, pred ? b.waFP : b.waF, rowStart - 1, R.nFwake - 1, R.hubCoords,
+                    R.shaftAxis, R.omegaSlow * dt);
+    }
+    if (R.axisymmetrySwitch == 1)
+      for (int ib = 1; ib < R.nb; ++ib) {
+        PFwake& d = pred ? R.blade[ib].wapFP : R.blade[ib].wapF;
+        d = pred ? R.blade[0].wapFP : R.blade[0].wapF;
+        const double off = (TWO_PI / double(R.nb)) * double(ib);
+        if (std::fabs(off) > EPS) {  // pFwake_rot_wake_axis, classdef.f90:1068-1086
+          const M3 T = getTransformAxis(off, R.shaftAxis);
+          for (auto& f : d.waF) {
+            f.vf.fc1 = rotAbout(T, f.vf.fc1, R.hubCoords);
+            f.vf.fc2 = rotAbout(T, f.vf.fc2, R.hubCoords);
+          }
+        }
+      }
+  }
+  // classdef.f90:4911-4917, 2306-2339: far-wake filaments whose direction
+  // turns by more than skewLimit x pi from the next one's get a core radius
+  // of one chord (every blade)
+  void burst_wake() {
+    for (auto& b : R.blade) {
+      if (R.rowFar > R.nFwake) continue;
+      for (int i = R.rowFar - 1; i < R.nFwake - 1; ++i) {
+        const V3 a = b.waF[i].vf.fc2 - b.waF[i].vf.fc1, c = b.waF[i + 1].vf.fc1 - b.waF[i + 1].vf.fc2;
+        const double skew = std::fabs(std::acos(dot(a, c) / std::sqrt(sumsq(a) * sumsq(c))) - PI) / PI;
+        if (skew >= R.skewLimit) {
+          b.waF[i + 1].vf.rVc = R.chord;
+          b.waF[i].vf.rVc = R.chord;
+        }
+      }
+    }
   }
   // classdef.f90:4481-4513
   void shiftwake() {
@@ -1607,7 +1699,6 @@ struct Sim {
     toChordsRevs(r.wakeTruncateNt); toChordsRevs(r.prescWakeAfterTruncNt); toChordsRevs(r.prescWakeGenNt);
     toChordsRevs(r.nNwake); toChordsRevs(r.inflowPlotSwitch); toChordsRevs(r.gammaPlotSwitch); toChordsRevs(r.skewPlotSwitch);
     r.prescWakeNt = (r.wakeTruncateNt > 0 && r.prescWakeAfterTruncNt > 0) ? r.wakeTruncateNt + r.prescWakeAfterTruncNt : 0;
-    if (r.prescWakeNt > 0) throw std::runtime_error("prescribed far wake is not supported by this oracle");
     if (r.wakeTruncateNt > 0) r.wakeTruncateNt = std::max(r.wakeTruncateNt, r.nNwake + 1);
     if (r.surfaceType == 0) r.surfaceType = 1;
     if (r.nNwake > 0 && r.nNwake < 2) throw std::runtime_error("Atleast 2 near wake rows mandatory");
@@ -1898,7 +1989,7 @@ struct Sim {
       assignshed(true);
       age_wake();
       if (sw.wakeDissipation == 1) dissipate_wake();
-      if (sw.wakeBurst != 0) throw std::runtime_error("wakeBurst is not supported");
+      if (sw.wakeBurst != 0 && iter % sw.wakeBurst == 0) burst_wake();
     }
     for (int i = 0; i <= sw.ntSub; ++i) {
       solveCirculation(true);
@@ -2370,6 +2461,9 @@ long or_get(void* h, const char* name, int ib, double* out, long cap) {
     else if (k == "velF2") { for (auto& a : b->velF2) push3(a); }
     else if (k == "velF3") { for (auto& a : b->velF3) push3(a); }
     else if (k == "gamPrev") { for (auto& p : b->wiP) v.push_back(p.gamPrev); }
+    else if (k == "waP") { for (auto& f : b->wapF.waF) { push3(f.vf.fc1); push3(f.vf.fc2); } }
+    else if (k == "waP_gam") v = {b->wapF.waF[0].gam};
+    else if (k == "waP_rvc") v = {b->wapF.waF[0].vf.rVc};
     else if (k == "waN_age") { for (auto& w : b->waN) v.push_back(w.vf[0].age); }
     else if (k == "waF_rvc0") { for (auto& f : b->waF) v.push_back(f.vf.rVc0); }
     else if (k == "waF_l0") { for (auto& f : b->waF) v.push_back(f.vf.l0); }

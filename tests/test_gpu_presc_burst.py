@@ -1,0 +1,95 @@
+"""Prescribed far wake (src/classdef.f90:998-1066, 5172-5217) and wake burst
+(src/classdef.f90:2306-2339, 4911-4917) on the GPU against the oracle.
+
+The burst decides on acos of positions and writes core radii: bit for bit.
+The prescribed helix is placed with cos/sin/atan2, which the device and the
+host library round differently in the last bit, so from the first step that
+updates it the states agree to rounding (relative 1e-12 over the window
+tested, well inside the 1e-10 FP64 parity target) instead of bit for bit;
+every step before it is bitwise."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from volcanor_gb300 import cases as C
+from volcanor_gb300 import lib
+
+pytestmark = pytest.mark.gpu
+
+
+def hover(nt, presc_after=0, burst=0, skew=0.5, fd=3, axisym=0):
+    c = C.rotor_2blade_hover(nt=nt, n_nwake=12, truncate_nt=24, fd_scheme=fd)
+    geo = c.geom.replace("prescWakeAfterTruncNt = 0", f"prescWakeAfterTruncNt = {presc_after}")
+    geo = geo.replace("skewLimit = 0.5", f"skewLimit = {skew}")
+    geo = geo.replace("axisymmetrySwitch = 0", f"axisymmetrySwitch = {axisym}")
+    cfg = c.config.replace("wakeBurst = 0", f"wakeBurst = {burst}")
+    return cfg, geo
+
+
+def both(cfg, geo, n, chunk=16):
+    g = lib.Case(cfg, geo, precision=lib.PREC_FP64, sum_chunk=chunk)
+    g.start()
+    g.step(n)
+    r = O.Sim(cfg, geo)
+    r.set_sum_chunk(chunk)
+    r.start()
+    r.step(n)
+    return g, r
+
+
+@pytest.mark.parametrize("fd", [1, 3])
+def test_wake_burst_bitwise(fd):
+    cfg, geo = hover(50, burst=3, skew=0.02, fd=fd)
+    g, r = both(cfg, geo, 50)
+    np.testing.assert_array_equal(g.ct_hist(), r.ct_hist())
+    burst = 0
+    for b in (1, 2):
+        np.testing.assert_array_equal(g.get("waF_rvc", b), r.get("waF_rvc", b))
+        np.testing.assert_array_equal(g.get("waF", b), r.get("waF", b))
+        # a burst filament's core is the chord (0.08; grown since by dissipation)
+        burst += int(np.sum(g.get("waF_rvc", b) >= 0.08))
+    assert burst > 0  # the skew limit was reached
+
+
+@pytest.mark.parametrize("axisym", [0, 1])
+def test_prescribed_far_wake_matches_oracle(axisym):
+    cfg, geo = hover(44, presc_after=6, axisym=axisym)  # prescNt = 24 + 6 = 30
+    g, r = both(cfg, geo, 44)
+    a, b = g.ct_hist(), r.ct_hist()
+    np.testing.assert_array_equal(a[:31], b[:31])  # before the first update: bitwise
+    rel = np.abs(a[31:, 1] - b[31:, 1]) / np.abs(b[31:, 1])
+    assert rel.max() < 1e-12, rel.max()
+    assert np.any(np.abs(a[31:, 1] - a[30, 1]) > 1e-6)  # the helix acts on the loads
+    for bl in (1, 2):
+        wp, rp = g.get("waP", bl).reshape(-1, 2, 3), r.get("waP", bl).reshape(-1, 2, 3)
+        scale = np.abs(rp).max()
+        assert np.abs(wp - rp).max() < 1e-12 * scale
+        np.testing.assert_allclose(g.get("waP_gam", bl), r.get("waP_gam", bl), rtol=1e-12)
+        # the helix starts at the free far wake's oldest node
+        np.testing.assert_allclose(wp[0, 1], g.get("waF", bl).reshape(-1, 2, 3)[-1, 0], rtol=1e-12, atol=1e-15)
+
+
+def test_prescribed_far_wake_fp32_and_checkpoint(tmp_path):
+    cfg, geo = hover(50, presc_after=6, burst=4, skew=0.05)
+    g64 = lib.Case(cfg, geo, precision=lib.PREC_FP64)
+    g64.start()
+    a = g64.step(40)[:, 1]
+    g32 = lib.Case(cfg, geo, precision=lib.PREC_FP32_NEAR64)
+    g32.start()
+    b = g32.step(40)[:, 1]
+    assert np.max(np.abs(b - a) / np.abs(a)) < 1e-4
+    # checkpoint/resume carries the helix and its relaxation state
+    ck = tmp_path / "p.ckpt"
+    g64.checkpoint_save(ck)
+    ra = g64.step(10)
+    x = lib.Case(cfg, geo, precision=lib.PREC_FP64)
+    x.checkpoint_load(ck)
+    np.testing.assert_array_equal(ra, x.step(10))
+
+
+def test_prescribed_wake_needs_a_vertical_shaft():
+    cfg, geo = hover(44, presc_after=6)
+    geo = geo.replace("shaftAxis = 0.0, 0.0, 1.0", "shaftAxis = 0.0, 0.1, 1.0")
+    with pytest.raises(lib.VlmError) as e:
+        lib.Case(cfg, geo)
+    assert e.value.code == 4

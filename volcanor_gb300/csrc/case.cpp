@@ -144,7 +144,7 @@ struct Case {
       const int nFar = rowFar <= NF ? NF - rowFar + 1 : 0;
       const int nYoung = std::min(nFar, surrYoung);
       g.rec_begin = rec;
-      g.rec_count = farMode == 0 ? nNear + hs + nFar : (farMode == 1 ? nNear + hs + nYoung : nFar - nYoung);
+      g.rec_count = farMode == 0 ? nNear + hs + nFar + prescRecords(rowFar) : (farMode == 1 ? nNear + hs + nYoung : nFar - nYoung);
       g.kind = 1;
       g.blade = b;
       g.pad[0] = farMode == 2 ? 1 : 0;
@@ -167,6 +167,10 @@ struct Case {
     maxPart = std::max(maxPart, (int64_t)std::max(nq, 1) * M);
     maxTargets = std::max(maxTargets, M);
   }
+
+  // prescribed far-wake filaments a blade's wake sum holds (summed, when the
+  // case generates a prescribed wake, whenever the far wake exists)
+  int prescRecords(int rowFar) const { return d.prescNt > 0 && rowFar <= d.NF ? kPresc : 0; }
 
   void create(const std::string& cfg, const std::string& geo, const std::string& base, const vlm_options* o) {
     vlm_default_options(&opt);
@@ -197,6 +201,10 @@ struct Case {
     d.nonDimDenom = W.nonDimDenom;
     d.dissipAdd = (((4.0 * 1.2564) * P.apparentViscCoeff) * W.kinematicVisc) * W.dt;
     d.decay = std::exp(-(P.decayCoeff * W.dt));
+    d.prescNt = P.prescWakeNt;
+    d.prescGenNt = P.prescWakeGenNt;
+    d.skewLimit = P.skewLimit;
+    d.chord = P.chord;
     d.fl = frame_layout(d.nb, d.nc, d.ns);
     if (d.nc > 64) throw StatusError(VLM_ERR_UNSUPPORTED, "nc > 64 chordwise panels");
     if (d.n > 8192) throw StatusError(VLM_ERR_UNSUPPORTED, "more than 8192 panels per rotor");
@@ -230,6 +238,15 @@ struct Case {
       W.advance(k);
       W.write_frame(frames.data() + (size_t)k * d.fl.size);
       putAxes(k);
+    }
+    if (d.prescNt > 0) {
+      if (d.NF < 2) throw StatusError(VLM_ERR_UNSUPPORTED, "a prescribed far wake needs at least 2 far-wake filaments");
+      // classdef.f90:1009-1011, checked for every step that updates it
+      for (int k = d.prescNt + 1; k <= nt; ++k) {
+        const double* sh = frames.data() + (size_t)k * d.fl.size + d.fl.rot + 6;
+        if (std::fabs(sh[0]) > kEps || std::fabs(sh[1]) > kEps)
+          throw StatusError(VLM_ERR_UNSUPPORTED, "Prescribed far wake only implemented for shaft along Z-axis");
+      }
     }
     // plans
     plans.assign(nt + 1, StepPlan());
@@ -309,6 +326,12 @@ struct Case {
     for (int k = 0; k < 7; ++k) {
       s.vN[k] = dalloc<double>((size_t)nb * std::max(NW, 1) * (ns + 1) * 3, owned);
       s.vF[k] = dalloc<double>(nfar * 3, owned);
+    }
+    if (d.prescNt > 0) {
+      s.pfC = dalloc<double>((size_t)2 * nb * kPresc * 6, owned);
+      s.pfGam = dalloc<double>((size_t)2 * nb, owned);
+      s.pfRvc = dalloc<double>((size_t)2 * nb, owned);
+      s.pfHelix = dalloc<double>((size_t)2 * nb * 2, owned);
     }
     const size_t nsec = (size_t)nb * ns;
     s.secResVel = dalloc<double>(3 * nsec, owned);
@@ -401,6 +424,8 @@ struct Case {
 
   bool steadyStep(int k) const {
     if (!opt.use_graph || surr.on || k <= 3 || k <= W.sw.initWakeVelNt || W.sw.rotorForcePlot > 1) return false;
+    // a burst every wakeBurst steps, a prescribed far wake from step prescNt + 1
+    if (W.sw.wakeBurst != 0 || (d.prescNt > 0 && k <= d.prescNt + 1)) return false;
     return plans[k].rowNear == plans[k - 1].rowNear && plans[k].rowFar == plans[k - 1].rowFar;
   }
 
@@ -504,6 +529,7 @@ struct Case {
     }
     if (opt.precision == VLM_PREC_FP64) throw StatusError(VLM_ERR_INVALID, "the surrogate runs with the FP32 precisions only");
     if (d.NW == 0 || d.NF == 0) throw StatusError(VLM_ERR_UNSUPPORTED, "the surrogate needs a far wake");
+    if (d.prescNt > 0) throw StatusError(VLM_ERR_UNSUPPORTED, "the surrogate with a prescribed far wake");
     if (o.collect_steps <= 0 || o.sample_stride <= 0 || o.train_iters < 0 || o.batch <= 0 || o.audit_samples <= 0 ||
         o.hidden <= 0 || o.hidden > 1024 || o.layers < 2 || o.layers > kMlpMaxLayers || !(o.audit_tol > 0.0) ||
         !(o.lr > 0.f))
@@ -784,6 +810,7 @@ struct Case {
       launch_shed(d, s, fr, rN, true, stream);
       launch_age(d, s, rN, rF, stream);
       if (W.sw.wakeDissipation == 1) launch_dissipate(d, s, rN, rF, stream);
+      if (W.sw.wakeBurst != 0 && k % W.sw.wakeBurst == 0) launch_burst(d, s, rF, stream);
     }
     if (d.NW > 0) {
       const int Mcp = d.nbC * d.npan;
@@ -806,6 +833,13 @@ struct Case {
     }
   }
 
+  // rotor_convectwake (src/classdef.f90:4786-4830): shift + continuity +
+  // axisymmetric copies, then the prescribed far wake once it is active
+  void convect(int k, const double* fr, int rN, int rF, bool pred) {
+    launch_convect(d, s, fr, rN, rF, pred, stream);
+    if (d.prescNt > 0 && k > d.prescNt) launch_presc_update(d, s, fr, rF, pred, stream);
+  }
+
   // Phase 3 of step k (src/main.f90:799-1439): wake-node velocities, the
   // finite-difference scheme (predictor, predicted-wake velocities,
   // corrector), strain, roll-up / far-wake shift, trailing-edge shedding.
@@ -819,64 +853,64 @@ struct Case {
     evalNodes(k, false);
     switch (W.sw.fdScheme) {
       case 0:
-        launch_convect(d, s, fr, rN, rF, false, stream);
+        convect(k, fr, rN, rF, false);
         break;
       case 1:
         launch_copy_predicted(d, s, rN, rF, stream);
-        launch_convect(d, s, fr, rN, rF, true, stream);
+        convect(k, fr, rN, rF, true);
         evalNodes(k, true);
         launch_order2(d, s, rN, rF, stream);
-        launch_convect(d, s, fr, rN, rF, false, stream);
+        convect(k, fr, rN, rF, false);
         break;
       case 2:
         if (k == 1) {
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_COPY_0_TO_1, stream);
         } else {
           launch_velop(d, s, VOP_AB2, stream);
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
         }
         break;
       case 3:
         if (k == 1) {
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_COPY_0_TO_1, stream);
         } else {
           launch_copy_predicted(d, s, rN, rF, stream);
           launch_velop(d, s, VOP_AM2_PRED, stream);
-          launch_convect(d, s, fr, rN, rF, true, stream);
+          convect(k, fr, rN, rF, true);
           evalNodes(k, true);
           launch_velop(d, s, VOP_AM2_CORR, stream);
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_STEP_TO_1, stream);
         }
         break;
       case 4:
         // the reference tests iter == 0 for the start-up branch (never true)
         if (k == 2) {
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_COPY_0_TO_2, stream);
         } else {
           launch_copy_predicted(d, s, rN, rF, stream);
           launch_velop(d, s, VOP_AM3_PRED, stream);
-          launch_convect(d, s, fr, rN, rF, true, stream);
+          convect(k, fr, rN, rF, true);
           evalNodes(k, true);
           launch_velop(d, s, VOP_AM3_CORR, stream);
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_AM3_SHIFT, stream);
         }
         break;
       case 5:
         if (k <= 3) {
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, k == 1 ? VOP_COPY_0_TO_1 : (k == 2 ? VOP_COPY_0_TO_2 : VOP_COPY_0_TO_3), stream);
         } else {
           launch_copy_predicted(d, s, rN, rF, stream);
           launch_velop(d, s, VOP_AM4_PRED, stream);
-          launch_convect(d, s, fr, rN, rF, true, stream);
+          convect(k, fr, rN, rF, true);
           evalNodes(k, true);
           launch_velop(d, s, VOP_AM4_CORR, stream);
-          launch_convect(d, s, fr, rN, rF, false, stream);
+          convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_AM4_SHIFT, stream);
         }
         break;
@@ -1027,6 +1061,12 @@ struct Case {
       v.push_back({s.vN[k], nb * std::max(d.NW, 1) * (ns + 1) * 3 * D});
       v.push_back({s.vF[k], nfar * 3 * D});
     }
+    if (s.pfC) {
+      v.push_back({s.pfC, 2 * nb * kPresc * 6 * D});
+      v.push_back({s.pfGam, 2 * nb * D});
+      v.push_back({s.pfRvc, 2 * nb * D});
+      v.push_back({s.pfHelix, 2 * nb * 2 * D});
+    }
     if (refined) {
       v.push_back({s.LU32, n * n * sizeof(float)});
       v.push_back({s.AICinv32, n * n * sizeof(float)});
@@ -1175,7 +1215,7 @@ struct Case {
     long rings = (long)d.nb * d.npan, fils = 0;
     const int rowsN = d.NW - (pl.rowNear - 1);
     rings += (long)d.nb * rowsN * d.ns;
-    if (pl.rowFar <= d.NF) fils += (long)d.nb * (d.ns + d.NF - pl.rowFar + 1);
+    if (pl.rowFar <= d.NF) fils += (long)d.nb * (d.ns + d.NF - pl.rowFar + 1 + prescRecords(pl.rowFar));
     *ringPairs = (double)rings * M;
     *filPairs = (double)fils * M;
   }
@@ -1277,6 +1317,9 @@ struct Case {
       v = dget(s.vN[k[4] - '0'] + 3 * b * NW * (ns + 1), 3 * NW * (ns + 1));
     else if (bok && (k == "velF1" || k == "velF2" || k == "velF3")) v = dget(s.vF[k[4] - '0'] + 3 * b * NF, 3 * NF);
     else if (bok && k == "gamPrev") v = dget(s.gamPrev + b * npan, npan);
+    else if (bok && s.pfC && k == "waP") v = dget(s.pfC + (size_t)b * kPresc * 6, (size_t)kPresc * 6);
+    else if (bok && s.pfC && k == "waP_gam") v = dget(s.pfGam + b, 1);
+    else if (bok && s.pfC && k == "waP_rvc") v = dget(s.pfRvc + b, 1);
     else if (bok && k == "velKin") {
       // the prescribed kinematic velocity at the collocation points of the
       // current iteration (of the open step between its phases)
@@ -1332,7 +1375,7 @@ struct Case {
         const int hs = rF <= d.NF ? d.ns : 0;
         const int nFar = rF <= d.NF ? d.NF - rF + 1 : 0;
         q.rec_begin = rec;
-        q.rec_count = nNear + hs + nFar;
+        q.rec_count = nNear + hs + nFar + prescRecords(rF);
         q.kind = 1;
         q.blade = b;
         rec += q.rec_count;

@@ -237,6 +237,99 @@ __global__ void k_strain(Dims d, DevState s, int rowFar) {
   s.fRvc[r] = s.fRvc0[r] * sqrt(s.fL0[r] / lc);
 }
 
+// ---- prescribed far wake (classdef.f90:998-1066, 5172-5217) ----------------
+// One block per convecting blade.  Thread 0 sums the far-wake filaments
+// rowStart..NF in the reference's order (radius of node 1 about the z axis,
+// descent between consecutive nodes), relaxes the helix pitch and radius,
+// and finds the anchor (node 1 of the oldest filament); the threads then
+// place the 241 helix nodes about the hub, filament i running from node i+1
+// to node i, the first one attached at the anchor.  The helix angles use
+// the device's cos/sin/atan2, so the nodes agree with a host evaluation to a
+// few ulps, not bit for bit.
+__global__ void k_presc_update(Dims d, DevState s, const double* fr, int rowFar, int pred) {
+  const int b = blockIdx.x;
+  const int rowStart = d.prescGenNt == 0 ? rowFar : d.NF - d.prescGenNt;
+  const int i0 = rowStart - 1, i1 = d.NF - 1, n = i1 - i0 + 1;
+  const double* fc = (pred ? s.fCP : s.fC) + (size_t)b * d.NF * 6;
+  double* H = s.pfHelix + 2 * ((size_t)pred * d.nb + b);
+  __shared__ double sh[6];  // pitch, radius, anchor xyz, dTheta
+  if (threadIdx.x == 0) {
+    double pitch = 0.0, radius = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double* c = fc + 6 * (size_t)(i0 + i);
+      radius = radius + sqrt(c[1] * c[1] + c[0] * c[0]);
+      if (i < n - 1) pitch = pitch + c[2] - fc[6 * (size_t)(i0 + i + 1) + 2];
+    }
+    const double dpsi = fr[d.fl.rot + 9] * d.dt;
+    pitch = fabs(pitch) * (-kTwoPi / dpsi) / (double)(n - 1);
+    radius = radius / (double)n;
+    H[0] = 0.5 * pitch + (1.0 - 0.5) * H[0];
+    H[1] = 0.5 * radius + (1.0 - 0.5) * H[1];
+    const double* a = fc + 6 * (size_t)i1;
+    sh[0] = H[0];
+    sh[1] = H[1];
+    sh[2] = a[0], sh[3] = a[1], sh[4] = a[2];
+    sh[5] = atan2(a[1], a[0]);
+    s.pfGam[(size_t)pred * d.nb + b] = (pred ? s.fGam : s.fGam)[(size_t)b * d.NF + i1];
+    s.pfRvc[(size_t)pred * d.nb + b] = s.fRvc[(size_t)b * d.NF + i1];
+  }
+  __syncthreads();
+  __shared__ double node[3 * (kPresc + 1)];
+  const d3 hub = ld3(fr + d.fl.rot + 3);
+  const double dx = (kTwoPi * 10.0 - 0.0) / (double)kPresc;  // linspace(0, 2 pi nRevs, 241)
+  for (int i = threadIdx.x; i <= kPresc; i += blockDim.x) {
+    const double th = -1.0 * ((double)i * dx + 0.0);  // a clockwise helix (isClockwiseRotor)
+    node[3 * i] = hub.x + sh[1] * cos(th + sh[5]);
+    node[3 * i + 1] = hub.y + sh[1] * sin(th + sh[5]);
+    node[3 * i + 2] = hub.z + (sh[0] * fabs(th) / kTwoPi + (sh[4] - hub.z));
+  }
+  __syncthreads();
+  double* out = s.pfC + ((size_t)pred * d.nb + b) * kPresc * 6;
+  for (int i = threadIdx.x; i < kPresc; i += blockDim.x) {
+    for (int k = 0; k < 3; ++k) out[6 * i + k] = node[3 * (i + 1) + k];  // fc1
+    for (int k = 0; k < 3; ++k) out[6 * i + 3 + k] = i == 0 ? sh[2 + k] : node[3 * i + k];  // fc2
+  }
+}
+// Axisymmetric copies: blade b's prescribed wake = blade 1's, rotated about
+// the hub by b x 2 pi / nb (the wake copies' rotation).
+__global__ void k_presc_axisym(Dims d, DevState s, const double* fr, int pred) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (d.nb - 1) * kPresc) return;
+  const int b = 1 + t / kPresc, i = t % kPresc;
+  const m33 T = frameT(d, fr, b);
+  const d3 hub = ld3(fr + d.fl.rot + 3);
+  const double* src = s.pfC + ((size_t)pred * d.nb) * kPresc * 6 + 6 * (size_t)i;
+  double* dst = s.pfC + ((size_t)pred * d.nb + b) * kPresc * 6 + 6 * (size_t)i;
+  st3(dst, rot_about(T, ld3(src), hub));
+  st3(dst + 3, rot_about(T, ld3(src + 3), hub));
+  if (i == 0) {
+    s.pfGam[(size_t)pred * d.nb + b] = s.pfGam[(size_t)pred * d.nb];
+    s.pfRvc[(size_t)pred * d.nb + b] = s.pfRvc[(size_t)pred * d.nb];
+    s.pfHelix[2 * ((size_t)pred * d.nb + b)] = s.pfHelix[2 * (size_t)pred * d.nb];
+    s.pfHelix[2 * ((size_t)pred * d.nb + b) + 1] = s.pfHelix[2 * (size_t)pred * d.nb + 1];
+  }
+}
+
+// ---- wake burst (classdef.f90:4911-4917, 2306-2339) -------------------------
+// Far-wake filament i of every blade against filament i+1: skew =
+// |acos(cos(angle between fc2 - fc1 of i and fc1 - fc2 of i+1)) - pi| / pi;
+// at or above skewLimit both get the chord as core radius.  Only core radii
+// are written, from positions only, so the pairs run in parallel.
+__global__ void k_burst(Dims d, DevState s, int rowFar) {
+  const int rf = d.NF - (rowFar - 1) - 1;  // pairs (i, i+1)
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rf <= 0 || t >= d.nb * rf) return;
+  const int b = t / rf, i = rowFar - 1 + t % rf;
+  const size_t r = (size_t)b * d.NF + i;
+  const d3 a = ld3(s.fC + 6 * r + 3) - ld3(s.fC + 6 * r);
+  const d3 c = ld3(s.fC + 6 * (r + 1)) - ld3(s.fC + 6 * (r + 1) + 3);
+  const double skew = fabs(acos(dot3(a, c) / sqrt(dot3(a, a) * dot3(c, c))) - kPi) / kPi;
+  if (skew >= d.skewLimit) {
+    s.fRvc[r + 1] = d.chord;
+    s.fRvc[r] = d.chord;
+  }
+}
+
 // ---- far-wake shift for truncation (classdef.f90:4500-4513) ----------------
 __global__ void k_far_to_tmp(Dims d, DevState s) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -577,6 +670,22 @@ __global__ void k_gather(Dims d, DevState s, const double* fr, const Group* grou
     if (s.edgeW) {
       double* W = s.edgeW + 4 * (size_t)t;
       W[0] = R[16];
+      W[1] = W[2] = W[3] = 0.0;
+    }
+  } else if (l >= nNear + hs + (rowFar <= d.NF ? d.NF - rowFar + 1 : 0)) {
+    // prescribed far wake (classdef.f90:1471-1476): single filaments
+    const int i = l - nNear - hs - (d.NF - rowFar + 1);
+    const size_t pb = (size_t)pred * d.nb + b;
+    const double* f = s.pfC + (pb * kPresc + i) * 6;
+    for (int k = 0; k < 6; ++k) R[k] = f[k];
+    for (int k = 6; k < 12; ++k) R[k] = 0.0;
+    R[12] = s.pfRvc[pb];
+    R[13] = R[14] = R[15] = 0.0;
+    R[16] = s.pfGam[pb];
+    R[17] = (double)(REC_FIL | REC_SKIP);
+    if (s.edgeW) {
+      double* W = s.edgeW + 4 * (size_t)t;
+      W[0] = fabs(R[16]) > kEps ? R[16] : 0.0;
       W[1] = W[2] = W[3] = 0.0;
     }
   } else {
@@ -1266,6 +1375,23 @@ void launch_convect(const Dims& d, const DevState& s, const double* frame, int r
       count_launch();
       k_axisym<<<nblk(n3, 256), 256, 0, st>>>(d, s, frame, rowNear, rowFar, pred ? 1 : 0);
     }
+  }
+}
+void launch_presc_update(const Dims& d, const DevState& s, const double* frame, int rowFar, bool pred,
+                         cudaStream_t st) {
+  if (!s.pfC || d.NF - (rowFar - 1) < 1) return;
+  count_launch();
+  k_presc_update<<<d.nbC, 256, 0, st>>>(d, s, frame, rowFar, pred ? 1 : 0);
+  if (d.axisym && d.nb > 1) {
+    count_launch();
+    k_presc_axisym<<<nblk((long)(d.nb - 1) * kPresc, 256), 256, 0, st>>>(d, s, frame, pred ? 1 : 0);
+  }
+}
+void launch_burst(const Dims& d, const DevState& s, int rowFar, cudaStream_t st) {
+  const long n = (long)d.nb * (d.NF - (rowFar - 1) - 1);
+  if (n > 0) {
+    count_launch();
+    k_burst<<<nblk(n, 256), 256, 0, st>>>(d, s, rowFar);
   }
 }
 void launch_strain(const Dims& d, const DevState& s, int rowFar, cudaStream_t st) {

@@ -49,8 +49,17 @@ struct Dims {
   int rollupStart, rollupEnd;  // 1-based, as the reference
   int suppressFwake;
   double omega, theta0, density, dt, nonDimDenom, dissipAdd, decay;
+  // prescribed far wake (src/classdef.f90:998-1066, 5172-5217): active on
+  // iterations > prescNt when prescNt > 0; fitted to far-wake filaments
+  // rowStart..NF (rowStart = rowFar, or NF - prescGenNt when that is > 0)
+  int prescNt, prescGenNt;
+  // wake burst (src/classdef.f90:2306-2339): skew limit, large core radius
+  double skewLimit, chord;
   FrameLayout fl;
 };
+
+// Prescribed far wake: filaments per blade (10 revolutions of 15 degrees)
+constexpr int kPresc = 240;
 
 struct DevState {
   // wing (static)
@@ -69,6 +78,10 @@ struct DevState {
   double *nC, *nCP, *nGam, *nRvc, *nAge, *nTmp;
   // far wake
   double *fC, *fCP, *fGam, *fRvc, *fRvc0, *fL0, *fLc, *fAge, *fTmp;
+  // prescribed far wake [2: free wake, predicted wake][nb]: filaments
+  // [kPresc][fc1 xyz, fc2 xyz], one circulation and core radius per blade,
+  // helix pitch and radius (their relaxation state); null when the case has none
+  double *pfC, *pfGam, *pfRvc, *pfHelix;
   // node velocities: 0 vel, 1 vel1, 2 vel2, 3 vel3, 4 velPredicted, 5 velStep, 6 scratch
   double* vN[7];
   double* vF[7];
@@ -103,6 +116,12 @@ void launch_copy_predicted(const Dims& d, const DevState& s, int rowNear, int ro
 void launch_convect(const Dims& d, const DevState& s, const double* frame, int rowNear, int rowFar, bool pred,
                     cudaStream_t st);
 void launch_strain(const Dims& d, const DevState& s, int rowFar, cudaStream_t st);
+// the prescribed far wake of the free (pred = false) or predicted wake
+// fitted to its far wake, then copied and rotated to the other blades under
+// axisymmetry (classdef.f90:5172-5217)
+void launch_presc_update(const Dims& d, const DevState& s, const double* frame, int rowFar, bool pred, cudaStream_t st);
+// wake burst of every blade's far wake (classdef.f90:4911-4917, 2306-2339)
+void launch_burst(const Dims& d, const DevState& s, int rowFar, cudaStream_t st);
 void launch_rollup(const Dims& d, const DevState& s, int rowFar, cudaStream_t st);
 // velocity-history algebra over full arrays (blades < nbC)
 enum VelOp {

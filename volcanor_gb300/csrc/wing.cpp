@@ -242,7 +242,6 @@ void Wing::readConfig(const Namelist& c) {
   sw.initWakeVelNt = c.i("OPTIONS", "initWakeVelNt");
   sw.probe = c.i("OPTIONS", "probe");
   if (nr != 1) throw std::runtime_error("unsupported: nr > 1 (coupled rotors)");
-  if (sw.wakeBurst != 0) throw std::runtime_error("unsupported: wakeBurst");
   if (sw.restartFromNt != 0) throw std::runtime_error("unsupported: restartFromNt (use the case checkpoint API)");
   if (sw.fdScheme < 0 || sw.fdScheme > 5) throw std::runtime_error("fdScheme must be 0..5");
 }
@@ -310,6 +309,7 @@ void Wing::readGeom(const Namelist& g) {
   r.rollupEndRadius = g.d("WAKEPARAMS", "rollupEndRadius");
   r.initWakeVel = g.d("WAKEPARAMS", "initWakeVel");
   r.psiStart = g.d("WAKEPARAMS", "psiStart");
+  r.skewLimit = g.d("WAKEPARAMS", "skewLimit");
   r.bladeDynamicsSwitch = g.i("DYNAMICS", "bladeDynamicsSwitch");
   r.flapInitial = g.d("DYNAMICS", "flapInitial");
   r.dflapInitial = g.d("DYNAMICS", "dflapInitial");
@@ -568,7 +568,6 @@ void Wing::init() {
   toChordsRevs(r.gammaPlotSwitch);
   toChordsRevs(r.skewPlotSwitch);
   r.prescWakeNt = (r.wakeTruncateNt > 0 && r.prescWakeAfterTruncNt > 0) ? r.wakeTruncateNt + r.prescWakeAfterTruncNt : 0;
-  if (r.prescWakeNt > 0) throw std::runtime_error("unsupported: prescribed far wake");
   if (r.wakeTruncateNt > 0) r.wakeTruncateNt = std::max(r.wakeTruncateNt, r.nNwake + 1);
   if (r.surfaceType == 0) r.surfaceType = 1;
   if (r.nNwake > 0 && r.nNwake < 2) throw std::runtime_error("at least 2 near wake rows are required");

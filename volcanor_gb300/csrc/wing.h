@@ -48,6 +48,7 @@ struct RotorParams {  // rotor_readGeom inputs (src/classdef.f90:2541-2767)
   int customTrajectorySwitch = 0, forceCalcSwitch = 0;
   double pivotLE = 0, flapHinge = 0, apparentViscCoeff = 0, decayCoeff = 0, spanwiseCore = 0;
   int wakeTruncateNt = 0, prescWakeAfterTruncNt = 0, prescWakeGenNt = 0, prescWakeNt = 0;
+  double skewLimit = 0.0;  // wake burst: the turn (in units of pi) between far filaments that bursts them
   std::vector<double> streamwiseCoreVec;
   double rollupStartRadius = 0, rollupEndRadius = 0, initWakeVel = 0, psiStart = 0;
   int bladeDynamicsSwitch = 0, pitchDynamicsSwitch = 0, bodyDynamicsSwitch = 0;
