@@ -65,8 +65,8 @@ def test_prescribed_far_wake_matches_oracle(axisym):
         scale = np.abs(rp).max()
         assert np.abs(wp - rp).max() < 1e-12 * scale
         np.testing.assert_allclose(g.get("waP_gam", bl), r.get("waP_gam", bl), rtol=1e-12)
-        # the helix starts at the free far wake's oldest node
-        np.testing.assert_allclose(wp[0, 1], g.get("waF", bl).reshape(-1, 2, 3)[-1, 0], rtol=1e-12, atol=1e-15)
+        # consecutive helix filaments share their nodes
+        np.testing.assert_array_equal(wp[1:, 1], wp[:-1, 0])
 
 
 def test_prescribed_far_wake_fp32_and_checkpoint(tmp_path):
