@@ -77,7 +77,8 @@ def test_prescribed_far_wake_fp32_and_checkpoint(tmp_path):
     g32 = lib.Case(cfg, geo, precision=lib.PREC_FP32_NEAR64)
     g32.start()
     b = g32.step(40)[:, 1]
-    assert np.max(np.abs(b - a) / np.abs(a)) < 1e-4
+    # the helix drives CT through zero here: errors relative to the largest CT
+    assert np.max(np.abs(b - a)) / np.max(np.abs(a)) < 1e-4
     # checkpoint/resume carries the helix and its relaxation state
     ck = tmp_path / "p.ckpt"
     g64.checkpoint_save(ck)
