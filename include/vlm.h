@@ -180,7 +180,8 @@ int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows);
  * Between vlm_case_loads and vlm_case_wake_step the case holds the state the
  * reference writes its per-step files from (filaments2file, probes2file,
  * src/main.f90:788,795): vlm_case_get / vlm_case_get_wake /
- * vlm_case_vind_points read it there.  The three calls in sequence produce
+ * vlm_case_vind_points read it there (the wing arrays and rowNear / rowFar
+ * are those of the open step; iter stays at the last finished one).  The three calls in sequence produce
  * the same bits as vlm_case_step(c, 1, row) (loads called on the iterations
  * vlm_case_step computes them). */
 int vlm_case_aic_factor(vlm_case* c);

@@ -65,6 +65,8 @@ def lib():
         L.or_get.restype = i64
         L.or_sim_vind_points.argtypes = [vp, dp, i64, dp, i32]
         L.or_sim_skip_to.argtypes = [vp, i32]
+        L.or_sim_step_open.argtypes = [vp]
+        L.or_sim_step_close.argtypes = [vp]
         L.or_set.argtypes = [vp, cp, i32, dp, i64]
         L.or_vind_rings.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
         L.or_vind_filaments.argtypes = [dp, dp, dp, i64, dp, i64, dp, i32]
@@ -128,6 +130,14 @@ class Sim:
 
     def step(self, n: int = 1):
         _check(lib().or_sim_step(self._h, int(n)))
+
+    def step_open(self):
+        """The next iteration up to its loads (the reference's mid-step state)."""
+        _check(lib().or_sim_step_open(self._h))
+
+    def step_close(self):
+        """The rest of an opened iteration (the wake update)."""
+        _check(lib().or_sim_step_close(self._h))
 
     def skip_to(self, k: int):
         """Advance to iteration k with the prescribed kinematics only (no

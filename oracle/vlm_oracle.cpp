@@ -1982,6 +1982,12 @@ struct Sim {
 
   // main.f90:400-1452 (one iteration)
   void step() {
+    stepOpen();
+    stepClose();
+  }
+  // main.f90:400-764: the iteration up to its loads (the point where the
+  // reference writes filaments2file and probes2file, :788,795)
+  void stepOpen() {
     if (!started) start();
     if (iter >= nt) throw std::runtime_error("all timesteps done");
     advanceKinematics();
@@ -2003,6 +2009,9 @@ struct Sim {
       computeForces();
       force2file();
     }
+  }
+  // main.f90:799-1452: the rest of the iteration (wake update)
+  void stepClose() {
     if (sw.wakeSuppress == 0 && R.nNwake > 0) wakeUpdate();
   }
 
@@ -2280,6 +2289,10 @@ int or_test_freestream(void* h, int withOmega) {
 int or_dir_lift_drag(void* h) { return guarded([&]() { static_cast<Sim*>(h)->rotor_dirLiftDrag(); }); }
 int or_calc_sec_alpha(void* h) { return guarded([&]() { static_cast<Sim*>(h)->rotor_calc_secAlpha(); }); }
 int or_calc_force(void* h) { return guarded([&]() { static_cast<Sim*>(h)->rotor_calc_force(); }); }
+
+// One iteration in two halves: up to its loads, then the wake update.
+int or_sim_step_open(void* h) { return guarded([&]() { static_cast<Sim*>(h)->stepOpen(); }); }
+int or_sim_step_close(void* h) { return guarded([&]() { static_cast<Sim*>(h)->stepClose(); }); }
 
 // Kinematics-only advance to iteration k (see Sim::skipTo).
 int or_sim_skip_to(void* h, int k) { return guarded([&]() { static_cast<Sim*>(h)->skipTo(k); }); }

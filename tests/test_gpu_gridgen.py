@@ -132,3 +132,31 @@ def test_gridgen_run_matches_oracle_sums(tmp_path, fix):
     ref += np.array([10.0, 0.0, 0.0])
     # the file holds 16 significant digits; the GPU sums in blocks
     np.testing.assert_allclose(U.T, ref, rtol=0, atol=1e-12 * np.max(np.abs(ref)))
+
+
+def test_filament_file_taken_mid_step_matches_oracle_mid_step(tmp_path):
+    """The reference writes filamentsNNNNN.dat inside iteration NNNNN, after the
+    loads and before the wake update (src/main.f90:788): the step's separate
+    calls reach that state, and it equals the oracle's state at the same point."""
+    cfg, geo = _case()
+    g = lib.Case(cfg, geo, precision=lib.PREC_FP64, sum_chunk=16)
+    r = O.Sim(cfg, geo)
+    r.set_sum_chunk(16)
+    g.start()
+    r.start()
+    g.step(13)
+    r.step(13)
+    g.solve_circulation()
+    g.loads()
+    r.step_open()
+    assert g.geti("iter") == 13 and g.geti("rowFar") == r.geti("rowFar")
+    F = G.read_filaments(G.write_filaments(tmp_path / "filaments00014.dat", G.filaments_from_case(g)))
+    R = _oracle_filaments(r)
+    np.testing.assert_array_equal(F.vr_wing[:, FC_RVC_GAM_VR], R.vr_wing[:, FC_RVC_GAM_VR])
+    np.testing.assert_array_equal(F.vr_nwake[:, FC_RVC_GAM_VR], R.vr_nwake[:, FC_RVC_GAM_VR])
+    np.testing.assert_array_equal(F.vf_te[:, FC_RVC_VF], R.vf_te[:, FC_RVC_VF])
+    np.testing.assert_array_equal(F.vf_far[:, FC_RVC_VF], R.vf_far[:, FC_RVC_VF])
+    np.testing.assert_array_equal(F.gam_far, R.gam_far)
+    g.wake_step()
+    r.step_close()
+    np.testing.assert_array_equal(g.ct_hist(), r.ct_hist())

@@ -1337,7 +1337,8 @@ struct Case {
     else if (k == "forceDim") v = forceDim();
     else if (k == "profileWork") v = {profileWork[0], profileWork[1]};
     else if (bok && (k == "CP" || k == "nCap" || k == "vr")) {
-      auto f = dget(frame(iter), d.fl.size);
+      // the wing of the current iteration (of the open step between its phases)
+      auto f = dget(frame(phase != 0 ? iter + 1 : iter), d.fl.size);
       for (size_t p = 0; p < npan; ++p) {
         const double* r = f.data() + d.fl.pan + (b * npan + p) * kPan;
         if (k == "CP") v.insert(v.end(), r + 12, r + 15);
@@ -1972,7 +1973,8 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value) {
   if (!c || !name || !value) return VLM_ERR_INVALID;
   const std::string k = name;
   const Case& C = c->c;
-  const StepPlan& pl = C.plans[C.iter];
+  // rowNear/rowFar of the current iteration (of the open step between its phases)
+  const StepPlan& pl = C.plans[C.phase != 0 ? C.iter + 1 : C.iter];
   if (k == "nt") *value = C.W.nt;
   else if (k == "nb") *value = C.d.nb;
   else if (k == "nc") *value = C.d.nc;

@@ -140,6 +140,22 @@ class ResultsWriter:
             self._p("bladedynamics.csv").write_text(dynamics_header() + "\n")
             self._write_iteration(self.case.ct_hist()[0])
 
+    def step_with_snapshot(self, snapshot):
+        """Advances one step through the separate calls and calls
+        snapshot(case) between the loads and the wake update, where the
+        reference writes its per-step files (filaments2file, probes2file,
+        src/main.f90:788,795); writes the force files as run() does.
+        Returns (the step's CT row or None on an iteration without loads,
+        snapshot's result)."""
+        it = int(self.case.geti("iter")) + 1
+        self.case.solve_circulation()
+        row = self.case.loads() if self.plot > 0 and it % self.plot == 0 else None
+        result = snapshot(self.case)
+        self.case.wake_step()
+        if row is not None:
+            self._write_iteration(row)
+        return row, result
+
     def run(self, nsteps: int):
         """Advances nsteps steps; returns their (nsteps, 10) CT rows."""
         out = []

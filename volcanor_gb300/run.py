@@ -5,8 +5,9 @@ Reads the case's ``config.nml`` / ``geom01.nml`` (and PLOT3D files), runs
 its ``nt`` timesteps and writes ``Results/`` as the reference does:
 ``r01Params.json`` at start-up, the force files every ``rotorForcePlot``
 iterations (ForceNonDim, ForceDim, bYYForceDistNNNNN) and, every
-``gridPlot`` iterations once the far wake exists, ``filamentsNNNNN.dat``
-(taken between steps; see volcanor_gb300.gridgen).  The reference's own
+``gridPlot`` iterations once the far wake exists, ``filamentsNNNNN.dat``,
+taken where the reference takes it: inside the iteration, after its loads
+and before the wake update (the step's separate calls).  The reference's own
 post-processing (tests/test_*.py, parseResults.py) reads the directory
 unchanged.
 
@@ -41,14 +42,28 @@ def run_case(case_dir, precision: int = lib.PREC_FP64, steps: int | None = None,
     gp = grid_plot if grid_plot is not None else _grid_plot(d)
     rows, fil = None, []
     it = 0
+    def snapshot(c):
+        k = c.geti("iter") + 1
+        if c.geti("nFwake") > 0 and c.geti("rowFar") <= c.geti("nFwake"):
+            return G.write_filaments(out / f"filaments{k:05d}.dat", G.filaments_from_case(c))
+        return None
+
     while it < nt:
         k = nt - it
         if gp > 0:
             k = min(k, gp - it % gp)
-        rows = w.run(k)
+        if gp > 0 and (it + k) % gp == 0:
+            # the file iteration itself runs as separate calls, the file taken mid-step
+            if k > 1:
+                rows = w.run(k - 1)
+            row, f = w.step_with_snapshot(snapshot)
+            if row is not None:
+                rows = row[None, :]
+            if f is not None:
+                fil.append(f)
+        else:
+            rows = w.run(k)
         it += k
-        if gp > 0 and it % gp == 0 and case.geti("nFwake") > 0 and case.geti("rowFar") <= case.geti("nFwake"):
-            fil.append(G.write_filaments(out / f"filaments{it:05d}.dat", G.filaments_from_case(case)))
     return {"steps": nt, "wall_s": time.perf_counter() - t0, "last_row": None if rows is None else rows[-1],
             "filament_files": fil}
 
