@@ -415,6 +415,9 @@ def run_ours(args):
                               "core 0.002)")
             out[key] = k3
     tmpdir.cleanup()
+    if rank == 0 and not args.no_batch:
+        # the batched sweep of 256 uneven cases (its own steady state first)
+        out["batch"] = measure_batch(args, args.batch_cases, args.batch_steps, 3)
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -481,14 +484,12 @@ def run_reference(args):
     print(json.dumps(out))
 
 
-def run_batch(args):
-    """Batched sweep: 256 independent uneven rotor cases (volcanor_gb300/cases.py
-    batch_sweep) advanced together; after every case reached its steady state
-    each batch step is one CUDA-graph launch.  Reports case-timesteps/s."""
+def measure_batch(args, n: int, K: int, W: int):
+    """Batched sweep: n independent uneven rotor cases (volcanor_gb300/cases.py
+    batch_sweep) advanced together; once every case is in its steady state
+    each batch step is one CUDA-graph launch.  Returns case-timesteps/s."""
     from volcanor_gb300 import lib
     prec = {"fp32near": lib.PREC_FP32_NEAR64, "fp32": lib.PREC_FP32, "fp64": lib.PREC_FP64}[args.precision]
-    K, W = args.steps, args.warmup
-    n = args.batch_cases
     steady = 8 * 72 + 2
     cases = C.batch_sweep(n, seed=0, nt=steady + W + 2 * K)
     t0 = time.perf_counter()
@@ -511,18 +512,27 @@ def run_batch(args):
     for _ in range(K):
         b.step(1)
     e2e = n * K / (time.perf_counter() - t1)
-    out = {"metric": "batched free-wake case-timesteps/s", "value": round(value, 2), "unit": "case-timesteps/s",
-           "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
-           "data": f"synthetic ({n} seeded uneven rotor cases, volcanor_gb300/cases.py batch_sweep)",
-           "config": {"workload": f"{n} independent rotor cases: 2-4 blades, 24-400 rings, collective 2-12 deg, "
-                                  "advance ratio 0-0.3, wakes of 1-8 revolutions (5k-120k filaments), steady state, "
-                                  "one CUDA-graph launch per batch step", "precision": args.precision},
-           "e2e": {"value": round(e2e, 2), "unit": "case-timesteps/s",
-                   "h2d_bytes_per_step": None, "d2h_bytes_per_step": n * 80},
-           "gpu_launches": int(launches), "graph_launches_per_step": 1,
-           "warmup_wall_s": round(warm_s, 1), "clocks": clk.summary(),
-           "ct_finite": bool(np.all(np.isfinite(rows)))}
+    b.close()
+    return {"metric": "batched free-wake case-timesteps/s", "value": round(value, 2), "unit": "case-timesteps/s",
+            "steps": K, "warmup": W, "ms_per_step": round(ms / K, 4),
+            "workload": f"{n} independent rotor cases: 2-4 blades, 24-400 rings, collective 2-12 deg, advance ratio "
+                        "0-0.3, wakes of 1-8 revolutions (5k-120k filaments), steady state, one CUDA-graph launch "
+                        "per batch step", "precision": args.precision,
+            "e2e": {"value": round(e2e, 2), "unit": "case-timesteps/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": n * 80},
+            "gpu_launches": int(launches), "graph_launches_per_step": 1, "warmup_wall_s": round(warm_s, 1),
+            "clocks": clk.summary(), "ct_finite": bool(np.all(np.isfinite(rows)))}
+
+
+def run_batch(args):
+    """The batched sweep alone (--workload batch)."""
+    r = measure_batch(args, args.batch_cases, args.steps, args.warmup)
+    out = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"), "n_gpus": 1,
+           "steps": r.pop("steps"), "warmup": r.pop("warmup"), "ms_per_step": r.pop("ms_per_step"),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+           "data": f"synthetic ({args.batch_cases} seeded uneven rotor cases, volcanor_gb300/cases.py batch_sweep)",
+           "config": {"workload": r.pop("workload"), "precision": r.pop("precision")}}
+    out.update(r)
     print(json.dumps(out))
 
 
@@ -621,6 +631,8 @@ def main():
     ap.add_argument("--workload", default="hover2", choices=["hover2", "batch", "forward4"],
                     help="hover2: the headline 2-blade hover case; batch: 256 uneven cases in one graph launch")
     ap.add_argument("--batch-cases", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batch key of the default line")
+    ap.add_argument("--no-batch", action="store_true", help="leave the batched sweep out of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
