@@ -195,7 +195,9 @@ int vlm_case_wake_step(vlm_case* c);
 int vlm_case_get_wake(vlm_case* c, int blade, double* waN, double* waN_gam, double* waF, double* waF_gam);
 
 /* Integer state: nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter,
- * nbConvect, wakeTruncateNt, rotorForcePlot; nearPairs (near-field filament-target pairs of the
+ * nbConvect, wakeTruncateNt, rotorForcePlot, the output switches (wakePlot, wakeTipPlot, gridPlot,
+ * probe, wakeSuppress, skewPlotSwitch, inflowPlotSwitch, gammaPlotSwitch, after the reference's
+ * conversion of chords/revolutions), rollupStart, rollupEnd; nearPairs (near-field filament-target pairs of the
  * last FP32 evaluation) and nodeChunks (chunks of the next step's wake-node
  * evaluation) describe this library's kernels. */
 int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
@@ -203,6 +205,7 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  * the array is per blade.  Returns the element count, or -1 for an unknown
  * name.  Names and layouts (Fortran column-major, xyz fastest):
  *   dt, nonDimDenom, lu_residual    scalars (lu_residual: last refined solve, 0 without refinement)
+ *   Omega, theta0                   scalars: rotor speed (rad/s), collective pitch (rad)
  *   ct_hist                         (10, iter+1) CT rows so far
  *   AIC, AIC_inv                    (n, n); gamVec (n)
  *   gam (blade)                     (nc, ns) wing circulation
@@ -221,6 +224,9 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *                                   multi-step schemes (velNwake1..3, velFwake1..3)
  *   velKin (blade)                  (3, nc, ns) the kinematic velocity at the collocation points
  *                                   of the current iteration (during an open step, of that step)
+ *   hub                             (3) hub coordinates; yAxis (blade) (3) the blade's y axis;
+ *   secCP (blade)                   (3, ns) section points -- all of the current iteration
+ *                                   (of the open step between its phases)
  *   waP (blade)                     (3, 2, 240) the prescribed far wake's filaments (fc(:,1), fc(:,2)),
  *                                   cases with prescWakeAfterTruncNt > 0 only (src/classdef.f90:222-236)
  *   waP_gam, waP_rvc (blade)        scalars: its circulation and core radius
@@ -255,7 +261,10 @@ int64_t vlm_params_json(const char* config_text, const char* geom_text, const ch
 int64_t vlm_wing_kinematics(const char* config_text, const char* geom_text, const char* base_dir, int iter,
                             const char* name, int blade, double* out, int64_t cap);
 /* Induced velocity of the current wing + wake at M points (probes / gridgen:
- * src/libPostprocess.f90:333-361, src/gridgen.f90:115-140). */
+ * src/libPostprocess.f90:333-361, src/gridgen.f90:115-140).  Between the
+ * phases of an open step it is the state inside that iteration (the wing
+ * and wake rows of the open step), which is where the reference evaluates
+ * its probe and inflow files (src/main.f90:764-797). */
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V);
 /* Checkpoint / resume: replaces the reference's restart files
  * (Restart/restartNNNNN.dat written every restartWriteNt steps and read for

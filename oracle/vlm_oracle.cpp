@@ -2362,7 +2362,8 @@ int or_set(void* h, const char* name, int ib, const double* in, long n) {
   });
 }
 
-// Integer state: name in {nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter, nbConvect, ctRows}
+// Integer state: name in {nt, nb, nc, ns, n, nNwake, nFwake, rowNear, rowFar, iter, nbConvect, ctRows,
+// wakeTruncateNt, rollupStart, rollupEnd, wakeSuppress}
 long or_geti(void* h, const char* name) {
   Sim* s = static_cast<Sim*>(h);
   std::string k = name;
@@ -2382,6 +2383,7 @@ long or_geti(void* h, const char* name) {
   if (k == "wakeTruncateNt") return r.wakeTruncateNt;
   if (k == "rollupStart") return r.rollupStart;
   if (k == "rollupEnd") return r.rollupEnd;
+  if (k == "wakeSuppress") return s->sw.wakeSuppress;
   return -1;
 }
 
@@ -2399,7 +2401,7 @@ long or_geti(void* h, const char* name) {
 //   secLiftDir, secDragDir, secLift, secForceInertial, secLiftInPlane,
 //   secLiftOutPlane, secChordwiseResVel, secCP   [is][xyz]
 //   secCL, secTheta, secAlpha, secArea, secChord, forceDist   [is] (forceDist: [is][16])
-//   forceInertial, lift             xyz (blade)
+//   forceInertial, lift, yAxis      xyz (blade); hub: xyz (rotor)
 //   rotorLift, rotorForceInertial   xyz (rotor)
 //   waN                             [i + NW*j][filament][fc1, fc2] (all rows)
 //   waN_gam, waN_rvc                [i + NW*j], [i + NW*j][filament]
@@ -2422,6 +2424,7 @@ long or_get(void* h, const char* name, int ib, double* out, long cap) {
   else if (k == "ct_hist") { for (auto& row : s->ctHist) v.insert(v.end(), row.begin(), row.end()); }
   else if (k == "rotorLift") push3(r.lift);
   else if (k == "rotorForceInertial") push3(r.forceInertial);
+  else if (k == "hub") push3(r.hubCoords);
   else if (b) {
     if (k == "PC") { for (auto& p : b->wiP) for (int c = 0; c < 4; ++c) push3(p.PC[c]); }
     else if (k == "vr") { for (auto& p : b->wiP) for (int f = 0; f < 4; ++f) { push3(p.vr.vf[f].fc1); push3(p.vr.vf[f].fc2); } }
@@ -2441,6 +2444,7 @@ long or_get(void* h, const char* name, int ib, double* out, long cap) {
     else if (k == "secLiftOutPlane") { for (auto& a : b->secLiftOutPlane) push3(a); }
     else if (k == "secChordwiseResVel") { for (auto& a : b->secChordwiseResVel) push3(a); }
     else if (k == "secCP") { for (auto& a : b->secCP) push3(a); }
+    else if (k == "yAxis") push3(b->yAxis);
     else if (k == "secCL") v = b->secCL;
     else if (k == "secTheta") v = b->secTheta;
     else if (k == "secAlpha") v = b->secAlpha;

@@ -1288,6 +1288,8 @@ struct Case {
     const bool bok = b >= 0 && b < d.nb;
     const size_t npan = d.npan, NW = d.NW, NF = d.NF, ns = d.ns;
     if (k == "dt") v = {W.dt};
+    else if (k == "Omega") v = {d.omega};
+    else if (k == "theta0") v = {d.theta0};
     else if (k == "lu_residual") v = refine ? dget(s.luRes, 1) : std::vector<double>{0.0};
     else if (k == "nonDimDenom") v = {W.nonDimDenom};
     else if (k == "ct_hist") v = dget(s.ctHist, (size_t)(iter + 1) * 10);
@@ -1317,6 +1319,21 @@ struct Case {
       v = dget(s.vN[k[4] - '0'] + 3 * b * NW * (ns + 1), 3 * NW * (ns + 1));
     else if (bok && (k == "velF1" || k == "velF2" || k == "velF3")) v = dget(s.vF[k[4] - '0'] + 3 * b * NF, 3 * NF);
     else if (bok && k == "gamPrev") v = dget(s.gamPrev + b * npan, npan);
+    else if (k == "hub" || (bok && (k == "yAxis" || k == "secCP"))) {
+      // kinematics of the current iteration (of the open step between its phases)
+      const int fi = phase != 0 ? iter + 1 : iter;
+      const double* f = hFrames + (size_t)fi * d.fl.size;
+      if (k == "hub") v.assign(f + d.fl.rot + 3, f + d.fl.rot + 6);
+      else if (k == "yAxis") {
+        const double* ax = secAxes.data() + (size_t)fi * d.nb * (3 + 3 * ns) + (size_t)b * (3 + 3 * ns);
+        v.assign(ax, ax + 3);
+      } else {
+        for (size_t is = 0; is < ns; ++is) {
+          const double* sec = f + d.fl.sec + ((size_t)b * ns + is) * kSec + 6;
+          v.insert(v.end(), sec, sec + 3);
+        }
+      }
+    }
     else if (bok && s.pfC && k == "waP") v = dget(s.pfC + (size_t)b * kPresc * 6, (size_t)kPresc * 6);
     else if (bok && s.pfC && k == "waP_gam") v = dget(s.pfGam + b, 1);
     else if (bok && s.pfC && k == "waP_rvc") v = dget(s.pfRvc + b, 1);
@@ -1355,9 +1372,11 @@ struct Case {
     useDevice();
     if (!started) throw StatusError(VLM_ERR_STATE, "vlm_case_start must be called first");
     if (M <= 0) return;
-    // groups of the current state: wing + wake at the current rows
-    const StepPlan& pl = plans[std::max(iter, 1)];
-    const int rN = iter == 0 ? d.NW + 1 : pl.rowNear, rF = iter == 0 ? d.NF + 1 : pl.rowFar;
+    // groups of the current state: wing + wake at the current rows (of the
+    // open step between its phases)
+    const int fi = phase != 0 ? iter + 1 : iter;
+    const StepPlan& pl = plans[std::max(fi, 1)];
+    const int rN = fi == 0 ? d.NW + 1 : pl.rowNear, rF = fi == 0 ? d.NF + 1 : pl.rowFar;
     std::vector<Group> g;
     int rec = 0;
     for (int b = 0; b < d.nb; ++b) {
@@ -1403,7 +1422,7 @@ struct Case {
       DevState t = s;
       t.rec64 = rec64;
       t.edgeW = nullptr;  // ring by ring: the probe's record count is not the plans'
-      launch_gather(d, t, frame(iter), dg, (int)g.size(), rec, rN, rF, false, stream);
+      launch_gather(d, t, frame(fi), dg, (int)g.size(), rec, rN, rF, false, stream);
       if (opt.precision == VLM_PREC_FP64) {
         launch_partial64(rec64, dc, nq, dP, (int)M, part, stream);
       } else {
@@ -1988,6 +2007,16 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value) {
   else if (k == "nbConvect") *value = C.d.nbC;
   else if (k == "wakeTruncateNt") *value = C.W.P.wakeTruncateNt;
   else if (k == "rotorForcePlot") *value = C.W.sw.rotorForcePlot;
+  else if (k == "wakePlot") *value = C.W.sw.wakePlot;
+  else if (k == "wakeTipPlot") *value = C.W.sw.wakeTipPlot;
+  else if (k == "gridPlot") *value = C.W.sw.gridPlot;
+  else if (k == "probe") *value = C.W.sw.probe;
+  else if (k == "wakeSuppress") *value = C.W.sw.wakeSuppress;
+  else if (k == "skewPlotSwitch") *value = C.W.P.skewPlotSwitch;
+  else if (k == "inflowPlotSwitch") *value = C.W.P.inflowPlotSwitch;
+  else if (k == "gammaPlotSwitch") *value = C.W.P.gammaPlotSwitch;
+  else if (k == "rollupStart") *value = C.d.rollupStart;
+  else if (k == "rollupEnd") *value = C.d.rollupEnd;
   else if (k == "nearPairs" || k == "nodeChunks") {
     // near-field filament-target pairs of the last FP32 evaluation; chunks
     // of the next step's wake-node evaluation
