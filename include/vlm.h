@@ -125,12 +125,15 @@ int vlm_biot_savart_filaments_device(const double* fc, const double* rvc, const 
  * library, held on every device that loads the library until the process
  * exits.  Limits: N <= 16384 rings, M <= 65536 points; larger sizes return
  * VLM_ERR_INVALID with a message, as does a VLM_PREC_FP32_NEAR64 call with
- * more than 65536 near-field pairs.  The rings are summed in one block,
- * i.e. in the reference's order.
- * The first call on a device looks up the scratch array's device address
- * and keeps it for the life of the process, so make that first call before
- * any CUDA stream capture, and do not reset the device (cudaDeviceReset)
- * once it has been made.  All calls on a
+ * more than 65536 near-field pairs.  FP64 sums the rings in one block,
+ * i.e. in the reference's order; the FP32 precisions split them into as
+ * many blocks as fill the device (at most 256 and 65536 / M).
+ * The call waits for its stream before it returns, so it cannot be
+ * captured into a CUDA graph: on a capturing stream it returns
+ * VLM_ERR_INVALID without launching anything.  The first call on a device
+ * looks up the scratch array's device address and keeps it for the life of
+ * the process: do not reset the device (cudaDeviceReset) once it has been
+ * made.  All calls on a
  * device share the scratch and the call returns after its stream has
  * finished; calls that overlap on the GPU (other host threads or streams at
  * the same time) race on the scratch and must be serialised by the caller. */

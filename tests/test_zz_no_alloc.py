@@ -47,10 +47,11 @@ TOL = {lib.PREC_FP64: 1e-12, lib.PREC_FP32: 2e-5, lib.PREC_FP32_NEAR64: 2e-5}
 
 
 @pytest.mark.parametrize("precision", [lib.PREC_FP64, lib.PREC_FP32, lib.PREC_FP32_NEAR64])
-def test_noalloc_matches_allocating_entry_point_on_two_calls(precision):
+def test_noalloc_matches_allocating_entry_point_over_calls(precision):
     rng = np.random.default_rng(20 + precision)
-    for call in range(2):  # the second call reuses the scratch left by the first
-        N, M = (3000, 5000) if call == 0 else (16384, 1111)
+    # the later calls reuse the scratch left by the first; M = 64 splits the
+    # FP32 sums into the most chunks, M = 65536 leaves room for one
+    for N, M in ((3000, 5000), (16384, 1111), (16384, 64), (2000, 65536)):
         corners, rvc, gam = rings(rng, N)
         P = rng.uniform(0, 1, size=(M, 3))
         P[:10] = corners[:10, 2]  # targets on ring corners
@@ -78,3 +79,30 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     assert b"16384" in buf.value
     rc = L.vlm_biot_savart_rings_noalloc(None, None, None, 10, None, 65537, None, lib.PREC_FP32, None)
     assert rc == 1
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call waits for its stream, which a capturing stream cannot do: it
+    returns VLM_ERR_INVALID before it launches anything, and the capture
+    stays valid."""
+    L = lib.load()
+    rng = np.random.default_rng(3)
+    corners, rvc, gam = rings(rng, 10)
+    dev = torch.device("cuda")
+    tc, tr, tg = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (corners, rvc, gam))
+    tp = torch.rand(10, 3, dtype=torch.float64, device=dev)
+    tv = torch.zeros_like(tp)
+    x = torch.zeros(4, device=dev)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        x += 1.0
+        rc = L.vlm_biot_savart_rings_noalloc(tc.data_ptr(), tr.data_ptr(), tg.data_ptr(), 10, tp.data_ptr(), 10,
+                                             tv.data_ptr(), lib.PREC_FP64, ctypes.c_void_p(s.cuda_stream))
+    assert rc == 1
+    buf = ctypes.create_string_buffer(512)
+    L.vlm_last_error(buf, 512)
+    assert b"capturing" in buf.value
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(x.cpu(), torch.ones(4))

@@ -26,6 +26,9 @@ namespace {
 constexpr int64_t kMaxRings = 16384;
 constexpr int64_t kMaxPoints = 65536;
 constexpr int64_t kMaxNear = 65536;
+// Chunks of the FP32 sums (whose summation order is free): enough to fill the
+// device when M is small; M x chunks partials must fit the part buffer.
+constexpr int kMaxChunks = 256;
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kOffRec64 = 0;
@@ -35,7 +38,9 @@ constexpr size_t kOffNear = kOffPart + align256(kMaxPoints * 3 * sizeof(double))
 constexpr size_t kNearBytes = near_scratch_bytes((int)kMaxPoints, (size_t)kMaxNear);  // near-field grid + pair list
 constexpr size_t kOffNacc = kOffNear + align256(kNearBytes);
 constexpr size_t kOffTables = kOffNacc + align256(kMaxPoints * 3 * sizeof(long long));
-constexpr size_t kScratchBytes = kOffTables + 256;  // chunk, group, control words
+constexpr size_t kOffGroup = kOffTables + align256(kMaxChunks * sizeof(Chunk));
+constexpr size_t kOffCtl = kOffGroup + align256(sizeof(Group));
+constexpr size_t kScratchBytes = kOffCtl + 256;  // chunk table, group, control words
 
 // One fixed scratch area per device that loads the library, held until exit.
 // Every FP32 + FP64-near call clears the near-field accumulators it uses
@@ -47,22 +52,28 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 std::mutex g_mu;
 unsigned char* g_base[64] = {nullptr};
 
-// Resets the per-call tables in the scratch: one chunk spanning all rings
-// (the reference's summation order), one wing-kind group, zeroed control
-// words (error flag and near-pair count).
-__global__ void k_noalloc_tables(unsigned char* base, int N) {
-  if (threadIdx.x != 0) return;
+// The per-call chunk table, passed by value (2 KiB of kernel parameters).
+struct ChunkList {
+  int n;
+  Chunk c[kMaxChunks];
+};
+
+// Writes the per-call tables into the scratch: the chunk table, one
+// wing-kind group over all N rings, zeroed control words (error flag and
+// near-pair count).
+__global__ void k_noalloc_tables(unsigned char* base, ChunkList cl, int N) {
   Chunk* ch = reinterpret_cast<Chunk*>(base + kOffTables);
-  Group* g = reinterpret_cast<Group*>(base + kOffTables + 64);
-  int* ctl = reinterpret_cast<int*>(base + kOffTables + 128);
-  ch->rec_begin = 0;
-  ch->rec_count = N;
+  for (int q = threadIdx.x; q < cl.n; q += blockDim.x) ch[q] = cl.c[q];
+  if (threadIdx.x != 0) return;
+  Group* g = reinterpret_cast<Group*>(base + kOffGroup);
+  int* ctl = reinterpret_cast<int*>(base + kOffCtl);
   g->rec_begin = 0;
   g->rec_count = N;
   g->chunk_begin = 0;
-  g->chunk_count = N > 0 ? 1 : 0;
+  g->chunk_count = cl.n;
   g->kind = 0;
   g->blade = 0;
+  g->pad[0] = g->pad[1] = 0;
   for (int k = 0; k < 4; ++k) ctl[k] = 0;
 }
 
@@ -95,8 +106,13 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   if (M == 0) return VLM_OK;
   if ((N > 0 && (!corners || !rvc || !gam)) || !P || !V) return fail(VLM_ERR_INVALID, "null device pointer");
   cudaStream_t st = (cudaStream_t)stream;
+  // the call waits for its stream (below), which a capturing stream cannot do
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return fail(VLM_ERR_INVALID, "vlm_biot_savart_rings_noalloc cannot be called on a capturing stream");
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= 64) return fail(VLM_ERR_CUDA, "device ordinal out of range");
   unsigned char* base = nullptr;
@@ -118,26 +134,44 @@ extern "C" int vlm_biot_savart_rings_noalloc(const double* corners, const double
   unsigned char* near = base + kOffNear;
   long long* nacc = reinterpret_cast<long long*>(base + kOffNacc);
   Chunk* chunks = reinterpret_cast<Chunk*>(base + kOffTables);
-  Group* group = reinterpret_cast<Group*>(base + kOffTables + 64);
-  int* ctl = reinterpret_cast<int*>(base + kOffTables + 128);
+  Group* group = reinterpret_cast<Group*>(base + kOffGroup);
+  int* ctl = reinterpret_cast<int*>(base + kOffCtl);
 
+  // FP64: one chunk over all rings, the reference's summation order.  FP32:
+  // the chunks that fill the device (plan_chunks32), at most kMaxPoints / M
+  // so that the M x chunks partials and near-field accumulators fit.
+  ChunkList cl{};
+  cl.n = N > 0 ? 1 : 0;
+  cl.c[0] = Chunk{0, (int32_t)N};
+  if (N > 0 && precision != VLM_PREC_FP64) {
+    Group hg{0, (int32_t)N, 0, 0, 0, 0, {0, 0}};
+    const int capq = (int)std::min<int64_t>(kMaxChunks, kMaxPoints / M);
+    const int nq = plan_chunks32(&hg, 1, (int)M, partial32_slots(), cl.c, capq);
+    if (nq >= 1) {
+      cl.n = nq;
+    } else {
+      cl.n = 1;
+      cl.c[0] = Chunk{0, (int32_t)N};
+    }
+  }
   count_launch();
-  k_noalloc_tables<<<1, 32, 0, st>>>(base, (int)N);
+  k_noalloc_tables<<<1, 256, 0, st>>>(base, cl, (int)N);
   if (N > 0) {
     launch_rings_to_rec64(corners, rvc, gam, N, rec64, st);
     if (precision == VLM_PREC_FP64) {
       launch_partial64(rec64, chunks, 1, P, (int)M, part, st);
+      launch_combine(part, (int)M, group, 1, 2, V, st);
     } else {
       const bool nearOn = precision == VLM_PREC_FP32_NEAR64;
       if (nearOn) {
-        e = cudaMemsetAsync(nacc, 0, (size_t)M * 3 * sizeof(long long), st);
+        e = cudaMemsetAsync(nacc, 0, (size_t)M * cl.n * 3 * sizeof(long long), st);
         if (e != cudaSuccess) return fail(VLM_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
       }
       launch_pack32(rec64, (int)N, nearOn ? 4.0 : 0.0, rec32, st);
-      launch_partial32(rec32, rec64, chunks, 1, (int)N, P, (int)M, part, ctl, nearOn ? near : nullptr, kNearBytes, nacc,
-                       st);
+      launch_partial32(rec32, rec64, chunks, cl.n, (int)N, P, (int)M, part, ctl, nearOn ? near : nullptr, kNearBytes,
+                       nacc, st);
+      launch_combine_unordered(part, (int)M, group, 1, cl.n, 2, V, st);
     }
-    launch_combine(part, (int)M, group, 1, 2, V, st);
   } else {
     count_launch();
     k_zero<<<(unsigned)((3 * M + 255) / 256), 256, 0, st>>>(V, 3 * M);
