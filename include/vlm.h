@@ -381,6 +381,13 @@ int64_t vlm_mlp_param_count(const vlm_mlp* m);
 int vlm_mlp_get_params(vlm_mlp* m, float* out);
 int vlm_mlp_set_params(vlm_mlp* m, const float* in);
 int vlm_mlp_forward(vlm_mlp* m, const float* X, int64_t n, float* Y);
+/* Forward-pass arithmetic: 1 = tensor cores (tcgen05 MMAs, BF16 weights and
+ * activations, FP32 accumulation, all layers fused in one kernel; the
+ * default when every layer is at most 256 wide), 0 = FP32 CUDA cores (the
+ * arithmetic of training).  VLM_ERR_UNSUPPORTED if the network does not fit
+ * the tensor-core kernel.  get returns the current mode. */
+int vlm_mlp_set_inference(vlm_mlp* m, int mode);
+int vlm_mlp_get_inference(const vlm_mlp* m);
 /* Gradient of the batch MSE with respect to every parameter, and the loss. */
 int vlm_mlp_gradient(vlm_mlp* m, const float* X, const float* T, int64_t n, float* grad, float* loss);
 /* iters Adam steps (learning rate lr) over consecutive batches of the

@@ -32,6 +32,27 @@ def forward(p, sizes, X, keep=False):
     return H if keep else H[-1]
 
 
+def bf16(x):
+    """Rounds to the nearest BF16 value (ties to even), returned as float64:
+    the top 16 bits of the float32 after adding the rounding bias."""
+    f = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    u = f.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward_bf16(p, sizes, X):
+    """The tensor-core inference arithmetic: weights, inputs and every hidden
+    activation rounded to BF16, products summed exactly (FP64 here, FP32 on
+    the GPU), FP32 biases, tanh before the rounding."""
+    Ws, bs = unpack(np.asarray(p, dtype=np.float32).astype(np.float64), sizes)
+    H = bf16(X)
+    for l, (W, b) in enumerate(zip(Ws, bs)):
+        Z = H @ bf16(W).T + b
+        H = Z if l == len(Ws) - 1 else bf16(np.tanh(Z))
+    return H
+
+
 def loss(p, sizes, X, T):
     Y = forward(p, sizes, X)
     return float(np.mean((Y - np.asarray(T, dtype=np.float64)) ** 2))

@@ -63,3 +63,18 @@ def test_gpu_training_fits_a_smooth_function():
     print("validation loss ratio", l1 / l0)
     # the same network, data and schedule in PyTorch reach about 1e-3
     assert l1 < 0.005 * l0
+
+
+def test_bf16_rounding():
+    """Round to nearest, ties to even, at BF16's 8-bit significand."""
+    one = 1.0
+    assert MO.bf16(one) == 1.0
+    assert MO.bf16(1 + 2 ** -8) == 1.0                # halfway, even below
+    assert MO.bf16(1 + 3 * 2 ** -8) == 1 + 2 ** -6    # halfway, even above
+    assert MO.bf16(1 + 2 ** -8 + 2 ** -12) == 1 + 2 ** -7
+    assert MO.bf16(-3.0) == -3.0
+    x = np.random.default_rng(0).normal(0, 10, 10000).astype(np.float32)
+    r = MO.bf16(x)
+    assert np.all(np.abs(r - x) <= np.abs(x) * 2.0 ** -8)
+    torch = pytest.importorskip("torch")
+    assert np.array_equal(r, torch.from_numpy(x).to(torch.bfloat16).float().numpy().astype(np.float64))

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_EXACT = ["bs64.cu", "solver.cu"]
 CU_FAST = ["bs32.cu"]
-CU_PLAIN = ["noalloc.cu", "mlp.cu", "surrogate.cu", "peak.cu"]
+CU_PLAIN = ["noalloc.cu", "mlp.cu", "mlp_tc.cu", "surrogate.cu", "peak.cu"]
 CXX = ["wing.cpp", "case.cpp", "plan.cpp"]
 
 

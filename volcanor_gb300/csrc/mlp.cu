@@ -222,12 +222,30 @@ void Mlp::create(const std::vector<int>& sizes, uint64_t seed, cudaStream_t stre
   MLP_CUDA(cudaMemset(m, 0, sizeof(float) * sh.nparam));
   MLP_CUDA(cudaMemset(v, 0, sizeof(float) * sh.nparam));
   adamStep = 0;
+  tcFits = tc.plan(sh);
+  if (tcFits) {
+    MLP_CUDA(cudaMalloc(&tcImg, tc.imgBytes));
+    MLP_CUDA(cudaMalloc(&tcErr, sizeof(int)));
+    MLP_CUDA(cudaMemset(tcErr, 0, sizeof(int)));
+  }
+  useTc = tcFits;
+  tcStale = true;
+}
+
+bool Mlp::setTensorCores(bool on) {
+  if (on && !tcFits) return false;
+  useTc = on;
+  return true;
 }
 
 void Mlp::destroy() {
   for (float* q : {p, g, m, v, act, dact, loss, part})
     if (q) cudaFree(q);
   p = g = m = v = act = dact = loss = part = nullptr;
+  if (tcImg) cudaFree(tcImg);
+  if (tcErr) cudaFree(tcErr);
+  tcImg = nullptr;
+  tcErr = nullptr;
   cap = 0;
 }
 
@@ -244,6 +262,14 @@ void Mlp::reserve(int batch) {
 }
 
 void Mlp::forward(const float* X, int n, float* Y) {
+  if (useTc) {
+    if (tcStale) {
+      tc_pack(p, sh, tc, tcImg, st);
+      tcStale = false;
+    }
+    tc_forward(tc, tcImg, X, n, Y, tcErr, st);
+    return;
+  }
   const int chunk = std::max(cap, 1);
   for (int r0 = 0; r0 < n; r0 += chunk) {
     const int rows = std::min(chunk, n - r0);
@@ -302,6 +328,7 @@ void Mlp::grad(const float* X, const float* T, int n) {
 
 void Mlp::adam(float lr, float b1, float b2, float eps) {
   ++adamStep;
+  tcStale = true;
   const float c1 = 1.f - std::pow(b1, (float)adamStep), c2 = 1.f - std::pow(b2, (float)adamStep);
   count_launch();
   k_adam<<<(unsigned)((sh.nparam + 255) / 256), 256, 0, st>>>(p, g, m, v, sh.nparam, lr, b1, b2, eps, c1, c2);
@@ -380,8 +407,20 @@ extern "C" int vlm_mlp_set_params(vlm_mlp* h, const float* in) {
   if (!h || !in) return VLM_ERR_INVALID;
   return mlp_guard([&]() {
     MLP_CUDA(cudaMemcpy(h->net.p, in, sizeof(float) * h->net.sh.nparam, cudaMemcpyHostToDevice));
+    h->net.tcStale = true;
   });
 }
+
+extern "C" int vlm_mlp_set_inference(vlm_mlp* h, int mode) {
+  if (!h || mode < 0 || mode > 1) return VLM_ERR_INVALID;
+  if (!h->net.setTensorCores(mode == 1)) {
+    g_err = "vlm_mlp_set_inference: the network does not fit the tensor-core kernel (a layer wider than 256)";
+    return VLM_ERR_UNSUPPORTED;
+  }
+  return VLM_OK;
+}
+
+extern "C" int vlm_mlp_get_inference(const vlm_mlp* h) { return h ? (h->net.useTc ? 1 : 0) : -1; }
 
 extern "C" int vlm_mlp_forward(vlm_mlp* h, const float* X, int64_t n, float* Y) {
   if (!h || n < 0 || (n > 0 && (!X || !Y)) || n > (1 << 28)) return VLM_ERR_INVALID;
@@ -395,6 +434,14 @@ extern "C" int vlm_mlp_forward(vlm_mlp* h, const float* X, int64_t n, float* Y) 
     h->net.forward(h->dX, (int)n, h->dY);
     MLP_CUDA(cudaGetLastError());
     MLP_CUDA(cudaMemcpy(Y, h->dY, sizeof(float) * n * out, cudaMemcpyDeviceToHost));
+    if (h->net.useTc) {
+      int e = 0;
+      MLP_CUDA(cudaMemcpy(&e, h->net.tcErr, sizeof(int), cudaMemcpyDeviceToHost));
+      if (e) {
+        MLP_CUDA(cudaMemset(h->net.tcErr, 0, sizeof(int)));
+        throw std::runtime_error("tensor-core MLP: a bounded wait expired");
+      }
+    }
   });
 }
 

@@ -112,6 +112,8 @@ SIGNATURES = {
     "vlm_mlp_get_params": (ctypes.c_int, [_vp, _fp]),
     "vlm_mlp_set_params": (ctypes.c_int, [_vp, _fp]),
     "vlm_mlp_forward": (ctypes.c_int, [_vp, _fp, _i64, _fp]),
+    "vlm_mlp_set_inference": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "vlm_mlp_get_inference": (ctypes.c_int, [_vp]),
     "vlm_mlp_gradient": (ctypes.c_int, [_vp, _fp, _fp, _i64, _fp, _fp]),
     "vlm_mlp_train": (ctypes.c_int, [_vp, _fp, _fp, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_float, _fp]),
 }
@@ -452,6 +454,17 @@ class Mlp:
         Y = np.zeros((X.shape[0], self.sizes[-1]), dtype=np.float32)
         _err(load().vlm_mlp_forward(self._h, _fptr(X), X.shape[0], _fptr(Y)))
         return Y
+
+    INFER_FP32, INFER_TENSOR_CORES = 0, 1
+
+    def set_inference(self, mode: int) -> None:
+        """Forward-pass arithmetic: INFER_TENSOR_CORES (BF16 tcgen05 MMAs,
+        the default when the network fits) or INFER_FP32 (CUDA cores)."""
+        _err(load().vlm_mlp_set_inference(self._h, int(mode)))
+
+    @property
+    def inference(self) -> int:
+        return int(load().vlm_mlp_get_inference(self._h))
 
     def gradient(self, X, T):
         X = _f32(X).reshape(-1, self.sizes[0])
