@@ -37,6 +37,9 @@ def test_gpu_forward_and_gradient_match_oracle():
     net.set_params(p)
     p32 = net.get_params().astype(np.float64)
     X, T = batch(700)
+    # the FP32 CUDA-core forward pass (the arithmetic of training); the BF16
+    # tensor-core pass has its own bound in test_gpu_mlp_tc.py
+    net.set_inference(lib.Mlp.INFER_FP32)
     Y = net.forward(X)
     Yo = MO.forward(p32, SIZES, X.astype(np.float32))
     assert np.max(np.abs(Y - Yo)) < 1e-5 * max(1.0, np.max(np.abs(Yo)))
