@@ -313,6 +313,39 @@ int vlm_batch_step(vlm_batch* b, int nsteps, double* ct_rows);
 /* Device time of the last vlm_batch_step call (all cases), milliseconds. */
 int vlm_batch_last_step_ms(vlm_batch* b, double* ms);
 
+/* ---- coupled rotors (nr > 1) -------------------------------------------------
+ * Replaces the multi-rotor form of src/main.f90: rotor(nr) allocated and
+ * read from geom01.nml .. geomNN.nml (:17-39), and every induced-velocity sum
+ * of the iteration run over all rotors -- the initial solution with the other
+ * rotors' wings (:147-153), the RHS with every rotor's wake and the other
+ * rotors' wings (:549-561), the loads without every rotor's bound vortices
+ * (:632-652), and the wake-node velocities from every rotor's wing and wake
+ * (:808-827, 1052-1076) -- with each do-ir loop of the iteration run over the
+ * rotors in turn.  Every rotor is a lifting surface with a wake
+ * (surfaceType >= 0, nNwake > 0); image and non-lifting surfaces and
+ * sub-iterations (ntSub, ntSubInit) give VLM_ERR_UNSUPPORTED.  Rotor ir > 0
+ * is initialised with dt, nt and the switches as rotor ir - 1 left them
+ * (rotor_init's intent(inout) arguments, src/classdef.f90:2778-3011).  opt
+ * applies to every rotor; all rotors run on one stream; no graph replay.
+ * A rotor's vlm_case handle (vlm_system_rotor) serves the getters, files and
+ * checkpoint saves; stepping, phase, surrogate, point-query and checkpoint
+ * load calls on it return VLM_ERR_STATE. */
+typedef struct vlm_system vlm_system;
+int vlm_system_create(const char* config_text, int nr, const char* const* geom_texts, const char* base_dir,
+                      const vlm_options* opt, vlm_system** out);
+/* config.nml and geom01.nml .. geomNN.nml (NN = nr of config.nml) of a case directory */
+int vlm_system_create_from_dir(const char* case_dir, const vlm_options* opt, vlm_system** out);
+int vlm_system_destroy(vlm_system* y);
+int vlm_system_rotor_count(const vlm_system* y);
+/* Borrowed handle of rotor ir (0-based). */
+int vlm_system_rotor(vlm_system* y, int ir, vlm_case** out);
+int vlm_system_start(vlm_system* y);
+/* nsteps iterations of every rotor; ct_rows (if not NULL): nsteps x nr x 10
+ * (each rotor's rXXForceNonDim.csv row of each step). */
+int vlm_system_step(vlm_system* y, int nsteps, double* ct_rows);
+/* Device time of the last vlm_system_step call, milliseconds. */
+int vlm_system_last_step_ms(vlm_system* y, double* ms);
+
 /* ---- learned far-wake surrogate of a case -----------------------------------
  * No counterpart in the reference (it sums the far wake directly).  With the
  * FP32 precisions, the OLD far wake -- the rolled-up tip filaments behind the

@@ -57,6 +57,34 @@ module vlm_gb300
       integer(c_int), value :: nsteps
       real(c_double), intent(out) :: ct_rows(10, *)
     end function
+    ! coupled rotors (nr > 1): config.nml + geom01.nml .. geomNN.nml of a case
+    ! directory; rotor handles (0-based ir) serve vlm_case_get / _get_int
+    integer(c_int) function vlm_system_create_from_dir(dir, opt, ys) bind(c, name='vlm_system_create_from_dir')
+      import :: c_int, c_char, c_ptr, vlm_options
+      character(kind=c_char), intent(in) :: dir(*)
+      type(vlm_options), intent(in) :: opt
+      type(c_ptr), intent(out) :: ys
+    end function
+    integer(c_int) function vlm_system_rotor(ys, ir, cs) bind(c, name='vlm_system_rotor')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ys
+      integer(c_int), value :: ir
+      type(c_ptr), intent(out) :: cs
+    end function
+    integer(c_int) function vlm_system_start(ys) bind(c, name='vlm_system_start')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ys
+    end function
+    integer(c_int) function vlm_system_step(ys, nsteps, ct_rows) bind(c, name='vlm_system_step')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ys
+      integer(c_int), value :: nsteps
+      real(c_double), intent(out) :: ct_rows(10, *)
+    end function
+    integer(c_int) function vlm_system_destroy(ys) bind(c, name='vlm_system_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ys
+    end function
     integer(c_int) function vlm_case_get_int(cs, name, val) bind(c, name='vlm_case_get_int')
       import :: c_int, c_ptr, c_char, c_int64_t
       type(c_ptr), value :: cs

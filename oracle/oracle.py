@@ -75,6 +75,14 @@ def lib():
         L.or_matvec.argtypes = [dp, dp, i32, dp]
         L.or_lsq2.argtypes = [ctypes.c_double, dp, dp, i32]
         L.or_lsq2.restype = ctypes.c_double
+        L.or_sys_create.restype = vp
+        L.or_sys_create.argtypes = [i32, cp, ctypes.POINTER(cp), cp]
+        L.or_sys_free.argtypes = [vp]
+        L.or_sys_set_sum_chunk.argtypes = [vp, i32]
+        L.or_sys_start.argtypes = [vp]
+        L.or_sys_step.argtypes = [vp, i32]
+        L.or_sys_rotor.restype = vp
+        L.or_sys_rotor.argtypes = [vp, i32]
         _lib = L
     return _lib
 
@@ -195,6 +203,46 @@ class Sim:
         V = np.zeros_like(P)
         _check(lib().or_sim_vind_points(self._h, _ptr(P), P.shape[0], _ptr(V), int(predicted)))
         return V
+
+
+class _RotorView(Sim):
+    """One rotor of a System (the handle belongs to the system)."""
+
+    def __init__(self, handle, owner):
+        self._h = handle
+        self._owner = owner
+
+    def __del__(self):
+        pass
+
+
+class System:
+    """Coupled rotors (nr > 1): config.nml and one geomXX.nml per rotor,
+    stepped with every rotor's wing and wake in every induced-velocity sum."""
+
+    def __init__(self, config_text: str, geom_texts, base_dir: str | os.PathLike = ""):
+        L = lib()
+        g = [t.encode() for t in geom_texts]
+        arr = (ctypes.c_char_p * len(g))(*g)
+        self._h = L.or_sys_create(len(g), config_text.encode(), arr, str(base_dir).encode())
+        if not self._h:
+            raise OracleError(L.or_last_error().decode())
+        self.rotors = [_RotorView(L.or_sys_rotor(self._h, i), self) for i in range(len(g))]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().or_sys_free(h)
+            self._h = None
+
+    def set_sum_chunk(self, c: int):
+        _check(lib().or_sys_set_sum_chunk(self._h, int(c)))
+
+    def start(self):
+        _check(lib().or_sys_start(self._h))
+
+    def step(self, n: int = 1):
+        _check(lib().or_sys_step(self._h, int(n)))
 
 
 def vind_rings(corners, rvc, gam, P, chunk: int = 0) -> np.ndarray:

@@ -38,6 +38,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <memory>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -606,6 +607,12 @@ struct Sim {
   int nthreads = 0;
   int sumChunk = 0;  // see ChunkSum
   bool started = false;
+  // Rotors of a coupled system (nr > 1, main.f90:17-29), in rotor order,
+  // this one at index self; empty for a lone rotor.  Every induced-velocity
+  // sum over "all rotors" of the reference's loop runs over sys.
+  std::vector<Sim*> sys;
+  int self = 0;
+  bool member = false;  // created as a rotor of a system: nr > 1 allowed
 
   // ---- blade kinematics -------------------------------------------------
   // classdef.f90:1092-1112
@@ -1021,6 +1028,14 @@ struct Sim {
     return acc;
   }
 
+  // main.f90:808-827: the zeroed node velocity plus vind_on?wake_byRotor
+  // (libCommon.f90:114-211: wing + wake of a rotor) of every rotor in turn
+  V3 byAllRotors(V3 P, bool pred) const {
+    if (sys.empty()) return V3() + (rotor_vind_bywing(P) + rotor_vind_bywake(P, pred));
+    V3 a;
+    for (const Sim* o : sys) a = a + (o->rotor_vind_bywing(P) + o->rotor_vind_bywake(P, pred));
+    return a;
+  }
   // libCommon.f90:114-211 for blade ib; writes vel (rows rowNear..NW) and velF (rowFar..NF)
   void vind_onWake(int ib, bool pred, std::vector<V3>& velN, std::vector<V3>& velF) {
     const Blade& b = R.blade[ib];
@@ -1035,13 +1050,11 @@ struct Sim {
       if (t < nT) {
         int j = t / rows, i = R.rowNear - 1 + t % rows;
         V3 P = j < ns ? wn[i + NW * j].vf[1].fc1 : wn[i + NW * (ns - 1)].vf[2].fc1;
-        V3 v = rotor_vind_bywing(P) + rotor_vind_bywake(P, pred);
-        velN[i + NW * j] = V3() + v;
+        velN[i + NW * j] = byAllRotors(P, pred);
       } else {
         int i = R.rowFar - 1 + (t - nT);
         V3 P = wf[i].vf.fc1;
-        V3 v = rotor_vind_bywing(P) + rotor_vind_bywake(P, pred);
-        velF[i] = V3() + v;
+        velF[i] = byAllRotors(P, pred);
       }
     }
   }
@@ -1345,7 +1358,13 @@ struct Sim {
     return v;
   }
   void solveCirculation(bool withWake) {
-    int nc = R.nc, ns = R.ns, n = R.n();
+    computeRHS(withWake);
+    solveRHS();
+  }
+  // main.f90:522-591 (and :120-183 without the wake): velCP and the RHS;
+  // in a system the wake of every rotor and the wings of the others
+  void computeRHS(bool withWake) {
+    int nc = R.nc, ns = R.ns;
     std::fill(R.RHS.begin(), R.RHS.end(), 0.0);
     int tot = R.nbConvect * ns * nc;
 #pragma omp parallel for schedule(static)
@@ -1356,13 +1375,24 @@ struct Sim {
       int row = ic + nc * is + ns * nc * ib;
       p.velCP = kinematicVelCP(b, is, p.CP);
       p.velCPm = p.velCP;
-      if (withWake) p.velCP = p.velCP + rotor_vind_bywake(p.CP, false);
+      if (sys.empty()) {
+        if (withWake) p.velCP = p.velCP + rotor_vind_bywake(p.CP, false);
+      } else {
+        for (size_t jr = 0; jr < sys.size(); ++jr) {
+          if (withWake) p.velCP = p.velCP + sys[jr]->rotor_vind_bywake(p.CP, false);
+          if ((int)jr != self) p.velCP = p.velCP + sys[jr]->rotor_vind_bywing(p.CP);
+        }
+      }
       R.RHS[row] = dot(p.velCP, p.nCap);
     }
     if (R.axisymmetrySwitch == 1)
       for (int ib = 1; ib < R.nb; ++ib)
         for (int k = 0; k < nc * ns; ++k) R.RHS[nc * ns * ib + k] = R.RHS[k];
     for (auto& r : R.RHS) r = -1.0 * r;
+  }
+  // main.f90:594-603: gamVec = AIC_inv RHS, map_gam
+  void solveRHS() {
+    const int n = R.n();
     R.gamVecPrev = R.gamVec;
     matvec(R.AIC_inv, R.RHS, R.gamVec, n);
     map_gam();
@@ -1393,7 +1423,9 @@ struct Sim {
       int ic = t % nc, is = (t / nc) % ns, ib = t / (nc * ns);
       WingPanel& p = R.blade[ib].w(ic, is);
       p.velCPTotal = p.velCP;
-      p.velCPTotal = p.velCPTotal - rotor_vind_bywing_boundVortices(p.CP);
+      if (sys.empty()) p.velCPTotal = p.velCPTotal - rotor_vind_bywing_boundVortices(p.CP);
+      else
+        for (const Sim* o : sys) p.velCPTotal = p.velCPTotal - o->rotor_vind_bywing_boundVortices(p.CP);
       p.velCPTotal = p.velCPTotal + rotor_vind_bywing(p.CP);
     }
     if (R.axisymmetrySwitch == 1)
@@ -1503,7 +1535,9 @@ struct Sim {
     sw.fdScheme = c.i("OPTIONS", "fdScheme");
     sw.initWakeVelNt = c.i("OPTIONS", "initWakeVelNt");
     sw.probe = c.i("OPTIONS", "probe");
-    if (nr != 1) throw std::runtime_error("only nr = 1 is supported by this oracle");
+    if (nr != 1 && !member) throw std::runtime_error("nr > 1: create the rotors as a system (or_sys_create)");
+    if (member && (sw.ntSub != 0 || sw.ntSubInit != 0))
+      throw std::runtime_error("coupled rotors: sub-iterations (ntSub, ntSubInit) are not supported");
   }
   void readGeom(const Namelist& g) {
     std::string ver = g.s("VERSION", "fileFormatVersion", "");
@@ -1947,6 +1981,20 @@ struct Sim {
 
   // main.f90:43-58, 62-81, 95-377
   void start() {
+    startGeometry();
+    for (int i = 0; i <= sw.ntSubInit; ++i) {
+      solveCirculation(false);
+      if (sw.ntSubInit != 0) {
+        double s = 0.0;
+        for (int k = 0; k < R.n(); ++k) s = s + (R.gamVec[k] - R.gamVecPrev[k]) * (R.gamVec[k] - R.gamVecPrev[k]);
+        if (std::sqrt(s) <= EPS) break;
+      }
+    }
+    startWake();
+    startLoads();
+  }
+  // main.f90:43-58, 62-81, 95-116: initial pitch, AIC and its inverse, rotor speed
+  void startGeometry() {
     for (int ib = 0; ib < R.nb; ++ib) {
       Blade& b = R.blade[ib];
       b.theta = gettheta(R.psiStart, ib + 1);
@@ -1961,17 +2009,15 @@ struct Sim {
       R.velBody = R.velBodyHistory[0];
       R.omegaBody = R.omegaBodyHistory[0];
     }
-    for (int i = 0; i <= sw.ntSubInit; ++i) {
-      solveCirculation(false);
-      if (sw.ntSubInit != 0) {
-        double s = 0.0;
-        for (int k = 0; k < R.n(); ++k) s = s + (R.gamVec[k] - R.gamVecPrev[k]) * (R.gamVec[k] - R.gamVecPrev[k]);
-        if (std::sqrt(s) <= EPS) break;
-      }
-    }
+  }
+  // main.f90:226-233: wake rows and the first trailing-edge shed row
+  void startWake() {
     R.rowFar = R.nFwake + 1;
     R.rowNear = R.nNwake + 1;
     if (R.nNwake > 0) assignshed(false);
+  }
+  // main.f90:235-377: the loads of the initial solution
+  void startLoads() {
     if (sw.rotorForcePlot != 0) {
       computeForces();
       for (auto& b : R.blade) b.MflapLiftPrev = b.MflapLift;
@@ -1991,12 +2037,7 @@ struct Sim {
     if (!started) start();
     if (iter >= nt) throw std::runtime_error("all timesteps done");
     advanceKinematics();
-    if (sw.wakeSuppress == 0 && R.nNwake > 0) {
-      assignshed(true);
-      age_wake();
-      if (sw.wakeDissipation == 1) dissipate_wake();
-      if (sw.wakeBurst != 0 && iter % sw.wakeBurst == 0) burst_wake();
-    }
+    preWake();
     for (int i = 0; i <= sw.ntSub; ++i) {
       solveCirculation(true);
       if (sw.ntSub != 0) {
@@ -2008,6 +2049,15 @@ struct Sim {
     if (sw.rotorForcePlot != 0 && iter % sw.rotorForcePlot == 0) {
       computeForces();
       force2file();
+    }
+  }
+  // main.f90:464-490: leading-edge shed row, ageing, dissipation, burst
+  void preWake() {
+    if (sw.wakeSuppress == 0 && R.nNwake > 0) {
+      assignshed(true);
+      age_wake();
+      if (sw.wakeDissipation == 1) dissipate_wake();
+      if (sw.wakeBurst != 0 && iter % sw.wakeBurst == 0) burst_wake();
     }
   }
   // main.f90:799-1452: the rest of the iteration (wake update)
@@ -2090,16 +2140,106 @@ struct Sim {
       for (size_t k = 0; k < b.velF.size(); ++k) f(b.velF[k], b.velF1[k], b.velF2[k], b.velF3[k], b.velFP[k], b.velFStep[k]);
     }
   }
-  // main.f90:799-1439
+  // main.f90:799-1439, run as four stages so that a system of rotors runs
+  // each stage for every rotor before the next (the reference's do-ir loops):
+  // 0 the node velocities, 1 the scheme up to the predicted wake, 2 the
+  // predicted-wake velocities, 3 the corrector, strain and roll-up.
   void wakeUpdate() {
-    evalWakeVel(false);
+    for (int st = 0; st < 4; ++st) wakeStage(st);
+  }
+  // whether this iteration's scheme evaluates the predicted wake
+  bool predicts() const {
+    switch (sw.fdScheme) {
+      case 1: return true;
+      case 3: return iter != 1;
+      case 4: return iter != 2;  // the reference tests iter == 0 (never true), main.f90:1118
+      case 5: return iter > 3;
+      default: return false;
+    }
+  }
+  void wakeStage(int st) {
     int fd = sw.fdScheme;
+    if (st == 0) {
+      evalWakeVel(false);
+      return;
+    }
+    if (st == 2) {
+      if (predicts()) evalWakeVel(true);
+      return;
+    }
+    if (st == 3) {
+      wakeCorrector();
+      if (sw.wakeStrain == 1) strain_wake();
+      if (R.rowNear == 1) { rollup(); assignshed(false); }
+      else assignshed(false);
+      return;
+    }
+    // st == 1: the scheme up to its predicted wake (all of it when it has none)
     if (fd == 0) {
       rotor_convectwake(false);
     } else if (fd == 1) {
       copyPredicted();
       rotor_convectwake(true);
-      evalWakeVel(true);
+    } else if (fd == 2) {
+      if (iter == 1) {
+        rotor_convectwake(false);
+        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3&) { v1 = v; });
+      } else {
+        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3& st) {
+          st = 0.5 * (3.0 * v - v1);
+          v1 = st;
+          v = st;
+        });
+        rotor_convectwake(false);
+      }
+    } else if (fd == 3) {
+      if (iter == 1) {
+        rotor_convectwake(false);
+        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3&) { v1 = v; });
+      } else {
+        copyPredicted();
+        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3& st) {
+          st = v;
+          v = 0.5 * (3.0 * v - v1);
+        });
+        rotor_convectwake(true);
+      }
+    } else if (fd == 4) {
+      if (iter == 2) {
+        rotor_convectwake(false);
+        forAllVel([](V3& v, V3&, V3& v2, V3&, V3&, V3&) { v2 = v; });
+      } else {
+        copyPredicted();
+        forAllVel([](V3& v, V3& v1, V3& v2, V3&, V3&, V3& st) {
+          st = v;
+          v = ((23.0 * v - 16.0 * v2) + 5.0 * v1) / 12.0;
+        });
+        rotor_convectwake(true);
+      }
+    } else if (fd == 5) {
+      if (iter <= 3) {
+        rotor_convectwake(false);
+        int it = iter;
+        forAllVel([it](V3& v, V3& v1, V3& v2, V3& v3, V3&, V3&) {
+          if (it == 1) v1 = v; else if (it == 2) v2 = v; else v3 = v;
+        });
+      } else {
+        copyPredicted();
+        forAllVel([](V3& v, V3& v1, V3& v2, V3& v3, V3&, V3& st) {
+          st = v;
+          v = (((55.0 * v - 59.0 * v3) + 37.0 * v2) - 9.0 * v1) / 24.0;
+        });
+        rotor_convectwake(true);
+      }
+    } else {
+      throw std::runtime_error("bad fdScheme");
+    }
+  }
+  // the schemes' corrector (after the predicted-wake velocities)
+  void wakeCorrector() {
+    if (!predicts()) return;
+    int fd = sw.fdScheme;
+    if (fd == 1) {
       // libCommon.f90:213-258: stencil indices are relative to rowNear/rowFar
       int NW = R.nNwake, ns = R.ns;
       for (int ib = 0; ib < R.nbConvect; ++ib) {
@@ -2127,78 +2267,92 @@ struct Sim {
         }
       }
       rotor_convectwake(false);
-    } else if (fd == 2) {
-      if (iter == 1) {
-        rotor_convectwake(false);
-        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3&) { v1 = v; });
-      } else {
-        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3& st) {
-          st = 0.5 * (3.0 * v - v1);
-          v1 = st;
-          v = st;
-        });
-        rotor_convectwake(false);
-      }
     } else if (fd == 3) {
-      if (iter == 1) {
-        rotor_convectwake(false);
-        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3&) { v1 = v; });
-      } else {
-        copyPredicted();
-        forAllVel([](V3& v, V3& v1, V3&, V3&, V3&, V3& st) {
-          st = v;
-          v = 0.5 * (3.0 * v - v1);
-        });
-        rotor_convectwake(true);
-        evalWakeVel(true);
-        forAllVel([](V3& v, V3&, V3&, V3&, V3& vp, V3& st) { v = (vp + st) * 0.5; });
-        rotor_convectwake(false);
-        forAllVel([](V3&, V3& v1, V3&, V3&, V3&, V3& st) { v1 = st; });
-      }
+      forAllVel([](V3& v, V3&, V3&, V3&, V3& vp, V3& st) { v = (vp + st) * 0.5; });
+      rotor_convectwake(false);
+      forAllVel([](V3&, V3& v1, V3&, V3&, V3&, V3& st) { v1 = st; });
     } else if (fd == 4) {
-      // the reference tests iter == 0 here (never true), main.f90:1118
-      if (iter == 2) {
-        rotor_convectwake(false);
-        forAllVel([](V3& v, V3&, V3& v2, V3&, V3&, V3&) { v2 = v; });
-      } else {
-        copyPredicted();
-        forAllVel([](V3& v, V3& v1, V3& v2, V3&, V3&, V3& st) {
-          st = v;
-          v = ((23.0 * v - 16.0 * v2) + 5.0 * v1) / 12.0;
-        });
-        rotor_convectwake(true);
-        evalWakeVel(true);
-        forAllVel([](V3& v, V3&, V3& v2, V3&, V3& vp, V3& st) { v = ((5.0 * vp + 8.0 * st) - 1.0 * v2) / 12.0; });
-        rotor_convectwake(false);
-        forAllVel([](V3&, V3& v1, V3& v2, V3&, V3&, V3& st) { v1 = v2; v2 = st; });
-      }
+      forAllVel([](V3& v, V3&, V3& v2, V3&, V3& vp, V3& st) { v = ((5.0 * vp + 8.0 * st) - 1.0 * v2) / 12.0; });
+      rotor_convectwake(false);
+      forAllVel([](V3&, V3& v1, V3& v2, V3&, V3&, V3& st) { v1 = v2; v2 = st; });
     } else if (fd == 5) {
-      if (iter <= 3) {
-        rotor_convectwake(false);
-        int it = iter;
-        forAllVel([it](V3& v, V3& v1, V3& v2, V3& v3, V3&, V3&) {
-          if (it == 1) v1 = v; else if (it == 2) v2 = v; else v3 = v;
-        });
-      } else {
-        copyPredicted();
-        forAllVel([](V3& v, V3& v1, V3& v2, V3& v3, V3&, V3& st) {
-          st = v;
-          v = (((55.0 * v - 59.0 * v3) + 37.0 * v2) - 9.0 * v1) / 24.0;
-        });
-        rotor_convectwake(true);
-        evalWakeVel(true);
-        forAllVel([](V3& v, V3&, V3& v2, V3& v3, V3& vp, V3& st) {
-          v = (((9.0 * vp + 19.0 * st) - 5.0 * v3) + 1.0 * v2) / 24.0;
-        });
-        rotor_convectwake(false);
-        forAllVel([](V3&, V3& v1, V3& v2, V3& v3, V3&, V3& st) { v1 = v2; v2 = v3; v3 = st; });
-      }
-    } else {
-      throw std::runtime_error("bad fdScheme");
+      forAllVel([](V3& v, V3&, V3& v2, V3& v3, V3& vp, V3& st) {
+        v = (((9.0 * vp + 19.0 * st) - 5.0 * v3) + 1.0 * v2) / 24.0;
+      });
+      rotor_convectwake(false);
+      forAllVel([](V3&, V3& v1, V3& v2, V3& v3, V3&, V3& st) { v1 = v2; v2 = v3; v3 = st; });
     }
-    if (sw.wakeStrain == 1) strain_wake();
-    if (R.rowNear == 1) { rollup(); assignshed(false); }
-    else assignshed(false);
+  }
+};
+
+// Coupled rotors (nr > 1): rotor(1..nr) of main.f90, each a Sim whose
+// induced-velocity sums run over all of them (Sim::sys), advanced with
+// every do-ir loop of the reference's iteration run over the rotors in
+// order: kinematics, shedding/ageing/dissipation, all RHS (every wake, the
+// other wings, main.f90:522-591), all solves, all loads (every rotor's bound
+// vortices, :623-690), and the wake update stage by stage (node velocities
+// from every rotor's wing and wake, :799-1439).  Lifting surfaces only
+// (no image rotors, surfaceType >= 0) and no sub-iterations.
+struct System {
+  std::vector<std::unique_ptr<Sim>> r;
+  // main.f90:17-39: config.nml once, geomXX.nml per rotor; each rotor's init
+  // sees dt, nt and the switches as the previous one left them
+  // (classdef.f90:2778-3011, intent(inout))
+  void create(int nr, const std::string& config, const std::vector<std::string>& geoms, const std::string& base) {
+    Namelist c;
+    c.parse(config);
+    if (nr < 1 || (int)geoms.size() != nr) throw std::runtime_error("system: one geometry per rotor");
+    for (int ir = 0; ir < nr; ++ir) {
+      auto s = std::make_unique<Sim>();
+      s->member = true;
+      s->baseDir = base;
+      s->readConfig(c);
+      if (s->nr != nr) throw std::runtime_error("system: config.nml nr does not match the number of geometries");
+      if (ir > 0) {
+        s->dt = r[ir - 1]->dt;
+        s->nt = r[ir - 1]->nt;
+        s->sw = r[ir - 1]->sw;
+      }
+      Namelist g;
+      g.parse(geoms[ir]);
+      s->readGeom(g);
+      if (s->R.surfaceType < 0 || std::abs(s->R.surfaceType) == 2)
+        throw std::runtime_error("system: image and non-lifting surfaces are not supported");
+      s->init();
+      r.push_back(std::move(s));
+    }
+    std::vector<Sim*> all;
+    for (auto& s : r) all.push_back(s.get());
+    for (int ir = 0; ir < nr; ++ir) {
+      r[ir]->sys = all;
+      r[ir]->self = ir;
+    }
+  }
+  const Switches& sw() const { return r[0]->sw; }
+  void start() {
+    for (auto& s : r) s->startGeometry();
+    for (auto& s : r) s->computeRHS(false);
+    for (auto& s : r) s->solveRHS();
+    for (auto& s : r) s->startWake();
+    for (auto& s : r) s->startLoads();
+    for (auto& s : r) s->started = true;
+  }
+  void step() {
+    if (!r[0]->started) throw std::runtime_error("system: start first");
+    if (r[0]->iter >= r[0]->nt) throw std::runtime_error("all timesteps done");
+    for (auto& s : r) s->advanceKinematics();
+    for (auto& s : r) s->preWake();
+    for (auto& s : r) s->computeRHS(true);
+    for (auto& s : r) s->solveRHS();
+    if (sw().rotorForcePlot != 0 && r[0]->iter % sw().rotorForcePlot == 0)
+      for (auto& s : r) {
+        s->computeForces();
+        s->force2file();
+      }
+    if (sw().wakeSuppress == 0)
+      for (int st = 0; st < 4; ++st)
+        for (auto& s : r)
+          if (s->R.nNwake > 0) s->wakeStage(st);
   }
 };
 
@@ -2240,6 +2394,32 @@ void* or_sim_create(const char* config_text, const char* geom_text, const char* 
 }
 
 void or_sim_free(void* h) { delete static_cast<Sim*>(h); }
+
+// A system of nr coupled rotors from config.nml and geom01..geomNN.nml texts.
+void* or_sys_create(int nr, const char* config_text, const char* const* geom_texts, const char* base_dir) {
+  System* y = nullptr;
+  int rc = guarded([&]() {
+    y = new System();
+    std::vector<std::string> g;
+    for (int i = 0; i < nr; ++i) g.push_back(geom_texts[i]);
+    y->create(nr, config_text, g, base_dir ? base_dir : "");
+  });
+  if (rc != 0) { delete y; return nullptr; }
+  return y;
+}
+void or_sys_free(void* h) { delete static_cast<System*>(h); }
+int or_sys_set_sum_chunk(void* h, int c) {
+  return guarded([&]() { for (auto& s : static_cast<System*>(h)->r) s->sumChunk = c; });
+}
+int or_sys_start(void* h) { return guarded([&]() { static_cast<System*>(h)->start(); }); }
+int or_sys_step(void* h, int n) {
+  return guarded([&]() { for (int k = 0; k < n; ++k) static_cast<System*>(h)->step(); });
+}
+// Rotor ir (0-based) as a Sim handle for or_get / or_geti (owned by the system).
+void* or_sys_rotor(void* h, int ir) {
+  System* y = static_cast<System*>(h);
+  return ir >= 0 && ir < (int)y->r.size() ? y->r[ir].get() : nullptr;
+}
 
 void or_set_threads(int n) {
 #ifdef _OPENMP

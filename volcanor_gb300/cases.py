@@ -126,6 +126,41 @@ class Case:
         return d
 
 
+@dataclass
+class SystemCase:
+    """Coupled rotors (nr > 1): one config.nml, geom01.nml .. geomNN.nml."""
+
+    name: str
+    config: str
+    geoms: list
+
+    def write(self, directory: str | Path) -> Path:
+        d = Path(directory)
+        d.mkdir(parents=True, exist_ok=True)
+        (d / "config.nml").write_text(self.config)
+        for i, g in enumerate(self.geoms):
+            (d / f"geom{i + 1:02d}.nml").write_text(g)
+        return d
+
+
+def rotor_pair(nt: int = 60, ns: int = 8, n_nwake: int = 24, truncate_nt: int = 30, hub2=(0.0, 0.0, -0.3),
+               omega2: float = -100.0, hub1=(0.0, 0.0, 0.0), fd_scheme: int = 3, dissipation: int = 1,
+               **geom_overrides) -> SystemCase:
+    """Two coupled 2-blade hover rotors (R = 1 m, c = 0.08 m, collective 8
+    deg, dt = 5 deg): by default coaxial and counter-rotating, the second
+    0.3 R below the first."""
+    cfg = config_text(nt=nt, dt=0.0, nr=2, density=1.2, kinematicVisc=1.5e-5, fdScheme=fd_scheme,
+                      wakeDissipation=dissipation)
+    base = dict(nb=2, nc=1, ns=ns, nNwake=n_nwake, span=1.0, rootcut=0.2, chord=0.08, shaftAxis=(0.0, 0.0, 1.0),
+                theta0=8.0, velBody=(0.0, 0.0, 0.0), spanSpacing=1, chordSpacing=1, spanwiseCore=0.05,
+                streamwiseCoreVec=0.05, apparentViscCoeff=5.0, wakeTruncateNt=truncate_nt, symmetricTau=0,
+                pivotLE=0.25)
+    base.update(geom_overrides)
+    g1 = geom_text(**{**base, "Omega": 100.0, "hubCoords": tuple(hub1), "cgCoords": tuple(hub1)})
+    g2 = geom_text(**{**base, "Omega": omega2, "hubCoords": tuple(hub2), "cgCoords": tuple(hub2)})
+    return SystemCase("rotor_pair", cfg, [g1, g2])
+
+
 def wing_ar4(nt: int = 200, fd_scheme: int = 1, n_nwake: Optional[int] = None) -> Case:
     """Flat wing, c = 1 m, AR 4, 4 x 13 rings, alpha 5 deg, V = 10 m/s, dt = c/(4V)."""
     cfg = config_text(nt=nt, dt=0.025, density=1.0, fdScheme=fd_scheme, wakeDissipation=0)

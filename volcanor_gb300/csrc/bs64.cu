@@ -138,6 +138,102 @@ __global__ void k_combine_tree(const double* __restrict__ part, int M, const Gro
   }
 }
 
+// Coupled rotors: the groups carry the index of the sum they belong to
+// (Group::term, non-decreasing).  mode 0 (wake nodes, src/main.f90:808-827):
+// v = 0, then v = v + (wing_t + wake_t) for every term in turn, one term per
+// source rotor (libCommon.f90:114-211 adds a rotor's wing and wake);
+// out[m] = v.  mode 3 (collocation points, src/main.f90:549-561):
+// out[t][m] = 0 + the term's groups in order, one per-rotor wake or wing
+// sum each, which the RHS adds to velCP in turn.  With a single term, mode 0
+// equals k_combine's mode 0 bit for bit.
+__device__ __forceinline__ void term_done(int mode, int t, int M, int m, d3& v, d3& wing, d3& wake, d3& ts,
+                                          double* out) {
+  if (mode == 0) {
+    v = v + (wing + wake);
+  } else {
+    double* o = out + 3 * ((size_t)t * M + m);
+    o[0] = ts.x;
+    o[1] = ts.y;
+    o[2] = ts.z;
+  }
+  wing = wake = ts = zero3();
+}
+
+__global__ void k_combine_terms(const double* __restrict__ part, int M, const Group* __restrict__ groups,
+                                int ngroups, int mode, double* __restrict__ out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M || ngroups <= 0) return;
+  d3 v = zero3(), wing = zero3(), wake = zero3(), ts = zero3();
+  int t = groups[0].term;
+  for (int g = 0; g < ngroups; ++g) {
+    const Group G = groups[g];
+    if (G.term != t) {
+      term_done(mode, t, M, m, v, wing, wake, ts, out);
+      t = G.term;
+    }
+    d3 gs = zero3();
+    for (int q = G.chunk_begin; q < G.chunk_begin + G.chunk_count; ++q) {
+      const double* pp = part + ((size_t)q * M + m) * 3;
+      gs = gs + mk3(pp[0], pp[1], pp[2]);
+    }
+    if (mode == 0) {
+      if (G.kind == 0) wing = wing + gs;
+      else wake = wake + gs;
+    } else {
+      ts = ts + gs;
+    }
+  }
+  term_done(mode, t, M, m, v, wing, wake, ts, out);
+  if (mode == 0) {
+    out[3 * (size_t)m] = v.x;
+    out[3 * (size_t)m + 1] = v.y;
+    out[3 * (size_t)m + 2] = v.z;
+  }
+}
+
+// The same with k_combine_tree's fixed-shape tree per group (FP32 paths).
+__global__ void k_combine_terms_tree(const double* __restrict__ part, int M, const Group* __restrict__ groups,
+                                     int ngroups, int mode, int G, double* __restrict__ out) {
+  const size_t gt = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int m = (int)(gt / G), l = (int)(gt % G);
+  const bool live = m < M;
+  if (ngroups <= 0) return;
+  d3 v = zero3(), wing = zero3(), wake = zero3(), ts = zero3();
+  int t = groups[0].term;
+  for (int g = 0; g < ngroups; ++g) {
+    const Group G_ = groups[g];
+    if (G_.term != t) {
+      if (live && l == 0) term_done(mode, t, M, m, v, wing, wake, ts, out);
+      t = G_.term;
+    }
+    d3 gs = zero3();
+    if (live)
+      for (int q = G_.chunk_begin + l; q < G_.chunk_begin + G_.chunk_count; q += G) {
+        const double* pp = part + ((size_t)q * M + m) * 3;
+        gs = gs + mk3(pp[0], pp[1], pp[2]);
+      }
+    for (int o = G >> 1; o > 0; o >>= 1) {
+      gs.x = gs.x + __shfl_xor_sync(0xffffffffu, gs.x, o, G);
+      gs.y = gs.y + __shfl_xor_sync(0xffffffffu, gs.y, o, G);
+      gs.z = gs.z + __shfl_xor_sync(0xffffffffu, gs.z, o, G);
+    }
+    if (mode == 0) {
+      if (G_.kind == 0) wing = wing + gs;
+      else wake = wake + gs;
+    } else {
+      ts = ts + gs;
+    }
+  }
+  if (live && l == 0) {
+    term_done(mode, t, M, m, v, wing, wake, ts, out);
+    if (mode == 0) {
+      out[3 * (size_t)m] = v.x;
+      out[3 * (size_t)m + 1] = v.y;
+      out[3 * (size_t)m + 2] = v.z;
+    }
+  }
+}
+
 __global__ void k_rings_to_rec64(const double* __restrict__ corners, const double* __restrict__ rvc,
                                  const double* __restrict__ gam, int64_t N, double* __restrict__ rec) {
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -215,6 +311,20 @@ void launch_combine_unordered(const double* part, int M, const Group* groups, in
   const size_t threads = (size_t)M * G;
   count_launch();
   k_combine_tree<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(part, M, groups, ngroups, mode, G, out);
+}
+
+void launch_combine_terms(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
+                          bool ordered, double* out, cudaStream_t s) {
+  if (M <= 0 || ngroups <= 0) return;
+  count_launch();
+  if (ordered) {
+    k_combine_terms<<<(M + 127) / 128, 128, 0, s>>>(part, M, groups, ngroups, mode, out);
+    return;
+  }
+  int G = 1;
+  while (G < 32 && G * 8 < max_chunks) G <<= 1;
+  const size_t threads = (size_t)M * G;
+  k_combine_terms_tree<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(part, M, groups, ngroups, mode, G, out);
 }
 
 void launch_fils_to_rec64(const double* fc, const double* rvc, const double* gam, int64_t N, double* rec,

@@ -67,6 +67,7 @@ struct Case {
   DevState s{};
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;
+  bool ownStream = true;  // false for the rotors of a system after the first (one stream for all)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // the loads (CT row) of a step only read the solution and feed no later
   // part of the step: they run on a side stream, joined at the step's end
@@ -107,7 +108,7 @@ struct Case {
     if (evFork) cudaEventDestroy(evFork);
     if (evJoin) cudaEventDestroy(evJoin);
     if (side) cudaStreamDestroy(side);
-    if (stream) cudaStreamDestroy(stream);
+    if (stream && ownStream) cudaStreamDestroy(stream);
   }
 
   // chunk table of one evaluation: the FP64 summation order, or the FP32
@@ -172,14 +173,17 @@ struct Case {
   // case generates a prescribed wake, whenever the far wake exists)
   int prescRecords(int rowFar) const { return d.prescNt > 0 && rowFar <= d.NF ? kPresc : 0; }
 
-  void create(const std::string& cfg, const std::string& geo, const std::string& base, const vlm_options* o) {
+  void create(const std::string& cfg, const std::string& geo, const std::string& base, const vlm_options* o,
+              const Case* prevRotor = nullptr, bool asMember = false, cudaStream_t sharedStream = nullptr) {
     vlm_default_options(&opt);
     if (o) opt = *o;
     if (opt.precision < 0 || opt.precision > 2) throw StatusError(VLM_ERR_INVALID, "precision must be 0, 1 or 2");
     if (opt.solve_mode < -1 || opt.solve_mode > 1) throw StatusError(VLM_ERR_INVALID, "solve_mode must be -1, 0 or 1");
     refine = opt.solve_mode == 1 || (opt.solve_mode == -1 && opt.precision != VLM_PREC_FP64);
     chunk64 = opt.sum_chunk;
-    W.load(cfg, geo, base);
+    member = asMember;
+    if (member) W.loadMember(cfg, geo, base, prevRotor ? &prevRotor->W : nullptr);
+    else W.load(cfg, geo, base);
     const RotorParams& P = W.P;
     d.nb = P.nb;
     d.nc = P.nc;
@@ -212,7 +216,12 @@ struct Case {
 
     VLM_CUDA(cudaSetDevice(opt.device));
     slots32 = opt.nbody_slots > 0 ? opt.nbody_slots : partial32_slots();
-    VLM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    if (sharedStream) {
+      stream = sharedStream;
+      ownStream = false;
+    } else {
+      VLM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    }
     VLM_CUDA(cudaEventCreate(&ev0));
     VLM_CUDA(cudaEventCreate(&ev1));
     VLM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
@@ -469,7 +478,8 @@ struct Case {
 
   // one Biot-Savart evaluation of plan e (its records already gathered) at the
   // M targets P into out; prec -1 = the case's precision
-  void evaluate(const EvalPlan& e, int M, int mode, const double* P = nullptr, double* out = nullptr, int prec = -1) {
+  void evaluate(const EvalPlan& e, int M, int mode, const double* P = nullptr, double* out = nullptr, int prec = -1,
+                int nterms = 0) {
     if (!P) P = s.targets;
     if (!out) out = s.outv;
     if (prec < 0) prec = opt.precision;
@@ -484,11 +494,163 @@ struct Case {
                        nearOn ? s.nearScratch : nullptr, s.nearBytes, s.nacc, stream, s.edgeW);
     }
     if (e.nchunks == 0) {
-      VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M, stream));
+      VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M * std::max(nterms, 1), stream));
       return;
     }
-    if (prec == VLM_PREC_FP64) launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, out, stream);
+    if (nterms > 0)
+      launch_combine_terms(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, prec == VLM_PREC_FP64, out, stream);
+    else if (prec == VLM_PREC_FP64) launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, out, stream);
     else launch_combine_unordered(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, out, stream);
+  }
+
+  // ---- coupled rotors (nr > 1, vlm_system) ----------------------------------
+  // Every rotor of a system is a Case on the system's one stream.  Its RHS
+  // and wake-node evaluations sum the records of every rotor: each source
+  // rotor's records are gathered from that rotor's state into a segment of
+  // this rotor's record array, and the group table carries the per-rotor
+  // sums (Group::term) in the reference's order (src/main.f90:549-561,
+  // 817-826; libCommon.f90:114-211).
+  bool member = false;
+  int self = 0;
+  std::vector<Case*> sys;
+  struct SysSeg {
+    int jr = 0, lgoff = 0, lng = 0, nrec = 0, recOff = 0;  // source rotor, its local groups, records, offset
+  };
+  struct SysEval {
+    EvalPlan e;
+    int soff = 0, nseg = 0, nterms = 0;
+  };
+  std::vector<SysSeg> hSegs;
+  std::vector<SysEval> sysRhs, sysNode;  // per iteration
+  SysEval sysStart;                      // the initial solution: the other rotors' wings
+  double* sysOut = nullptr;              // [term][collocation point][xyz]
+  double* sysBound = nullptr;            // [rotor][collocation point][xyz] bound-vortex velocities
+  int maxTerms = 1;
+
+  // records of one blade's wake sum (the whole wake)
+  int wakeRecords(int rowNear, int rowFar) const {
+    const int nNear = (d.NW - (rowNear - 1)) * d.ns;
+    const int hs = rowFar <= d.NF ? d.ns : 0;
+    const int nFar = rowFar <= d.NF ? d.NF - rowFar + 1 : 0;
+    return nNear + hs + nFar + prescRecords(rowFar);
+  }
+
+  // kind 0: the initial solution (main.f90:147-153: the other rotors' wings);
+  // 1: the RHS of step k (every rotor's wake, then its wing unless it is this
+  // rotor, one term each); 2: the wake nodes of step k (wing + wake of every
+  // rotor, one term per rotor)
+  void addSysEval(SysEval& se, int kind, int k, int M) {
+    se = SysEval();
+    se.soff = (int)hSegs.size();
+    std::vector<Group> comb;
+    int rec = 0, term = 0;
+    for (int jr = 0; jr < (int)sys.size(); ++jr) {
+      const Case& o = *sys[jr];
+      const int rN = o.plans[k].rowNear, rF = o.plans[k].rowFar;
+      std::vector<Group> loc;
+      int lrec = 0;
+      auto add = [&](int kindG, int t) {
+        for (int b = 0; b < o.d.nb; ++b) {
+          Group g{};
+          g.rec_begin = lrec;
+          g.rec_count = kindG == 0 ? o.d.npan : o.wakeRecords(rN, rF);
+          g.kind = kindG;
+          g.blade = b;
+          g.term = t;
+          lrec += g.rec_count;
+          loc.push_back(g);
+        }
+      };
+      if (kind == 0) {
+        if (jr == self) continue;
+        add(0, term++);
+      } else if (kind == 1) {
+        add(1, term++);
+        if (jr != self) add(0, term++);
+      } else {
+        add(0, term);
+        add(1, term);
+        ++term;
+      }
+      SysSeg sg;
+      sg.jr = jr;
+      sg.lgoff = (int)hGroups.size();
+      sg.lng = (int)loc.size();
+      sg.nrec = lrec;
+      sg.recOff = rec;
+      hGroups.insert(hGroups.end(), loc.begin(), loc.end());
+      hSegs.push_back(sg);
+      for (Group g : loc) {
+        g.rec_begin += rec;
+        comb.push_back(g);
+      }
+      rec += lrec;
+    }
+    se.nseg = (int)hSegs.size() - se.soff;
+    se.nterms = term;
+    EvalPlan& e = se.e;
+    e.goff = (int)hGroups.size();
+    hGroups.insert(hGroups.end(), comb.begin(), comb.end());
+    e.ngroups = (int)comb.size();
+    e.nrec = rec;
+    e.coff = (int)hChunks.size();
+    std::vector<Chunk> tmp(rec + e.ngroups + 1);
+    const int nq = chunkTable(hGroups.data() + e.goff, e.ngroups, M, tmp.data(), (int)tmp.size());
+    if (nq < 0) throw std::runtime_error("chunk table overflow");
+    hChunks.insert(hChunks.end(), tmp.begin(), tmp.begin() + nq);
+    e.nchunks = nq;
+    for (int g = e.goff; g < e.goff + e.ngroups; ++g) e.maxq = std::max(e.maxq, hGroups[g].chunk_count);
+    maxRecords = std::max(maxRecords, rec);
+    maxChunks = std::max(maxChunks, nq);
+    maxPart = std::max(maxPart, (int64_t)std::max(nq, 1) * M);
+    maxTargets = std::max(maxTargets, M);
+    maxTerms = std::max(maxTerms, term);
+  }
+
+  // after every rotor of the system exists
+  void buildSystemPlans() {
+    const int nt = W.nt, Mcp = d.nbC * d.npan;
+    sysRhs.assign(nt + 1, SysEval());
+    sysNode.assign(nt + 1, SysEval());
+    addSysEval(sysStart, 0, 0, Mcp);
+    for (int k = 1; k <= nt; ++k) {
+      addSysEval(sysRhs[k], 1, k, Mcp);
+      addSysEval(sysNode[k], 2, k, node_target_count(d, plans[k].rowNear, plans[k].rowFar));
+    }
+    allocScratch();
+    sysOut = dalloc<double>((size_t)maxTerms * Mcp * 3, owned);
+    sysBound = dalloc<double>(sys.size() * (size_t)Mcp * 3, owned);
+  }
+
+  // the records of every source rotor at step k (frame fk), each from its own state
+  void sysGather(const SysEval& se, int k, bool pred, int fk) {
+    for (int i = 0; i < se.nseg; ++i) {
+      const SysSeg& g = hSegs[se.soff + i];
+      const Case& o = *sys[g.jr];
+      DevState sj = o.s;
+      sj.rec64 = s.rec64 + (size_t)g.recOff * kRec64;
+      sj.edgeW = s.edgeW ? s.edgeW + 4 * (size_t)g.recOff : nullptr;
+      launch_gather(o.d, sj, o.frame(fk), dGroups + g.lgoff, g.lng, g.nrec, o.plans[k].rowNear, o.plans[k].rowFar,
+                    pred, stream);
+    }
+  }
+  // velCP and the RHS at step k (frame k; k = 0: the initial solution)
+  void sysRhsPhase(int k) {
+    const SysEval& se = k == 0 ? sysStart : sysRhs[k];
+    const int Mcp = d.nbC * d.npan;
+    launch_cp_targets(d, frame(k), s.targets, stream);
+    sysGather(se, k, false, k);
+    evaluate(se.e, Mcp, 3, nullptr, sysOut, -1, se.nterms);
+    launch_rhs_terms(d, s, frame(k), sysOut, se.nterms, stream);
+  }
+  // the loads with every rotor's bound vortices (src/main.f90:632-652)
+  void sysLoads(int k) {
+    const int Mcp = d.nbC * d.npan;
+    for (int jr = 0; jr < (int)sys.size(); ++jr)
+      if (jr != self)
+        launch_bound_foreign(d, frame(k), sys[jr]->d, sys[jr]->s, sys[jr]->frame(k), sysBound + 3 * (size_t)jr * Mcp,
+                             stream);
+    launch_loads(d, s, frame(k), chunk64, k, stream, sysBound, (int)sys.size(), self);
   }
 
   // ---- learned far-wake surrogate ----------------------------------------
@@ -720,7 +882,11 @@ struct Case {
     const StepPlan& pl = plans[k];
     const int M = node_target_count(d, pl.rowNear, pl.rowFar);
     launch_node_targets(d, s, pl.rowNear, pl.rowFar, pred, s.targets, stream);
-    if (surr.on && surr.useNow) {
+    if (member) {
+      const SysEval& se = sysNode[k];
+      sysGather(se, k, pred, k);
+      evaluate(se.e, M, 0, nullptr, nullptr, -1, se.nterms);
+    } else if (surr.on && surr.useNow) {
       // near-wake nodes: direct without the far wake + the network's far-wake
       // velocity; far-wake nodes: + the direct far-wake sum
       const SurrPlans& sp = splans[k];
@@ -802,16 +968,10 @@ struct Case {
   // row, wake ageing and dissipation, the wake-induced velocity at the
   // collocation points, the RHS, the circulation solve.
   void enqueueSolvePhase(int k) {
+    prePhase(k);
     const StepPlan& pl = plans[k];
     const int rN = pl.rowNear, rF = pl.rowFar;
     const double* fr = stepFrame(k);
-    const bool wake = d.NW > 0 && W.sw.wakeSuppress == 0;
-    if (wake) {
-      launch_shed(d, s, fr, rN, true, stream);
-      launch_age(d, s, rN, rF, stream);
-      if (W.sw.wakeDissipation == 1) launch_dissipate(d, s, rN, rF, stream);
-      if (W.sw.wakeBurst != 0 && k % W.sw.wakeBurst == 0) launch_burst(d, s, rF, stream);
-    }
     if (d.NW > 0) {
       const int Mcp = d.nbC * d.npan;
       launch_cp_targets(d, fr, s.targets, stream);
@@ -833,6 +993,20 @@ struct Case {
     }
   }
 
+  // src/main.f90:464-490: leading-edge shed row, ageing, dissipation, burst
+  void prePhase(int k) {
+    const StepPlan& pl = plans[k];
+    const int rN = pl.rowNear, rF = pl.rowFar;
+    const double* fr = stepFrame(k);
+    const bool wake = d.NW > 0 && W.sw.wakeSuppress == 0;
+    if (wake) {
+      launch_shed(d, s, fr, rN, true, stream);
+      launch_age(d, s, rN, rF, stream);
+      if (W.sw.wakeDissipation == 1) launch_dissipate(d, s, rN, rF, stream);
+      if (W.sw.wakeBurst != 0 && k % W.sw.wakeBurst == 0) launch_burst(d, s, rF, stream);
+    }
+  }
+
   // rotor_convectwake (src/classdef.f90:4786-4830): shift + continuity +
   // axisymmetric copies, then the prescribed far wake once it is active
   void convect(int k, const double* fr, int rN, int rF, bool pred) {
@@ -845,75 +1019,112 @@ struct Case {
   // corrector), strain, roll-up / far-wake shift, trailing-edge shedding.
   // (Phase 2, the loads, only reads the solution.)
   void enqueueWakePhase(int k) {
+    const bool wake = d.NW > 0 && W.sw.wakeSuppress == 0;
+    if (!wake) return;
+    for (int st = 0; st < 4; ++st) wakeStage(k, st);
+  }
+
+  // whether step k's scheme evaluates the predicted wake
+  bool predicts(int k) const {
+    switch (W.sw.fdScheme) {
+      case 1: return true;
+      case 3: return k != 1;
+      case 4: return k != 2;  // the reference tests iter == 0 for the start-up branch (never true)
+      case 5: return k > 3;
+      default: return false;
+    }
+  }
+
+  // The wake update in four stages, so that coupled rotors run each stage for
+  // every rotor before the next (the reference's do-ir loops): 0 the node
+  // velocities, 1 the scheme up to the predicted wake (all of it when it has
+  // none), 2 the predicted-wake velocities, 3 the corrector, strain, roll-up
+  // / far-wake shift and the trailing-edge shed row.
+  void wakeStage(int k, int st) {
     const StepPlan& pl = plans[k];
     const int rN = pl.rowNear, rF = pl.rowFar;
     const double* fr = stepFrame(k);
-    const bool wake = d.NW > 0 && W.sw.wakeSuppress == 0;
-    if (!wake) return;
-    evalNodes(k, false);
-    switch (W.sw.fdScheme) {
-      case 0:
-        convect(k, fr, rN, rF, false);
-        break;
-      case 1:
-        launch_copy_predicted(d, s, rN, rF, stream);
-        convect(k, fr, rN, rF, true);
-        evalNodes(k, true);
-        launch_order2(d, s, rN, rF, stream);
-        convect(k, fr, rN, rF, false);
-        break;
-      case 2:
-        if (k == 1) {
+    if (st == 0) {
+      evalNodes(k, false);
+      return;
+    }
+    if (st == 2) {
+      if (predicts(k)) evalNodes(k, true);
+      return;
+    }
+    if (st == 1) {
+      switch (W.sw.fdScheme) {
+        case 0:
           convect(k, fr, rN, rF, false);
-          launch_velop(d, s, VOP_COPY_0_TO_1, stream);
-        } else {
-          launch_velop(d, s, VOP_AB2, stream);
-          convect(k, fr, rN, rF, false);
-        }
-        break;
-      case 3:
-        if (k == 1) {
-          convect(k, fr, rN, rF, false);
-          launch_velop(d, s, VOP_COPY_0_TO_1, stream);
-        } else {
+          break;
+        case 1:
           launch_copy_predicted(d, s, rN, rF, stream);
-          launch_velop(d, s, VOP_AM2_PRED, stream);
           convect(k, fr, rN, rF, true);
-          evalNodes(k, true);
+          break;
+        case 2:
+          if (k == 1) {
+            convect(k, fr, rN, rF, false);
+            launch_velop(d, s, VOP_COPY_0_TO_1, stream);
+          } else {
+            launch_velop(d, s, VOP_AB2, stream);
+            convect(k, fr, rN, rF, false);
+          }
+          break;
+        case 3:
+          if (k == 1) {
+            convect(k, fr, rN, rF, false);
+            launch_velop(d, s, VOP_COPY_0_TO_1, stream);
+          } else {
+            launch_copy_predicted(d, s, rN, rF, stream);
+            launch_velop(d, s, VOP_AM2_PRED, stream);
+            convect(k, fr, rN, rF, true);
+          }
+          break;
+        case 4:
+          if (k == 2) {
+            convect(k, fr, rN, rF, false);
+            launch_velop(d, s, VOP_COPY_0_TO_2, stream);
+          } else {
+            launch_copy_predicted(d, s, rN, rF, stream);
+            launch_velop(d, s, VOP_AM3_PRED, stream);
+            convect(k, fr, rN, rF, true);
+          }
+          break;
+        case 5:
+          if (k <= 3) {
+            convect(k, fr, rN, rF, false);
+            launch_velop(d, s, k == 1 ? VOP_COPY_0_TO_1 : (k == 2 ? VOP_COPY_0_TO_2 : VOP_COPY_0_TO_3), stream);
+          } else {
+            launch_copy_predicted(d, s, rN, rF, stream);
+            launch_velop(d, s, VOP_AM4_PRED, stream);
+            convect(k, fr, rN, rF, true);
+          }
+          break;
+      }
+      return;
+    }
+    if (predicts(k)) {
+      switch (W.sw.fdScheme) {
+        case 1:
+          launch_order2(d, s, rN, rF, stream);
+          convect(k, fr, rN, rF, false);
+          break;
+        case 3:
           launch_velop(d, s, VOP_AM2_CORR, stream);
           convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_STEP_TO_1, stream);
-        }
-        break;
-      case 4:
-        // the reference tests iter == 0 for the start-up branch (never true)
-        if (k == 2) {
-          convect(k, fr, rN, rF, false);
-          launch_velop(d, s, VOP_COPY_0_TO_2, stream);
-        } else {
-          launch_copy_predicted(d, s, rN, rF, stream);
-          launch_velop(d, s, VOP_AM3_PRED, stream);
-          convect(k, fr, rN, rF, true);
-          evalNodes(k, true);
+          break;
+        case 4:
           launch_velop(d, s, VOP_AM3_CORR, stream);
           convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_AM3_SHIFT, stream);
-        }
-        break;
-      case 5:
-        if (k <= 3) {
-          convect(k, fr, rN, rF, false);
-          launch_velop(d, s, k == 1 ? VOP_COPY_0_TO_1 : (k == 2 ? VOP_COPY_0_TO_2 : VOP_COPY_0_TO_3), stream);
-        } else {
-          launch_copy_predicted(d, s, rN, rF, stream);
-          launch_velop(d, s, VOP_AM4_PRED, stream);
-          convect(k, fr, rN, rF, true);
-          evalNodes(k, true);
+          break;
+        case 5:
           launch_velop(d, s, VOP_AM4_CORR, stream);
           convect(k, fr, rN, rF, false);
           launch_velop(d, s, VOP_AM4_SHIFT, stream);
-        }
-        break;
+          break;
+      }
     }
     if (W.sw.wakeStrain == 1) launch_strain(d, s, rF, stream);
     if (rN == 1) launch_rollup(d, s, rF, stream);
@@ -1600,6 +1811,103 @@ struct vlm_case {
   Case c;
 };
 
+// Coupled rotors (nr > 1): rotor(1..nr) of src/main.f90, each a Case on one
+// stream, advanced with every do-ir loop of the reference's iteration run
+// over the rotors in turn (src/main.f90:400-1452).
+struct vlm_system {
+  std::vector<std::unique_ptr<vlm_case>> r;
+  int iter = 0;
+  bool started = false;
+  double lastMs = 0;
+
+  Case& rotor(int i) { return r[i]->c; }
+  cudaStream_t stream() { return r[0]->c.stream; }
+  // rotor 0 owns the stream the others use: release them first
+  ~vlm_system() {
+    while (!r.empty()) r.pop_back();
+  }
+
+  void create(const std::string& cfg, const std::vector<std::string>& geoms, const std::string& base,
+              const vlm_options* o) {
+    const int nr = (int)geoms.size();
+    if (nr < 1) throw StatusError(VLM_ERR_INVALID, "a system needs at least one rotor");
+    for (int ir = 0; ir < nr; ++ir) {
+      auto c = std::make_unique<vlm_case>();
+      c->c.create(cfg, geoms[ir], base, o, ir ? &rotor(ir - 1) : nullptr, true, ir ? stream() : nullptr);
+      if (c->c.W.nr != nr)
+        throw StatusError(VLM_ERR_INVALID, "config.nml nr = " + std::to_string(c->c.W.nr) + " but " +
+                                               std::to_string(nr) + " rotor geometries");
+      if (c->c.d.NW <= 0) throw StatusError(VLM_ERR_UNSUPPORTED, "unsupported: a rotor of a system without a wake");
+      r.push_back(std::move(c));
+    }
+    std::vector<Case*> all;
+    for (auto& c : r) all.push_back(&c->c);
+    for (int ir = 0; ir < nr; ++ir) {
+      rotor(ir).sys = all;
+      rotor(ir).self = ir;
+    }
+    for (int ir = 0; ir < nr; ++ir) rotor(ir).buildSystemPlans();
+  }
+
+  // src/main.f90:43-377: pitch, AIC, the initial solution with the other
+  // rotors' wings, the first shed row and the loads of iteration 0
+  void start() {
+    if (started) throw StatusError(VLM_ERR_STATE, "system already started");
+    for (auto& c : r) c->c.aicFactor();
+    cudaStream_t st = stream();
+    for (auto& c : r) c->c.sysRhsPhase(0);
+    for (auto& c : r) launch_solve_only(c->c.d, c->c.s, st);
+    for (auto& c : r) launch_shed(c->c.d, c->c.s, c->c.frame(0), c->c.d.NW + 1, false, st);
+    if (rotor(0).W.sw.rotorForcePlot != 0)
+      for (auto& c : r) c->c.sysLoads(0);
+    VLM_CUDA(cudaGetLastError());
+    for (auto& c : r) c->c.finishSteps(0, nullptr);
+    for (auto& c : r) {
+      c->c.iter = 0;
+      c->c.started = true;
+    }
+    iter = 0;
+    started = true;
+  }
+
+  // nsteps iterations; ct_rows (if not null): [step][rotor][10]
+  void step(int nsteps, double* ctRows) {
+    if (!started) throw StatusError(VLM_ERR_STATE, "vlm_system_start must be called before vlm_system_step");
+    Case& c0 = rotor(0);
+    c0.useDevice();
+    for (auto& c : r) c->c.checkSteps(nsteps);
+    for (auto& c : r) c->c.uploadFrames(nsteps);
+    cudaStream_t st = stream();
+    const Switches& sw = c0.W.sw;
+    VLM_CUDA(cudaEventRecord(c0.ev0, st));
+    for (int k = iter + 1; k <= iter + nsteps; ++k) {
+      for (auto& c : r) c->c.prePhase(k);
+      for (auto& c : r) c->c.sysRhsPhase(k);
+      for (auto& c : r) launch_solve_only(c->c.d, c->c.s, st);
+      if (sw.rotorForcePlot != 0 && k % sw.rotorForcePlot == 0)
+        for (auto& c : r) c->c.sysLoads(k);
+      if (sw.wakeSuppress == 0)
+        for (int stg = 0; stg < 4; ++stg)
+          for (auto& c : r) c->c.wakeStage(k, stg);
+    }
+    VLM_CUDA(cudaEventRecord(c0.ev1, st));
+    VLM_CUDA(cudaGetLastError());
+    VLM_CUDA(cudaEventSynchronize(c0.ev1));
+    float ms = 0.f;
+    VLM_CUDA(cudaEventElapsedTime(&ms, c0.ev0, c0.ev1));
+    lastMs = ms;
+    const int nr = (int)r.size();
+    std::vector<double> rows((size_t)nsteps * 10);
+    for (int ir = 0; ir < nr; ++ir) {
+      rotor(ir).finishSteps(nsteps, ctRows ? rows.data() : nullptr);
+      if (ctRows)
+        for (int k = 0; k < nsteps; ++k)
+          std::memcpy(ctRows + ((size_t)k * nr + ir) * 10, rows.data() + (size_t)k * 10, 10 * sizeof(double));
+    }
+    iter += nsteps;
+  }
+};
+
 template <class F>
 static int guard(F f) {
   try {
@@ -1945,33 +2253,128 @@ int vlm_case_destroy(vlm_case* c) {
   return VLM_OK;
 }
 
+// A rotor of a system advances only with its system (vlm_system_step).
+static int member_refused() {
+  g_err = "this case is a rotor of a system: it advances with vlm_system_start / vlm_system_step";
+  return VLM_ERR_STATE;
+}
+
+int vlm_system_create(const char* config_text, int nr, const char* const* geom_texts, const char* base_dir,
+                      const vlm_options* opt, vlm_system** out) {
+  if (!out || !config_text || !geom_texts || nr < 1) {
+    g_err = "null argument or nr < 1";
+    return VLM_ERR_INVALID;
+  }
+  *out = nullptr;
+  for (int i = 0; i < nr; ++i)
+    if (!geom_texts[i]) {
+      g_err = "null geometry text";
+      return VLM_ERR_INVALID;
+    }
+  auto y = std::make_unique<vlm_system>();
+  const int rc = guard([&]() {
+    std::vector<std::string> g(geom_texts, geom_texts + nr);
+    y->create(config_text, g, base_dir ? base_dir : "", opt);
+  });
+  if (rc == VLM_OK) *out = y.release();
+  return rc;
+}
+
+int vlm_system_create_from_dir(const char* case_dir, const vlm_options* opt, vlm_system** out) {
+  if (!case_dir || !out) {
+    g_err = "null argument";
+    return VLM_ERR_INVALID;
+  }
+  std::string cfg;
+  std::vector<std::string> geoms;
+  const int rc = guard([&]() {
+    auto rd = [](const std::string& p) {
+      std::ifstream f(p);
+      if (!f) throw std::runtime_error("cannot open " + p);
+      std::stringstream ss;
+      ss << f.rdbuf();
+      return ss.str();
+    };
+    cfg = rd(std::string(case_dir) + "/config.nml");
+    Namelist c;
+    c.parse(cfg);
+    const int nr = c.i("PARAMS", "nr", 1);
+    if (nr < 1 || nr > 99) throw StatusError(VLM_ERR_INVALID, "config.nml: nr out of range");
+    for (int i = 1; i <= nr; ++i) {
+      char name[16];
+      std::snprintf(name, sizeof(name), "/geom%02d.nml", i);
+      geoms.push_back(rd(std::string(case_dir) + name));
+    }
+  });
+  if (rc != VLM_OK) return rc;
+  std::vector<const char*> g;
+  for (const auto& t : geoms) g.push_back(t.c_str());
+  return vlm_system_create(cfg.c_str(), (int)g.size(), g.data(), case_dir, opt, out);
+}
+
+int vlm_system_destroy(vlm_system* y) {
+  if (y && !y->r.empty()) cudaStreamSynchronize(y->stream());
+  delete y;
+  return VLM_OK;
+}
+
+int vlm_system_rotor_count(const vlm_system* y) { return y ? (int)y->r.size() : -1; }
+
+int vlm_system_rotor(vlm_system* y, int ir, vlm_case** out) {
+  if (!y || !out || ir < 0 || ir >= (int)y->r.size()) return VLM_ERR_INVALID;
+  *out = y->r[ir].get();
+  return VLM_OK;
+}
+
+int vlm_system_start(vlm_system* y) {
+  if (!y) return VLM_ERR_INVALID;
+  return guard([&]() { y->start(); });
+}
+
+int vlm_system_step(vlm_system* y, int nsteps, double* ct_rows) {
+  if (!y) return VLM_ERR_INVALID;
+  return guard([&]() { y->step(nsteps, ct_rows); });
+}
+
+int vlm_system_last_step_ms(vlm_system* y, double* ms) {
+  if (!y || !ms) return VLM_ERR_INVALID;
+  *ms = y->lastMs;
+  return VLM_OK;
+}
+
 int vlm_case_start(vlm_case* c) {
   if (!c) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.start(); });
 }
 
 int vlm_case_step(vlm_case* c, int nsteps, double* ct_rows) {
   if (!c) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.step(nsteps, ct_rows); });
 }
 
 int vlm_case_aic_factor(vlm_case* c) {
   if (!c) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.aicFactor(); });
 }
 
 int vlm_case_solve_circulation(vlm_case* c, const double* kinematic_vel, double* gam_out) {
   if (!c) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.phaseSolve(kinematic_vel, gam_out); });
 }
 
 int vlm_case_loads(vlm_case* c, double* ct_row) {
   if (!c) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.phaseLoads(ct_row); });
 }
 
 int vlm_case_wake_step(vlm_case* c) {
   if (!c) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.phaseWake(); });
 }
 
@@ -2105,6 +2508,7 @@ int64_t vlm_wing_kinematics(const char* config_text, const char* geom_text, cons
 
 int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V) {
   if (!c || (M > 0 && (!P || !V))) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.vindPoints(P, M, V); });
 }
 
@@ -2138,6 +2542,7 @@ void vlm_default_surrogate_options(vlm_surrogate_options* o) {
 
 int vlm_case_set_surrogate(vlm_case* c, const vlm_surrogate_options* o) {
   if (!c || !o) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.setSurrogate(*o); });
 }
 
@@ -2155,11 +2560,13 @@ int vlm_case_checkpoint_save(vlm_case* c, const char* path) {
 
 int vlm_case_checkpoint_load(vlm_case* c, const char* path) {
   if (!c || !path) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.checkpointLoad(path); });
 }
 
 int vlm_case_profile_eval(vlm_case* c, int reps, double* ms_per_launch, double* ring_pairs, double* fil_pairs) {
   if (!c || reps <= 0 || !ms_per_launch || !ring_pairs || !fil_pairs) return VLM_ERR_INVALID;
+  if (c->c.member) return member_refused();
   return guard([&]() { c->c.profileEval(reps, ms_per_launch, ring_pairs, fil_pairs); });
 }
 

@@ -1043,7 +1043,12 @@ struct ChunkAcc1 {
 // which evaluate the same filament function on the same corners.  Threads
 // 0..2 do the ordered sums of the x, y, z components.
 constexpr int kVcItems = 256;  // items per batch (a multiple of 4)
-__global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk) {
+// fb (coupled rotors, else null): the bound-vortex velocity of every rotor
+// at this rotor's collocation points, [rotor][point][xyz]; the entry of this
+// rotor (self) is computed here.  velCPTotal = velCP - bound of every rotor in
+// rotor order + this rotor's wing (src/main.f90:636-652).
+__global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const double* fr, int sumChunk,
+                                                     const double* fb, int nrs, int self) {
   __shared__ double F[kVcItems * 3];
   const int t = blockIdx.x;
   if (t >= d.nbC * d.npan) return;
@@ -1102,10 +1107,61 @@ __global__ void __launch_bounds__(256) k_velcp_total(Dims d, DevState s, const d
   }
   if (c < 3) {
     double v = s.velCP[3 * (size_t)t + c];
-    v = v - bound;
+    if (fb) {
+      const size_t M = (size_t)d.nbC * d.npan;
+      for (int jr = 0; jr < nrs; ++jr) v = v - (jr == self ? bound : fb[3 * (jr * M + t) + c]);
+    } else {
+      v = v - bound;
+    }
     v = v + wing;
     s.velCPTotal[3 * (size_t)t + c] = v;
   }
+}
+
+// Bound vortices of rotor (ds, ss, frs) at the collocation points of rotor
+// (dt, frt) (rotor_vind_bywing_boundVortices, src/classdef.f90:1376-1393,
+// 4445-4457): per blade, s = 0, s + (filament 2 + filament 4) gam over the
+// panels (spanwise stations outer), s - filament 2 gam of the trailing-edge
+// panels, blades added to 0 in order.  One thread per point.
+__global__ void k_bound_foreign(Dims dt, const double* frt, Dims ds, DevState ss, const double* frs,
+                                double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= dt.nbC * dt.npan) return;
+  const d3 P = ld3(panRec(dt, frt, t / dt.npan, t % dt.npan) + 12);
+  d3 bound = zero3();
+  for (int b = 0; b < ds.nb; ++b) {
+    d3 sb = zero3();
+    for (int p = 0; p < ds.npan; ++p) {
+      const double* w = panRec(ds, frs, b, p);
+      const double* rv = ss.wRvc + 4 * ((size_t)b * ds.npan + p);
+      const double g = ss.wGam[(size_t)b * ds.npan + p];
+      const d3 f1 = vf_vind64(make_corner64(P, ld3(w + 3)), make_corner64(P, ld3(w + 6)), rv[1]);
+      const d3 f3 = vf_vind64(make_corner64(P, ld3(w + 9)), make_corner64(P, ld3(w)), rv[3]);
+      sb = sb + (f1 + f3) * g;
+    }
+    for (int j = 0; j < ds.ns; ++j) {
+      const int p = (ds.nc - 1) + ds.nc * j;
+      const double* w = panRec(ds, frs, b, p);
+      sb = sb - vf_vind64(make_corner64(P, ld3(w + 3)), make_corner64(P, ld3(w + 6)),
+                          ss.wRvc[4 * ((size_t)b * ds.npan + p) + 1]) *
+                    ss.wGam[(size_t)b * ds.npan + p];
+    }
+    bound = bound + sb;
+  }
+  st3(out + 3 * (size_t)t, bound);
+}
+
+// velCP = kinematic velocity + each term in turn (coupled rotors:
+// src/main.f90:549-561, the wake of every rotor and the wing of the others,
+// one per-rotor sum per term); RHS = velCP . nCap
+__global__ void k_rhs_terms(Dims d, DevState s, const double* fr, const double* terms, int nterms, int M) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.nbC * d.npan) return;
+  const double* w = panRec(d, fr, t / d.npan, t % d.npan);
+  d3 v = ld3(w + 24);
+  for (int k = 0; k < nterms; ++k) v = v + ld3(terms + 3 * ((size_t)k * M + t));
+  st3(s.velCP + 3 * (size_t)t, v);
+  s.RHS[t] = dot3(v, ld3(w + 15));
 }
 
 // libMath.f90:293-426 (Doolittle inverse of lsq2's 3x3 normal matrix; its
@@ -1500,9 +1556,25 @@ void launch_step_begin(const Dims& d, const DevState& s, cudaStream_t st) {
   count_launch();
   k_step_begin<<<1, 256, 0, st>>>(d, s);
 }
-void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st) {
+void launch_rhs_terms(const Dims& d, const DevState& s, const double* frame, const double* terms, int nterms,
+                      cudaStream_t st) {
   count_launch();
-  k_velcp_total<<<d.nbC * d.npan, 256, 0, st>>>(d, s, frame, sumChunk);
+  k_rhs_terms<<<nblk(d.nbC * d.npan, 128), 128, 0, st>>>(d, s, frame, terms, nterms, d.nbC * d.npan);
+}
+void launch_solve_only(const Dims& d, const DevState& s, cudaStream_t st) {
+  count_launch();
+  if (s.LU32) k_solve_refine<<<1, 1024, 0, st>>>(d, s);
+  else k_solve<<<1, 1024, 0, st>>>(d, s);
+}
+void launch_bound_foreign(const Dims& dt, const double* frameT, const Dims& ds, const DevState& ss,
+                          const double* frameS, double* out, cudaStream_t st) {
+  count_launch();
+  k_bound_foreign<<<nblk(dt.nbC * dt.npan, 64), 64, 0, st>>>(dt, frameT, ds, ss, frameS, out);
+}
+void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st,
+                  const double* foreignBound, int nrs, int self) {
+  count_launch();
+  k_velcp_total<<<d.nbC * d.npan, 256, 0, st>>>(d, s, frame, sumChunk, foreignBound, nrs, self);
   count_launch();
   k_loads<<<1, 256, 0, st>>>(d, s, frame, iter);
 }

@@ -122,6 +122,10 @@ struct Group {
   int32_t kind;         // 0 = wing sum, 1 = wake sum
   int32_t blade;        // blade whose wing or wake the group sums
   int32_t pad[2];       // pad[0] = 1: a wake group of the far-wake filaments alone, from the pad[1]-th
+  // coupled rotors: the sum (one rotor's wing, wake, or wing + wake) this
+  // group belongs to; non-decreasing along a group table (launch_combine_terms)
+  int32_t term = 0;
+  int32_t pad2 = 0;
 };
 
 struct Chunk {
@@ -187,6 +191,13 @@ void launch_combine(const double* part, int M, const Group* groups, int ngroups,
 // is itself free.
 void launch_combine_unordered(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
                               double* out, cudaStream_t s);
+
+// Coupled rotors: chunk partials -> per-term sums (Group::term).  mode 0:
+// out[m] = sum over terms of (wing + wake), in term order; mode 3:
+// out[t * M + m] = the term's own sum.  ordered: the FP64 chunk order;
+// else the FP32 paths' fixed tree.
+void launch_combine_terms(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
+                          bool ordered, double* out, cudaStream_t s);
 
 // Launches a wait that nothing releases, bounded by `limit` polls: 1 if it
 // gave up and reported (the expected outcome), 0 if it did not, -1 on a CUDA

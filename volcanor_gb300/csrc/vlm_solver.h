@@ -169,7 +169,16 @@ void launch_solve(const Dims& d, const DevState& s, const double* frame, bool wi
 void launch_step_begin(const Dims& d, const DevState& s, cudaStream_t st);
 // velCPTotal, sectional resultant velocity, lift direction, forces, CT row
 // (iter < 0: the row of the device step counter)
-void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st);
+void launch_loads(const Dims& d, const DevState& s, const double* frame, int sumChunk, int iter, cudaStream_t st,
+                  const double* foreignBound = nullptr, int nrs = 1, int self = 0);
+// Coupled rotors (src/main.f90:522-603, 623-690): the RHS from the kinematic
+// velocity plus nterms per-rotor sums ([term][point][xyz]); the solve alone;
+// the bound vortices of rotor (ds, ss) at the collocation points of rotor dt.
+void launch_rhs_terms(const Dims& d, const DevState& s, const double* frame, const double* terms, int nterms,
+                      cudaStream_t st);
+void launch_solve_only(const Dims& d, const DevState& s, cudaStream_t st);
+void launch_bound_foreign(const Dims& dt, const double* frameT, const Dims& ds, const DevState& ss,
+                          const double* frameS, double* out, cudaStream_t st);
 
 // ---- learned far-wake surrogate (surrogate.cu) ------------------------------
 // targets: the convecting blades' CPs, then nNodes inner-wake nodes (every

@@ -214,6 +214,23 @@ void Wing::load(const std::string& configText, const std::string& geomText, cons
   init();
 }
 
+void Wing::loadMember(const std::string& configText, const std::string& geomText, const std::string& base,
+                      const Wing* prev) {
+  baseDir = base;
+  member = true;
+  Namelist c, g;
+  c.parse(configText);
+  g.parse(geomText);
+  readConfig(c);
+  if (prev) {
+    dt = prev->dt;
+    nt = prev->nt;
+    sw = prev->sw;
+  }
+  readGeom(g);
+  init();
+}
+
 // src/libCommon.f90:51-108
 void Wing::readConfig(const Namelist& c) {
   const std::string ver = c.s("VERSION", "fileFormatVersion", "");
@@ -241,7 +258,9 @@ void Wing::readConfig(const Namelist& c) {
   sw.fdScheme = c.i("OPTIONS", "fdScheme");
   sw.initWakeVelNt = c.i("OPTIONS", "initWakeVelNt");
   sw.probe = c.i("OPTIONS", "probe");
-  if (nr != 1) throw std::runtime_error("unsupported: nr > 1 (coupled rotors)");
+  if (nr != 1 && !member) throw std::runtime_error("nr > 1: coupled rotors are created with vlm_system_create");
+  if (member && (sw.ntSub != 0 || sw.ntSubInit != 0))
+    throw std::runtime_error("unsupported: sub-iterations (ntSub, ntSubInit) of coupled rotors");
   if (sw.restartFromNt != 0) throw std::runtime_error("unsupported: restartFromNt (use the case checkpoint API)");
   if (sw.fdScheme < 0 || sw.fdScheme > 5) throw std::runtime_error("fdScheme must be 0..5");
 }

@@ -92,6 +92,12 @@ class Wing {
  public:
   // config / geometry (throws std::runtime_error on invalid or unsupported input)
   void load(const std::string& configText, const std::string& geomText, const std::string& baseDir);
+  // Rotor ir of coupled rotors (nr > 1): the reference initialises its rotors
+  // in turn with dt, nt and the switches intent(inout) (src/main.f90:32-39,
+  // src/classdef.f90:2778-3011), so rotor ir > 0 starts from the values
+  // rotor ir - 1 left (prev; null for the first rotor).
+  void loadMember(const std::string& configText, const std::string& geomText, const std::string& baseDir,
+                  const Wing* prev);
   void start_pitch();                  // src/main.f90:43-58
   void advance(int iter);              // src/main.f90:412-463 kinematics of one step
   void write_frame(double* out) const;  // see vlm_solver.h for the layout
@@ -108,6 +114,7 @@ class Wing {
   d3 hub, cg, shaftAxis, xBody, yBody, zBody;
   std::vector<Blade> bl;
   std::string baseDir;
+  bool member = false;  // a rotor of coupled rotors: nr > 1 allowed
 
  private:
   void readConfig(const Namelist& c);

@@ -99,6 +99,15 @@ SIGNATURES = {
     "vlm_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
                                         ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
     "vlm_batch_destroy": (ctypes.c_int, [_vp]),
+    "vlm_system_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                         ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(_vp)]),
+    "vlm_system_create_from_dir": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(_vp)]),
+    "vlm_system_destroy": (ctypes.c_int, [_vp]),
+    "vlm_system_rotor_count": (ctypes.c_int, [_vp]),
+    "vlm_system_rotor": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "vlm_system_start": (ctypes.c_int, [_vp]),
+    "vlm_system_step": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "vlm_system_last_step_ms": (ctypes.c_int, [_vp, _dp]),
     "vlm_batch_case": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
     "vlm_batch_start": (ctypes.c_int, [_vp]),
     "vlm_batch_step": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
@@ -502,6 +511,57 @@ class _BorrowedCase(Case):
 
     def close(self):
         self._h = _vp()
+
+
+class System:
+    """Coupled rotors (nr > 1): config.nml and one geomXX.nml per rotor,
+    every induced-velocity sum over all rotors (include/vlm.h, vlm_system_*).
+    ``rotors[i]`` are borrowed Case handles for the getters."""
+
+    def __init__(self, config_text: str, geom_texts, base_dir: str | os.PathLike = "",
+                 precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
+                 solve_mode: Optional[int] = None, device: int = 0, lattice: Optional[bool] = None):
+        n = len(geom_texts)
+        self._geo = (ctypes.c_char_p * n)(*[g.encode() for g in geom_texts])
+        self.opt = options(precision, sum_chunk, near_factor, device=device, use_graph=False, solve_mode=solve_mode)
+        if lattice is not None:
+            self.opt.lattice = 1 if lattice else 0
+        self.nr = n
+        self._h = _vp()
+        _err(load().vlm_system_create(config_text.encode(), n, self._geo, str(base_dir).encode(),
+                                      ctypes.byref(self.opt), ctypes.byref(self._h)))
+        self.rotors = []
+        for i in range(n):
+            h = _vp()
+            _err(load().vlm_system_rotor(self._h, i, ctypes.byref(h)))
+            self.rotors.append(_BorrowedCase(h, self))
+
+    def start(self):
+        _err(load().vlm_system_start(self._h))
+
+    def step(self, n: int = 1, with_ct: bool = True) -> Optional[np.ndarray]:
+        """n iterations; CT rows as [step][rotor][10]."""
+        rows = np.zeros((n, self.nr, 10)) if with_ct else None
+        _err(load().vlm_system_step(self._h, int(n), _ptr(rows) if with_ct else None))
+        return rows
+
+    def last_step_ms(self) -> float:
+        ms = ctypes.c_double()
+        _err(load().vlm_system_last_step_ms(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            for r in self.rotors:
+                r._h = _vp()
+            load().vlm_system_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Batch:
