@@ -201,9 +201,23 @@ int vlm_case_get_wake(vlm_case* c, int blade, double* waN, double* waN_gam, doub
  * nbConvect, wakeTruncateNt, rotorForcePlot, the output switches (wakePlot, wakeTipPlot, gridPlot,
  * probe, wakeSuppress, skewPlotSwitch, inflowPlotSwitch, gammaPlotSwitch, after the reference's
  * conversion of chords/revolutions), rollupStart, rollupEnd; nearPairs (near-field filament-target pairs of the
- * last FP32 evaluation) and nodeChunks (chunks of the next step's wake-node
- * evaluation) describe this library's kernels. */
+ * last FP32 evaluation), nodeChunks and nodeShape (chunks and FP32 tile
+ * shape of the next step's wake-node evaluation; after the last step, of the
+ * last one) describe this library's kernels. */
 int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
+/* FP32 N-body tile shape (no counterpart in the reference).  By default a
+ * case autotunes: at the first steady-state step of each (rowNear, rowFar)
+ * signature (every later step of a truncated wake repeats it) it times its
+ * live wake-node and collocation-point evaluations with each compiled tile
+ * shape (0: 512 targets per block, 4 stages, 2 blocks per SM; 1: 256 targets
+ * per block, 3 stages, 3 blocks per SM) at the wave model's chunk count and at
+ * 1/2, 3/4, 3/2 and 2 times it, and keeps the fastest (vlm_case_get
+ * "autotune").  This call re-plans every step after the current one with
+ * `shape` and `chunks` chunks for the largest group of each evaluation (0 =
+ * the wave model's count) and turns the tuner off; shape -1 turns it back
+ * on.  FP32 precisions of a lone case without the surrogate; results change
+ * only in the FP32 summation order. */
+int vlm_case_set_tile(vlm_case* c, int shape, int chunks);
 /* Copy a named array into out (at most cap doubles); blade is 1-based where
  * the array is per blade.  Returns the element count, or -1 for an unknown
  * name.  Names and layouts (Fortran column-major, xyz fastest):
@@ -227,6 +241,12 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  *                                   multi-step schemes (velNwake1..3, velFwake1..3)
  *   velKin (blade)                  (3, nc, ns) the kinematic velocity at the collocation points
  *                                   of the current iteration (during an open step, of that step)
+ *   autotune                        per steady-state signature the FP32 tile autotuner
+ *                                   timed (first steady step of each): rowNear, rowFar,
+ *                                   candidates timed, then for the wake nodes and for
+ *                                   the collocation points: chosen tile shape, chunk
+ *                                   count of the largest group, ms per launch of the
+ *                                   choice, ms of the wave model's plan (11 per signature)
  *   hub                             (3) hub coordinates; yAxis (blade) (3) the blade's y axis;
  *   secCP (blade)                   (3, ns) section points -- all of the current iteration
  *                                   (of the open step between its phases)

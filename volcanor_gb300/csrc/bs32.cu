@@ -47,7 +47,6 @@ namespace vlm {
 
 namespace {
 
-constexpr int kTPT = 2;         // targets per thread
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr float kS2Min = 1e-30f;
 
@@ -219,23 +218,25 @@ __device__ __forceinline__ void rec_lat_pair(const float4* __restrict__ R4, cons
   }
 }
 
-// One block = 8 consumer warps (256 threads x 2 targets) + 1 producer warp.
-// The producer's lane 0 streams the chunk's records through kStages shared
-// stages with bulk copies; consumers wait on a stage's FULL barrier, compute,
-// and release it through its EMPTY barrier (one arrival per consumer warp).
-constexpr int kStages = 4;
+// One block = 8 consumer warps (256 threads x kTPT targets) + 1 producer
+// warp.  The producer's lane 0 streams the chunk's records through kStages
+// shared stages with bulk copies; consumers wait on a stage's FULL barrier,
+// compute, and release it through its EMPTY barrier (one arrival per
+// consumer warp).  Tile shapes (targets per thread, stages, resident blocks
+// per SM) are template arguments; kPartial32Shapes lists the compiled ones,
+// among which the case autotuner picks per evaluation.
 constexpr int kTileW = 128;                 // records per stage (24 KB)
 constexpr int kConsumerWarps = 8;
 constexpr int kBlockW = (kConsumerWarps + 1) * 32;
-static_assert(kConsumerWarps * 32 * kTPT == kTargetsPerBlock32, "targets per block");
 
 // LAT: the records are in lattice form (edges 2 and 3 marked when they carry
 // no circulation); otherwise every record is evaluated as a whole ring.
-template <bool LAT>
-__global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restrict__ rec32,
-                                                         const Chunk* __restrict__ chunks,
-                                                         const double* __restrict__ P, int M,
-                                                         double* __restrict__ part, int* __restrict__ ctl) {
+template <bool LAT, int kTPT, int kStages, int kMinBlocks>
+__global__ void __launch_bounds__(kBlockW, kMinBlocks) k_partial32(const float* __restrict__ rec32,
+                                                                  const Chunk* __restrict__ chunks,
+                                                                  const double* __restrict__ P, int M,
+                                                                  double* __restrict__ part, int* __restrict__ ctl) {
+  constexpr int kTargetsPerBlock = kConsumerWarps * 32 * kTPT;
   extern __shared__ __align__(16) float stage[];  // [kStages][kTileW * kRec32]
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ __align__(8) uint64_t empty[kStages];
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(kBlockW, 2) k_partial32(const float* __restric
   for (int u = 0; u < kTPT; ++u) {
     // runs of 256 targets per u: a warp's targets are two runs of 32
     // consecutive ones (measured 1-2 % faster than one run of 64)
-    mt[u] = blockIdx.x * kTargetsPerBlock32 + u * (32 * kConsumerWarps) + tid;
+    mt[u] = blockIdx.x * kTargetsPerBlock + u * (32 * kConsumerWarps) + tid;
     valid[u] = mt[u] < M;
     const int mm = valid[u] ? mt[u] : M - 1;
     px[u] = (float)P[3 * (size_t)mm];
@@ -815,51 +816,110 @@ void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec
   k_pack32<<<(nrec + 255) / 256, 256, 0, s>>>(rec64, nrec, near_factor, rec32, ew);
 }
 
-void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
-                      const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
-                      long long* nacc, cudaStream_t s, const double* ew) {
-  if (M <= 0 || nchunks <= 0) return;
-  const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
-  // the dynamic shared-memory opt-in is per device; set it once on each
+// The compiled tile shapes: {targets per thread, stages, blocks per SM}.
+// Shape 0 = 2 targets per thread, 4 stages (96 KB), 2 blocks per SM: the
+// most reuse of a staged record; shape 1 = 1 target per thread, 3 stages
+// (72 KB), 3 blocks per SM: twice the target blocks and 1.5x the resident
+// blocks, for evaluations whose grid would leave slots idle.
+template <int V>
+struct Shape32;
+template <>
+struct Shape32<0> {
+  static constexpr int tpt = 2, stages = 4, minb = 2;
+};
+template <>
+struct Shape32<1> {
+  static constexpr int tpt = 1, stages = 3, minb = 3;
+};
+static_assert(kPartial32Shapes == 2, "shape table");
+
+template <int V>
+int shape_smem() {
+  return Shape32<V>::stages * kTileW * kRec32 * (int)sizeof(float);
+}
+
+template <int V, bool LAT>
+void set_smem_attr() {
+  using S = Shape32<V>;
+  cudaFuncSetAttribute(k_partial32<LAT, S::tpt, S::stages, S::minb>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       shape_smem<V>());
+}
+
+template <int V>
+void launch_shape(bool lat, dim3 grid, const float* rec32, const Chunk* chunks, const double* P, int M, double* part,
+                  int* ctl, cudaStream_t s) {
+  using S = Shape32<V>;
+  if (lat) k_partial32<true, S::tpt, S::stages, S::minb><<<grid, kBlockW, shape_smem<V>(), s>>>(rec32, chunks, P, M, part, ctl);
+  else k_partial32<false, S::tpt, S::stages, S::minb><<<grid, kBlockW, shape_smem<V>(), s>>>(rec32, chunks, P, M, part, ctl);
+}
+
+// the dynamic shared-memory opt-in is per device; set it once on each
+void ensure_smem_attrs() {
   static std::atomic<bool> attr[64];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || !attr[dev].load(std::memory_order_acquire)) {
-    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_partial32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    set_smem_attr<0, false>();
+    set_smem_attr<0, true>();
+    set_smem_attr<1, false>();
+    set_smem_attr<1, true>();
     if (dev >= 0 && dev < 64) attr[dev].store(true, std::memory_order_release);
   }
-  dim3 grid((M + kTargetsPerBlock32 - 1) / kTargetsPerBlock32, nchunks);
-  count_launch();
-  if (ew) k_partial32<true><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
-  else k_partial32<false><<<grid, kBlockW, smem, s>>>(rec32, chunks, P, M, part, ctl);
-  if (!near_scratch || nrec <= 0) return;
-  // near field: targets binned in a grid, near pairs listed, FP64
-  // corrections of the listed pairs, corrections folded into the partials
+}
+
+int partial32_targets_per_block(int shape) { return kConsumerWarps * 32 * (shape == 1 ? Shape32<1>::tpt : Shape32<0>::tpt); }
+
+void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
+                      const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
+                      long long* nacc, cudaStream_t s, const double* ew, int shape, const NearOverlap* ov) {
+  if (M <= 0 || nchunks <= 0) return;
+  ensure_smem_attrs();
+  const int tpb = partial32_targets_per_block(shape);
+  dim3 grid((M + tpb - 1) / tpb, nchunks);
+  const bool nearOn = near_scratch && nrec > 0;
   const size_t gridBytes = near_grid_bytes(M);
-  if (near_bytes < gridBytes + (size_t)kNearAlign) {
+  if (nearOn && near_bytes < gridBytes + (size_t)kNearAlign) {
     count_launch();
     k_set_flag<<<1, 1, 0, s>>>(ctl, 3);
     return;
   }
+  // With ov, the near-field detection and FP64 correction (which read only
+  // the records and targets) run on ov->stream alongside the pair kernel;
+  // the fold into the partial sums waits for both.
+  cudaStream_t ns = s;
+  if (nearOn && ov) {
+    cudaEventRecord(ov->fork, s);
+    cudaStreamWaitEvent(ov->stream, ov->fork, 0);
+    ns = ov->stream;
+  }
+  count_launch();
+  if (shape == 1) launch_shape<1>(ew != nullptr, grid, rec32, chunks, P, M, part, ctl, s);
+  else launch_shape<0>(ew != nullptr, grid, rec32, chunks, P, M, part, ctl, s);
+  if (!nearOn) return;
+  // near field: targets binned in a grid, near pairs listed, FP64
+  // corrections of the listed pairs, corrections folded into the partials
   unsigned char* g = static_cast<unsigned char*>(near_scratch);
   NearPair* list = reinterpret_cast<NearPair*>(g + gridBytes);
   const int cap = (int)std::min<size_t>((near_bytes - gridBytes) / sizeof(NearPair), (size_t)1 << 30);
   const GridLayout L = grid_layout(M);
   const int T = grid_buckets(M);
   count_launches(7);
-  k_grid_init<<<1, 1, 0, s>>>(g, T);
-  k_zone_mean<<<(nrec + 255) / 256, 256, 0, s>>>(rec32, nrec, g);
-  cudaMemsetAsync(g + L.key, 0xFF, (size_t)T * sizeof(unsigned long long), s);
-  cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), s);
-  k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
-  k_grid_scan<<<1, 1024, 0, s>>>(M, g);
-  k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, s>>>(P, M, g);
-  k_near_find<<<(unsigned)(((size_t)nrec * 4 * 32 + 255) / 256), 256, 0, s>>>(rec32, nrec, chunks, nchunks, P, M, g,
-                                                                              list, cap, ctl);
+  k_grid_init<<<1, 1, 0, ns>>>(g, T);
+  k_zone_mean<<<(nrec + 255) / 256, 256, 0, ns>>>(rec32, nrec, g);
+  cudaMemsetAsync(g + L.key, 0xFF, (size_t)T * sizeof(unsigned long long), ns);
+  cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), ns);
+  k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
+  k_grid_scan<<<1, 1024, 0, ns>>>(M, g);
+  k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
+  k_near_find<<<(unsigned)(((size_t)nrec * 4 * 32 + 255) / 256), 256, 0, ns>>>(rec32, nrec, chunks, nchunks, P, M,
+                                                                               g, list, cap, ctl);
   const int sms = device_sm_count();
-  k_near_fix<<<4 * sms, 128, 0, s>>>(list, cap, rec32, rec64, ew, P, M, reinterpret_cast<unsigned long long*>(nacc),
-                                     ctl);
+  k_near_fix<<<4 * sms, 128, 0, ns>>>(list, cap, rec32, rec64, ew, P, M, reinterpret_cast<unsigned long long*>(nacc),
+                                      ctl);
+  if (ns != s) {
+    cudaEventRecord(ov->join, ns);
+    cudaStreamWaitEvent(s, ov->join, 0);
+  }
   const size_t n = (size_t)M * nchunks * 3;
   count_launch();
   k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * sms), 256, 0, s>>>(part, nacc, n);
@@ -882,18 +942,27 @@ int device_sm_count() {
   return cache[dev];
 }
 
-int partial32_slots() {
-  static std::atomic<int> cache[64];
+int partial32_slots(int shape) {
+  static std::atomic<int> cache[64][kPartial32Shapes];
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 2 * kPlanSmsWithoutDevice;
-  if (!cache[dev]) {
+  shape = shape == 1 ? 1 : 0;
+  const int fallback = (shape == 1 ? Shape32<1>::minb : Shape32<0>::minb) * kPlanSmsWithoutDevice;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fallback;
+  if (!cache[dev][shape]) {
     int per = 0;
-    const int smem = kStages * kTileW * kRec32 * (int)sizeof(float);
-    cudaFuncSetAttribute(k_partial32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<false>, kBlockW, smem);
-    cache[dev] = device_sm_count() * std::max(1, per);
+    ensure_smem_attrs();
+    if (shape == 1) {
+      using S = Shape32<1>;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true, S::tpt, S::stages, S::minb>, kBlockW,
+                                                    shape_smem<1>());
+    } else {
+      using S = Shape32<0>;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_partial32<true, S::tpt, S::stages, S::minb>, kBlockW,
+                                                    shape_smem<0>());
+    }
+    cache[dev][shape] = device_sm_count() * std::max(1, per);
   }
-  return cache[dev];
+  return cache[dev][shape];
 }
 
 int selftest_bounded_wait(uint32_t limit) {

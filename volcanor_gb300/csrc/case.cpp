@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <sstream>
@@ -53,7 +54,8 @@ struct EvalPlan {
   int goff = 0, ngroups = 0;  // into the step plan's group table
   int coff = 0, nchunks = 0;  // into the chunk table
   int nrec = 0;
-  int maxq = 0;  // most chunks of one group
+  int maxq = 0;   // most chunks of one group
+  int shape = 0;  // FP32 kernel tile shape (launch_partial32)
 };
 struct StepPlan {
   int rowNear = 0, rowFar = 0;
@@ -73,6 +75,9 @@ struct Case {
   // part of the step: they run on a side stream, joined at the step's end
   cudaStream_t side = nullptr;
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
+  // the near-field chain of an FP32 evaluation runs on its own stream
+  // alongside the pair kernel (launch_partial32)
+  NearOverlap nearOv{nullptr, nullptr, nullptr};
   bool loadsForked = false;
   std::vector<StepPlan> plans;  // index = iteration (0..nt)
   double* hFrames = nullptr;    // pinned host copy of every frame; uploaded per vlm_case_step call
@@ -108,6 +113,10 @@ struct Case {
     if (evFork) cudaEventDestroy(evFork);
     if (evJoin) cudaEventDestroy(evJoin);
     if (side) cudaStreamDestroy(side);
+    if (nearOv.stream) cudaStreamSynchronize(nearOv.stream);
+    if (nearOv.fork) cudaEventDestroy(nearOv.fork);
+    if (nearOv.join) cudaEventDestroy(nearOv.join);
+    if (nearOv.stream) cudaStreamDestroy(nearOv.stream);
     if (stream && ownStream) cudaStreamDestroy(stream);
   }
 
@@ -227,6 +236,9 @@ struct Case {
     VLM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     VLM_CUDA(cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming));
     VLM_CUDA(cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming));
+    VLM_CUDA(cudaStreamCreateWithFlags(&nearOv.stream, cudaStreamNonBlocking));
+    VLM_CUDA(cudaEventCreateWithFlags(&nearOv.fork, cudaEventDisableTiming));
+    VLM_CUDA(cudaEventCreateWithFlags(&nearOv.join, cudaEventDisableTiming));
 
     // frames: 0 = after the initial pitch, k = after the kinematics of step k
     std::vector<double> frames((size_t)(nt + 1) * d.fl.size);
@@ -491,7 +503,7 @@ struct Case {
       launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream, s.edgeW);
       VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
       launch_partial32(s.rec32, s.rec64, ch, e.nchunks, e.nrec, P, M, s.part, s.err + 2,
-                       nearOn ? s.nearScratch : nullptr, s.nearBytes, s.nacc, stream, s.edgeW);
+                       nearOn ? s.nearScratch : nullptr, s.nearBytes, s.nacc, stream, s.edgeW, e.shape, &nearOv);
     }
     if (e.nchunks == 0) {
       VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M * std::max(nterms, 1), stream));
@@ -501,6 +513,249 @@ struct Case {
       launch_combine_terms(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, prec == VLM_PREC_FP64, out, stream);
     else if (prec == VLM_PREC_FP64) launch_combine(s.part, M, dGroups + e.goff, e.ngroups, mode, out, stream);
     else launch_combine_unordered(s.part, M, dGroups + e.goff, e.ngroups, e.maxq, mode, out, stream);
+  }
+
+  // ---- autotuner of the FP32 N-body tile shape and chunking ----------------
+  // The chunk planner's wave model (plan.cpp) picks a chunk count per
+  // evaluation shape for tile shape 0.  At the first step whose (rowNear,
+  // rowFar) signature repeats the previous step's -- the steady state that
+  // every later step of a truncated wake repeats, and the one captured as a
+  // graph -- the case times, on its live state, the wake-node and the
+  // collocation-point evaluations for both tile shapes at the model's chunk
+  // count and at 1/2, 3/4, 3/2 and 2 times it (5 launches each after a warm
+  // one, CUDA events), and keeps the fastest for every later step of that
+  // signature if it beats the model's plan by more than 3 % (near ties keep
+  // the model's plan, so that a choice does not flip with timing noise).
+  // Only the FP32 pair kernel is timed (the near-field correction does not
+  // depend on the chunking).  Decisions are kept for the process, keyed by
+  // the device, precision, form and evaluation shape: every later case of
+  // the same shape -- another run of the same case file, the step driven
+  // phase by phase, a resumed checkpoint -- reuses them without timing, so
+  // runs in one process give the same bits.  Results: vlm_case_get
+  // "autotune"; vlm_case_set_tile fixes a plan instead.
+  struct TuneResult {
+    int rN = -1, rF = -1, candidates = 0;
+    int shape[2] = {0, 0}, chunks[2] = {0, 0};  // [0] wake nodes, [1] collocation points
+    double ms[2] = {0, 0}, modelMs[2] = {0, 0};
+  };
+  std::vector<TuneResult> tuned;
+  bool tileForced = false;  // vlm_case_set_tile fixed the shape: no autotuning
+  struct TileChoice {
+    int shape = 0, n = 0;
+    double ms = 0, modelMs = 0;
+  };
+  static std::mutex& tuneMutex() {
+    static std::mutex m;
+    return m;
+  }
+  static std::map<std::vector<int64_t>, TileChoice>& tuneCache() {
+    static std::map<std::vector<int64_t>, TileChoice> c;
+    return c;
+  }
+  // the (shape, n) table of evaluation `which` for every step from k on with
+  // pl's signature
+  void applyTile(int k, const StepPlan& pl, int which, const EvalPlan& e, int M, int shape, int n) {
+    std::vector<Group> g(hGroups.begin() + e.goff, hGroups.begin() + e.goff + e.ngroups);
+    const int cap = e.nrec + e.ngroups + 1;
+    std::vector<Chunk> ch((size_t)cap);
+    const int nq = build_chunks32(g.data(), e.ngroups, n, ch.data(), cap);
+    if (nq < 0) throw std::runtime_error("chunk table overflow");
+    const int off = (int)hChunks.size();
+    hChunks.insert(hChunks.end(), ch.begin(), ch.begin() + nq);
+    int maxq = 0;
+    for (const Group& x : g) maxq = std::max(maxq, x.chunk_count);
+    for (int kk = k; kk <= W.nt; ++kk) {
+      StepPlan& p2 = plans[kk];
+      if (p2.rowNear != pl.rowNear || p2.rowFar != pl.rowFar) continue;
+      EvalPlan& e2 = which == 0 ? p2.node : p2.rhs;
+      e2.shape = shape;
+      e2.coff = off;
+      e2.nchunks = nq;
+      e2.maxq = maxq;
+      for (int gi = 0; gi < e2.ngroups; ++gi) {
+        hGroups[e2.goff + gi].chunk_begin = g[gi].chunk_begin;
+        hGroups[e2.goff + gi].chunk_count = g[gi].chunk_count;
+      }
+    }
+    maxChunks = std::max(maxChunks, nq);
+    maxPart = std::max(maxPart, (int64_t)nq * M);
+  }
+  bool tuneOn() const {
+    return opt.precision != VLM_PREC_FP64 && opt.nbody_slots <= 0 && !member && !surr.on && d.NW > 0 &&
+           !tileForced;
+  }
+  // vlm_case_set_tile: every evaluation of the steps after the current one
+  // re-planned with tile shape `shape` and `n` chunks for the largest group
+  // (0: the wave model's count for that shape); shape -1 gives the choice back
+  // to the autotuner (the wave model's plans for shape 0 until it runs)
+  void setTile(int shape, int n) {
+    useDevice();
+    if (opt.precision == VLM_PREC_FP64) throw StatusError(VLM_ERR_INVALID, "tile shapes apply to the FP32 precisions");
+    if (shape < -1 || shape >= kPartial32Shapes || n < 0)
+      throw StatusError(VLM_ERR_INVALID, "shape must be -1 or 0.." + std::to_string(kPartial32Shapes - 1) +
+                                             ", chunks >= 0");
+    if (member || surr.on || opt.nbody_slots > 0)
+      throw StatusError(VLM_ERR_UNSUPPORTED, "tile shapes are set on a lone case without the surrogate");
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    const int sh = shape < 0 ? 0 : shape;
+    for (int k = iter + 1; k <= W.nt; ++k)
+      for (int which = 0; which < 2; ++which) {
+        StepPlan& pl = plans[k];
+        EvalPlan& e = which == 0 ? pl.node : pl.rhs;
+        if (e.ngroups == 0) continue;
+        const int M = which == 0 ? node_target_count(d, pl.rowNear, pl.rowFar) : d.nbC * d.npan;
+        Group* g = hGroups.data() + e.goff;
+        const int cap = e.nrec + e.ngroups + 1;
+        const int nn = n > 0 ? n : plan_count32(g, e.ngroups, M, partial32_slots(sh), cap,
+                                                partial32_targets_per_block(sh));
+        std::vector<Chunk> ch((size_t)cap);
+        const int nq = build_chunks32(g, e.ngroups, nn, ch.data(), cap);
+        if (nq < 0) throw std::runtime_error("chunk table overflow");
+        e.coff = (int)hChunks.size();
+        hChunks.insert(hChunks.end(), ch.begin(), ch.begin() + nq);
+        e.nchunks = nq;
+        e.shape = sh;
+        e.maxq = 0;
+        for (int gi = 0; gi < e.ngroups; ++gi) e.maxq = std::max(e.maxq, g[gi].chunk_count);
+        maxChunks = std::max(maxChunks, nq);
+        maxPart = std::max(maxPart, (int64_t)std::max(nq, 1) * M);
+      }
+    tileForced = shape >= 0;
+    tuned.clear();
+    // a captured step graph holds the old tables
+    if (gexec) {
+      cudaGraphExecDestroy(gexec);
+      gexec = nullptr;
+    }
+    allocScratch();
+  }
+  bool sigRepeats(int k) const {
+    return k > 3 && plans[k].rowNear == plans[k - 1].rowNear && plans[k].rowFar == plans[k - 1].rowFar;
+  }
+  bool tunedFor(const StepPlan& pl) const {
+    for (const TuneResult& t : tuned)
+      if (t.rN == pl.rowNear && t.rF == pl.rowFar) return true;
+    return false;
+  }
+  void autotune(int k) {
+    useDevice();
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    const StepPlan pl = plans[k];
+    TuneResult tr;
+    tr.rN = pl.rowNear;
+    tr.rF = pl.rowFar;
+    constexpr int kReps = 5;
+    constexpr int64_t kMaxTunePart = (int64_t)1 << 22;  // (chunks x targets) of a candidate
+    constexpr double kMargin = 0.97;                    // a plan must beat the model's by 3 %
+    std::vector<void*> tmp;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    VLM_CUDA(cudaEventCreate(&t0));
+    VLM_CUDA(cudaEventCreate(&t1));
+    bool changed = false;
+    for (int which = 0; which < 2; ++which) {
+      const EvalPlan e = which == 0 ? pl.node : pl.rhs;
+      const int M = which == 0 ? node_target_count(d, pl.rowNear, pl.rowFar) : d.nbC * d.npan;
+      if (M <= 0 || e.nrec <= 0) continue;
+      std::vector<int64_t> key = {opt.device, opt.precision, lattice() ? 1 : 0, which, M, e.ngroups};
+      for (int gi = 0; gi < e.ngroups; ++gi) key.push_back(hGroups[e.goff + gi].rec_count);
+      int bestShape = 0, bestN = 0;
+      double bestMs = 0.0, curMs = 0.0;
+      {
+        std::lock_guard<std::mutex> lk(tuneMutex());
+        auto it = tuneCache().find(key);
+        if (it != tuneCache().end()) {
+          bestShape = it->second.shape;
+          bestN = it->second.n;
+          bestMs = it->second.ms;
+          curMs = it->second.modelMs;
+        }
+      }
+      if (bestN > 0) {
+        applyTile(k, pl, which, e, M, bestShape, bestN);
+        tr.shape[which] = bestShape;
+        tr.chunks[which] = bestN;
+        tr.ms[which] = bestMs;
+        tr.modelMs[which] = curMs;
+        changed = true;
+        continue;
+      }
+      if (which == 0) launch_node_targets(d, s, pl.rowNear, pl.rowFar, false, s.targets, stream);
+      else launch_cp_targets(d, frame(k), s.targets, stream);
+      launch_gather(d, s, frame(k), dGroups + e.goff, e.ngroups, e.nrec, pl.rowNear, pl.rowFar, false, stream);
+      launch_pack32(s.rec64, e.nrec, 0.0, s.rec32, stream, s.edgeW);
+      std::vector<Group> g0(hGroups.begin() + e.goff, hGroups.begin() + e.goff + e.ngroups);
+      const int cap = e.nrec + e.ngroups + 1;
+      Chunk* dch = dalloc<Chunk>((size_t)cap, tmp);
+      double* dpart = dalloc<double>((size_t)kMaxTunePart * 3, tmp);
+      bestMs = 1e30;
+      curMs = 1e30;
+      int modelN = 0;
+      for (int shape = 0; shape < kPartial32Shapes; ++shape) {
+        const int tpb = partial32_targets_per_block(shape);
+        const int n0 = plan_count32(g0.data(), e.ngroups, M, partial32_slots(shape), cap, tpb);
+        int maxRec = 0;
+        for (const Group& g : g0) maxRec = std::max(maxRec, g.rec_count);
+        const int ns[5] = {n0, std::max(1, n0 / 2), std::max(1, 3 * n0 / 4), (3 * n0 + 1) / 2, 2 * n0};
+        std::vector<int> seen;
+        for (int n : ns) {
+          n = std::min(n, std::max(1, maxRec));
+          if (std::find(seen.begin(), seen.end(), n) != seen.end()) continue;
+          seen.push_back(n);
+          std::vector<Group> g = g0;
+          std::vector<Chunk> ch((size_t)cap);
+          const int nq = build_chunks32(g.data(), e.ngroups, n, ch.data(), cap);
+          if (nq <= 0 || (int64_t)nq * M > kMaxTunePart) continue;
+          VLM_CUDA(cudaMemcpyAsync(dch, ch.data(), sizeof(Chunk) * nq, cudaMemcpyHostToDevice, stream));
+          auto launch = [&]() {
+            launch_partial32(s.rec32, s.rec64, dch, nq, e.nrec, s.targets, M, dpart, s.err + 2, nullptr, 0, nullptr,
+                             stream, s.edgeW, shape);
+          };
+          launch();
+          VLM_CUDA(cudaEventRecord(t0, stream));
+          for (int r = 0; r < kReps; ++r) launch();
+          VLM_CUDA(cudaEventRecord(t1, stream));
+          VLM_CUDA(cudaEventSynchronize(t1));
+          float ms = 0.f;
+          VLM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+          const double per = ms / kReps;
+          ++tr.candidates;
+          if (shape == 0 && n == n0) {
+            curMs = per;
+            modelN = n0;
+          }
+          if (per < bestMs) {
+            bestMs = per;
+            bestShape = shape;
+            bestN = n;
+          }
+        }
+      }
+      if (bestN <= 0) continue;
+      // near ties keep the wave model's plan
+      if (modelN > 0 && !(bestMs < kMargin * curMs)) {
+        bestShape = 0;
+        bestN = modelN;
+        bestMs = curMs;
+      }
+      {
+        std::lock_guard<std::mutex> lk(tuneMutex());
+        tuneCache()[key] = TileChoice{bestShape, bestN, bestMs, curMs};
+      }
+      tr.shape[which] = bestShape;
+      tr.chunks[which] = bestN;
+      tr.ms[which] = bestMs;
+      tr.modelMs[which] = curMs;
+      applyTile(k, pl, which, e, M, bestShape, bestN);
+      changed = true;
+    }
+    VLM_CUDA(cudaStreamSynchronize(stream));
+    for (void* q : tmp) cudaFree(q);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    // the timing launches wrote no state; the device error word of the
+    // stream-ordered checks stays as it was (no near-field list was used)
+    if (changed) allocScratch();
+    tuned.push_back(tr);
   }
 
   // ---- coupled rotors (nr > 1, vlm_system) ----------------------------------
@@ -1145,6 +1400,7 @@ struct Case {
                                sizeof(double) * d.fl.size * nsteps, cudaMemcpyHostToDevice, stream));
   }
   void enqueueOne(int k) {
+    if (tuneOn() && sigRepeats(k) && !tunedFor(plans[k])) autotune(k);
     if (steadyStep(k)) {
       replayStep(k);
       return;
@@ -1208,6 +1464,7 @@ struct Case {
     }
     uploadFrames(1);
     iterSynced = false;
+    if (tuneOn() && sigRepeats(k) && !tunedFor(plans[k])) autotune(k);
     if (surr.on) surrPreStep(k);
     enqueueSolvePhase(k);
     VLM_CUDA(cudaGetLastError());
@@ -1411,7 +1668,7 @@ struct Case {
         VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
         launch_partial32(s.rec32, s.rec64, ch, pl.node.nchunks, pl.node.nrec, s.targets, M, s.part, s.err + 2,
                          opt.precision == VLM_PREC_FP32_NEAR64 ? s.nearScratch : nullptr, s.nearBytes, s.nacc,
-                         stream, s.edgeW);
+                         stream, s.edgeW, pl.node.shape, &nearOv);
       }
     };
     launch();  // warm
@@ -1564,6 +1821,15 @@ struct Case {
     else if (bok && b < d.nbC && k == "forceDist") v = forceDist(b);
     else if (k == "forceDim") v = forceDim();
     else if (k == "profileWork") v = {profileWork[0], profileWork[1]};
+    else if (k == "autotune") {
+      // per tuned signature: rowNear, rowFar, candidates timed, then for the
+      // wake nodes and the collocation points: shape, chunk count of the
+      // largest group, ms per launch of the choice, ms of the planner's plan
+      for (const TuneResult& t : tuned) {
+        v.insert(v.end(), {(double)t.rN, (double)t.rF, (double)t.candidates});
+        for (int w = 0; w < 2; ++w) v.insert(v.end(), {(double)t.shape[w], (double)t.chunks[w], t.ms[w], t.modelMs[w]});
+      }
+    }
     else if (bok && (k == "CP" || k == "nCap" || k == "vr")) {
       // the wing of the current iteration (of the open step between its phases)
       auto f = dget(frame(phase != 0 ? iter + 1 : iter), d.fl.size);
@@ -2420,11 +2686,12 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value) {
   else if (k == "gammaPlotSwitch") *value = C.W.P.gammaPlotSwitch;
   else if (k == "rollupStart") *value = C.d.rollupStart;
   else if (k == "rollupEnd") *value = C.d.rollupEnd;
+  else if (k == "nodeShape") *value = C.plans[std::min(C.iter + 1, C.W.nt)].node.shape;
   else if (k == "nearPairs" || k == "nodeChunks") {
     // near-field filament-target pairs of the last FP32 evaluation; chunks
     // of the next step's wake-node evaluation
     if (k == "nodeChunks") {
-      *value = C.iter < C.W.nt ? C.plans[C.iter + 1].node.nchunks : 0;
+      *value = C.plans[std::min(C.iter + 1, C.W.nt)].node.nchunks;
     } else {
       int v = 0;
       if (cudaStreamSynchronize(C.stream) != cudaSuccess ||
@@ -2538,6 +2805,11 @@ void vlm_default_surrogate_options(vlm_surrogate_options* o) {
   o->hidden = 128;
   o->layers = 4;
   o->seed = 1;
+}
+
+int vlm_case_set_tile(vlm_case* c, int shape, int chunks) {
+  if (!c) return VLM_ERR_INVALID;
+  return guard([&]() { c->c.setTile(shape, chunks); });
 }
 
 int vlm_case_set_surrogate(vlm_case* c, const vlm_surrogate_options* o) {

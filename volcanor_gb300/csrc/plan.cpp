@@ -32,17 +32,14 @@ constexpr int kMinChunk = 16;
 constexpr int64_t kMaxPartials = 1 << 24;  // (chunks x targets) bound: 384 MB of FP64 partial sums
 }  // namespace
 
-int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap, int targets_per_block) {
+int plan_count32(const Group* groups, int ngroups, int M, int slots, int cap, int targets_per_block) {
   int64_t total = 0;
   int maxRec = 0;
   for (int g = 0; g < ngroups; ++g) {
     total += std::max(0, groups[g].rec_count);
     maxRec = std::max(maxRec, groups[g].rec_count);
   }
-  if (total == 0 || M <= 0) {
-    for (int g = 0; g < ngroups; ++g) groups[g].chunk_begin = groups[g].chunk_count = 0;
-    return 0;
-  }
+  if (total == 0 || M <= 0) return 0;
   slots = std::max(1, slots);
   const int64_t bx = (M + targets_per_block - 1) / targets_per_block;
   const int nmax = std::max(1, std::min(maxRec / kMinChunk, 4 * slots));
@@ -71,7 +68,17 @@ int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, i
       bestQ = Q;
     }
   }
-  const int C = (maxRec + bestN - 1) / bestN;
+  return bestN;
+}
+
+int build_chunks32(Group* groups, int ngroups, int n, Chunk* chunks, int cap) {
+  int maxRec = 0;
+  for (int g = 0; g < ngroups; ++g) maxRec = std::max(maxRec, groups[g].rec_count);
+  if (n <= 0 || maxRec <= 0) {
+    for (int g = 0; g < ngroups; ++g) groups[g].chunk_begin = groups[g].chunk_count = 0;
+    return 0;
+  }
+  const int C = (maxRec + n - 1) / n;
   int nq = 0;
   for (int g = 0; g < ngroups; ++g) {
     Group& G = groups[g];
@@ -91,6 +98,11 @@ int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, i
     }
   }
   return nq;
+}
+
+int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap, int targets_per_block) {
+  const int n = plan_count32(groups, ngroups, M, slots, cap, targets_per_block);
+  return build_chunks32(groups, ngroups, n, chunks, cap);
 }
 
 }  // namespace vlm

@@ -137,8 +137,11 @@ struct Chunk {
 // Returns the number of chunks.
 int build_chunks(Group* groups, int ngroups, int chunk_size, Chunk* chunks, int cap);
 
-// Targets one FP32 kernel block covers.
+// Targets one FP32 kernel block covers (tile shape 0, the default).
 constexpr int kTargetsPerBlock32 = 512;
+// Compiled tile shapes of the FP32 kernel (launch_partial32's `shape`).
+constexpr int kPartial32Shapes = 2;
+int partial32_targets_per_block(int shape);
 
 // Chunk plan for the FP32 kernel (whose summation order is free): picks the
 // number of chunks per group that minimises the modelled run time of a grid
@@ -148,9 +151,14 @@ constexpr int kTargetsPerBlock32 = 512;
 // if cap is too small.
 int plan_chunks32(Group* groups, int ngroups, int M, int slots, Chunk* chunks, int cap,
                   int targets_per_block = kTargetsPerBlock32);
+// The two halves of plan_chunks32: the modelled best chunk count of the
+// largest group, and the table for a given count (the autotuner times
+// counts around the model's).
+int plan_count32(const Group* groups, int ngroups, int M, int slots, int cap, int targets_per_block);
+int build_chunks32(Group* groups, int ngroups, int n, Chunk* chunks, int cap);
 // Resident block slots of the FP32 kernel on the current device
 // (SMs x resident blocks per SM).
-int partial32_slots();
+int partial32_slots(int shape = 0);
 // Streaming multiprocessors of the current device (cached per device).
 int device_sm_count();
 
@@ -169,9 +177,16 @@ void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const
 // fixed-point range (4); ctl[1] counts the near pairs.  ctl must be zeroed before the call.
 // ew: the records' edge weights in lattice form (FP64 near field multiplies
 // by ew[4 rec + k] instead of the record's circulation), or null.
+// A second stream and two events on which launch_partial32 runs the
+// near-field detection and correction alongside the pair kernel.
+struct NearOverlap {
+  cudaStream_t stream;
+  cudaEvent_t fork, join;
+};
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
                       const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
-                      long long* nacc, cudaStream_t s, const double* ew = nullptr);
+                      long long* nacc, cudaStream_t s, const double* ew = nullptr, int shape = 0,
+                      const NearOverlap* ov = nullptr);
 // Converts FP64 records to FP32 records (near_factor <= 0 disables near-field);
 // ew as above (null: every active filament of a record carries its gam).
 void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s,

@@ -99,6 +99,7 @@ SIGNATURES = {
     "vlm_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
                                         ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(Options), ctypes.POINTER(_vp)]),
     "vlm_batch_destroy": (ctypes.c_int, [_vp]),
+    "vlm_case_set_tile": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "vlm_system_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                          ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(_vp)]),
     "vlm_system_create_from_dir": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(_vp)]),
@@ -320,6 +321,15 @@ class Case:
         rows = np.zeros((n, 10)) if with_ct else None
         _err(load().vlm_case_step(self._h, int(n), _ptr(rows) if with_ct else None))
         return rows
+
+    def set_tile(self, shape: int, chunks: int = 0):
+        """FP32 N-body tile shape for the steps to come (-1: autotune)."""
+        _err(load().vlm_case_set_tile(self._h, int(shape), int(chunks)))
+
+    def autotune(self) -> np.ndarray:
+        """Autotuner records: rows of rowNear, rowFar, candidates, then per
+        evaluation (wake nodes, collocation points) shape, chunks, ms, model ms."""
+        return self.get("autotune").reshape(-1, 11)
 
     # the step as separate calls (include/vlm.h): solve -> [loads] -> wake
     def aic_factor(self):
