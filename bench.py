@@ -308,6 +308,18 @@ def run_ours(args):
     exec_flops, exec_fils = (float(x) for x in case.get("profileWork"))
     near_pairs = case.geti("nearPairs") if prec == lib.PREC_FP32_NEAR64 else 0
     node_chunks = case.geti("nodeChunks")
+    tune = None
+    if prec != lib.PREC_FP64:
+        t = case.autotune()
+        if t.size:
+            r = t[-1]
+            tune = {"signature": [int(r[0]), int(r[1])], "candidates_timed": int(r[2]),
+                    "wake_nodes": {"shape": int(r[3]), "chunks_largest_group": int(r[4]), "ms": round(r[5], 4),
+                                   "wave_model_ms": round(r[6], 4)},
+                    "collocation_points": {"shape": int(r[7]), "chunks_largest_group": int(r[8]),
+                                           "ms": round(r[9], 4), "wave_model_ms": round(r[10], 4)},
+                    "note": "FP32 pair kernel alone, live steady-state evaluation; shape 0 = 512 targets/block, "
+                            "4 stages, 2 blocks/SM; 1 = 256 targets/block, 3 stages, 3 blocks/SM"}
     flops = RING_FLOP * rp + FIL_FLOP * fp
     achieved = flops / (ms_l / 1e3) / 1e12
     pk = peaks()
@@ -346,7 +358,7 @@ def run_ours(args):
                                      "(sources, targets, partials) stays in L2",
                      "kernel": "k_partial32" if prec != lib.PREC_FP64 else "k_partial64",
                      "ms_per_launch": round(ms_l, 4), "ring_pairs_per_launch": rp, "fil_pairs_per_launch": fp,
-                     "near_pairs_per_launch": near_pairs, "chunks": node_chunks,
+                     "near_pairs_per_launch": near_pairs, "chunks": node_chunks, "autotune": tune,
                      "executed_tflops": round(exec_flops / (ms_l / 1e3) / 1e12, 3),
                      "executed_frac": round(exec_flops / (ms_l / 1e3) / 1e12 / fp32_peak, 4),
                      "executed_fil_pairs_per_launch": exec_fils,
