@@ -299,7 +299,9 @@ int vlm_case_vind_points(vlm_case* c, const double* P, int64_t M, double* V);
  * of another precision, summation block or solve mode may also load it and
  * continue in its own arithmetic (a refining case factors the restored AIC
  * in FP32 when the file has no FP32 factors).  A case of other dimensions or
- * another format -> VLM_ERR_INVALID.  Not available with the surrogate
+ * another format -> VLM_ERR_INVALID.  A case with the surrogate saves its
+ * flow state (not the network or the surrogate's phase, so another case --
+ * e.g. the plain FP64 form -- can continue from it); it cannot load one
  * (VLM_ERR_UNSUPPORTED). */
 int vlm_case_checkpoint_save(vlm_case* c, const char* path);
 int vlm_case_checkpoint_load(vlm_case* c, const char* path);

@@ -53,3 +53,40 @@ def test_surrogate_reverts_when_the_audit_fails():
     assert st["audits"] > 0 and st["reverts"] == st["audits"] and st["active_steps"] == 0
     ref = forward_case(nt, lib.PREC_FP32_NEAR64, use_graph=False).step(nt)[:, 1]
     assert np.array_equal(ct, ref)
+
+
+def test_ct_error_with_the_surrogate_active(tmp_path):
+    """CT error against the plain FP64 form over 10-step windows started from
+    the surrogate run's own state (inside the free wake's pre-chaotic
+    horizon), on windows where the network summed the old far wake at every
+    step: the 4-blade forward-flight rotor with its 1-revolution near wake and
+    the default surrogate options (old far wake = past the 216 youngest
+    filaments per blade, audit tolerance 0.1), steps 801-880.  Measured
+    ~1e-3: the network's audited error (a few percent of the old-far-wake
+    velocity) shows in CT at that level, so the 1e-4 CT target is not met
+    with the surrogate active; the bound here is the measured level with
+    margin, 5e-3."""
+    nt = 880
+    c = C.rotor_4blade_forward(nt=nt)
+    c.write(tmp_path / "case")
+    g = lib.Case.from_case_dir(tmp_path / "case", precision=lib.PREC_FP32_NEAR64)
+    g.set_surrogate()
+    g.start()
+    g.step(800, with_ct=False)
+    f = lib.Case.from_case_dir(tmp_path / "case", precision=lib.PREC_FP64)
+    f.start()
+    active_errs = []
+    for j in range(8):
+        ck = tmp_path / "w.ckpt"
+        g.checkpoint_save(ck)
+        a0 = g.surrogate_stats()["active_steps"]
+        a = g.step(10)[:, 1]
+        active = g.surrogate_stats()["active_steps"] - a0
+        f.checkpoint_load(ck)
+        b = f.step(10)[:, 1]
+        err = float(np.max(np.abs(a - b) / np.abs(b)))
+        print("window", j, "active steps", active, "CT error", err)
+        if active == 10:
+            active_errs.append(err)
+    assert active_errs, "no window with the network active on every step"
+    assert max(active_errs) < 5e-3

@@ -1552,7 +1552,8 @@ struct Case {
   void checkpointSave(const std::string& path) {
     useDevice();
     if (!started) throw StatusError(VLM_ERR_STATE, "checkpoint before vlm_case_start");
-    if (surr.on) throw StatusError(VLM_ERR_UNSUPPORTED, "checkpoints of a case with the surrogate");
+    // a case with the surrogate saves its flow state; the network and the
+    // surrogate's phase are not part of a checkpoint
     VLM_CUDA(cudaStreamSynchronize(stream));
     std::ofstream f(path, std::ios::binary);
     if (!f) throw StatusError(VLM_ERR_IO, "cannot open " + path);
