@@ -218,6 +218,110 @@ __device__ __forceinline__ void rec_lat_pair(const float4* __restrict__ R4, cons
   }
 }
 
+// ---- packed pairs of FP32 values (the sm_100 family's f32x2 instructions) --
+// A thread with two targets evaluates every record for both at once: each
+// add / mul / fma below is one instruction for the two lanes, each lane
+// rounded exactly as the scalar instruction (.rn, .ftz as the unit's
+// -ftz=true).  The scalar functions above are rewritten only where a
+// negation would need its own instruction: -(a b) as (-a) b with the exactly
+// negated corner vector c - P, -(t - e) as e - t; both exact, so every lane
+// carries the scalar path's bits (k_near_fix recomputes those).
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2pack(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ f2 f2splat(float a) { return f2pack(a, a); }
+__device__ __forceinline__ void f2unpack(f2 r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f2 f2sub(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2mul(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 f2rsqrt(f2 a) {
+  float x, y;
+  f2unpack(a, x, y);
+  return f2pack(rsqrtf(x), rsqrtf(y));
+}
+
+// corner_vector for both targets: r = P - c, 1/|r|
+__device__ __forceinline__ void corner_pair(f2 px, f2 py, f2 pz, float cx, float cy, float cz, f2& rx, f2& ry, f2& rz,
+                                            f2& inv) {
+  rx = f2sub(px, f2splat(cx));
+  ry = f2sub(py, f2splat(cy));
+  rz = f2sub(pz, f2splat(cz));
+  inv = f2rsqrt(f2fma(rx, rx, f2fma(ry, ry, f2fma(rz, rz, f2splat(kS2Min)))));
+}
+
+// fil_fp32 for both targets; (cxk, cyk, czk) is corner K itself, whose
+// negated corner vector c - P the cross product takes
+template <int K>
+__device__ __forceinline__ void fil_pair(const RecView& v, f2 px, f2 py, f2 pz, float cxk, float cyk, float czk,
+                                         f2 rxk, f2 ryk, f2 rzk, f2 invk, f2 rxj, f2 ryj, f2 rzj, f2 invj, f2& ax,
+                                         f2& ay, f2& az) {
+  const f2 nrxk = f2sub(f2splat(cxk), px), nryk = f2sub(f2splat(cyk), py), nrzk = f2sub(f2splat(czk), pz);
+  const f2 kx = f2fma(ryk, rzj, f2mul(nrzk, ryj));
+  const f2 ky = f2fma(rzk, rxj, f2mul(nrxk, rzj));
+  const f2 kz = f2fma(rxk, ryj, f2mul(nryk, rxj));
+  const f2 c2 = f2fma(kx, kx, f2fma(ky, ky, f2mul(kz, kz)));
+  const f2 tt = f2fma(f2splat(v.ex[K]), rxk, f2fma(f2splat(v.ey[K]), ryk, f2mul(f2splat(v.ez[K]), rzk)));
+  const f2 d = f2fma(tt, invk, f2mul(f2sub(f2splat(v.eev[K]), tt), invj));
+  const f2 f = f2mul(d, f2rsqrt(f2fma(c2, c2, f2splat(v.a4v[K]))));
+  ax = f2fma(f, kx, ax);
+  ay = f2fma(f, ky, ay);
+  az = f2fma(f, kz, az);
+}
+
+// ring_fp32 for both targets (all four edges)
+__device__ __forceinline__ void ring_pair(const float4* __restrict__ R4, const float (&cx)[4], const float (&cy)[4],
+                                          const float (&cz)[4], f2 px, f2 py, f2 pz, f2& ax, f2& ay, f2& az) {
+  RecView v;
+  load_view(R4, v);
+  f2 rx[4], ry[4], rz[4], inv[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) corner_pair(px, py, pz, cx[k], cy[k], cz[k], rx[k], ry[k], rz[k], inv[k]);
+  fil_pair<0>(v, px, py, pz, cx[0], cy[0], cz[0], rx[0], ry[0], rz[0], inv[0], rx[1], ry[1], rz[1], inv[1], ax, ay, az);
+  fil_pair<1>(v, px, py, pz, cx[1], cy[1], cz[1], rx[1], ry[1], rz[1], inv[1], rx[2], ry[2], rz[2], inv[2], ax, ay, az);
+  fil_pair<2>(v, px, py, pz, cx[2], cy[2], cz[2], rx[2], ry[2], rz[2], inv[2], rx[3], ry[3], rz[3], inv[3], ax, ay, az);
+  fil_pair<3>(v, px, py, pz, cx[3], cy[3], cz[3], rx[3], ry[3], rz[3], inv[3], rx[0], ry[0], rz[0], inv[0], ax, ay, az);
+}
+
+// rec_lat_pair<2> with packed pairs
+__device__ __forceinline__ void rec_lat_packed(const float4* __restrict__ R4, const float (&cx)[4],
+                                               const float (&cy)[4], const float (&cz)[4], f2 px, f2 py, f2 pz, f2& ax,
+                                               f2& ay, f2& az) {
+  RecView v;
+  load_view(R4, v);
+  f2 rx[4], ry[4], rz[4], inv[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) corner_pair(px, py, pz, cx[k], cy[k], cz[k], rx[k], ry[k], rz[k], inv[k]);
+  fil_pair<0>(v, px, py, pz, cx[0], cy[0], cz[0], rx[0], ry[0], rz[0], inv[0], rx[1], ry[1], rz[1], inv[1], ax, ay, az);
+  fil_pair<1>(v, px, py, pz, cx[1], cy[1], cz[1], rx[1], ry[1], rz[1], inv[1], rx[2], ry[2], rz[2], inv[2], ax, ay, az);
+  const bool t2 = v.a4v[2] >= 0.f, t3 = v.a4v[3] >= 0.f;
+  if (t2 || t3) {
+    corner_pair(px, py, pz, cx[3], cy[3], cz[3], rx[3], ry[3], rz[3], inv[3]);
+    if (t2)
+      fil_pair<2>(v, px, py, pz, cx[2], cy[2], cz[2], rx[2], ry[2], rz[2], inv[2], rx[3], ry[3], rz[3], inv[3], ax, ay,
+                  az);
+    if (t3)
+      fil_pair<3>(v, px, py, pz, cx[3], cy[3], cz[3], rx[3], ry[3], rz[3], inv[3], rx[0], ry[0], rz[0], inv[0], ax, ay,
+                  az);
+  }
+}
+
 // One block = 8 consumer warps (256 threads x kTPT targets) + 1 producer
 // warp.  The producer's lane 0 streams the chunk's records through kStages
 // shared stages with bulk copies; consumers wait on a stage's FULL barrier,
@@ -306,7 +410,33 @@ __global__ void __launch_bounds__(kBlockW, kMinBlocks) k_partial32(const float* 
       ok = false;
       if (lane == 0) atomicExch(ctl, 1);
     }
-    if (ok) {
+    if (ok && kTPT == 2) {
+      // both targets in packed pairs
+      const int n = min(kTileW, ch.rec_count - t * kTileW);
+      const float* tile = stage + s * kTileW * kRec32;
+      const f2 PX = f2pack(px[0], px[kTPT - 1]), PY = f2pack(py[0], py[kTPT - 1]), PZ = f2pack(pz[0], pz[kTPT - 1]);
+      f2 AX = 0ull, AY = 0ull, AZ = 0ull;  // +0.0f in both lanes
+#pragma unroll 1
+      for (int r = 0; r < n; ++r) {
+        const float4* R4 = reinterpret_cast<const float4*>(tile + r * kRec32);
+        const float4 q0 = R4[0], q1 = R4[1], q2 = R4[2];  // corners
+        const float cx[4] = {q0.x, q0.w, q1.z, q2.y};
+        const float cy[4] = {q0.y, q1.x, q1.w, q2.z};
+        const float cz[4] = {q0.z, q1.y, q2.x, q2.w};
+        if (!LAT) ring_pair(R4, cx, cy, cz, PX, PY, PZ, AX, AY, AZ);
+        else rec_lat_packed(R4, cx, cy, cz, PX, PY, PZ, AX, AY, AZ);
+      }
+      float a0, a1;
+      f2unpack(AX, a0, a1);
+      acc64[0][0] += (double)a0;
+      acc64[kTPT - 1][0] += (double)a1;
+      f2unpack(AY, a0, a1);
+      acc64[0][1] += (double)a0;
+      acc64[kTPT - 1][1] += (double)a1;
+      f2unpack(AZ, a0, a1);
+      acc64[0][2] += (double)a0;
+      acc64[kTPT - 1][2] += (double)a1;
+    } else if (ok) {
       const int n = min(kTileW, ch.rec_count - t * kTileW);
       const float* tile = stage + s * kTileW * kRec32;
       float ax[kTPT], ay[kTPT], az[kTPT];
