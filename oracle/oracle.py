@@ -83,6 +83,8 @@ def lib():
         L.or_sys_step.argtypes = [vp, i32]
         L.or_sys_rotor.restype = vp
         L.or_sys_rotor.argtypes = [vp, i32]
+        L.or_c81_lookup.restype = ctypes.c_double
+        L.or_c81_lookup.argtypes = [cp, i32, ctypes.c_double, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -243,6 +245,11 @@ class System:
 
     def step(self, n: int = 1):
         _check(lib().or_sys_step(self._h, int(n)))
+
+
+def c81_lookup(path, coeff: int, alpha_deg: float, mach: float) -> float:
+    """CL (0), CD (1) or CM (2) of a C81 file at (alpha in degrees, Mach)."""
+    return float(lib().or_c81_lookup(str(path).encode(), int(coeff), float(alpha_deg), float(mach)))
 
 
 def vind_rings(corners, rvc, gam, P, chunk: int = 0) -> np.ndarray:

@@ -37,6 +37,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -439,6 +440,106 @@ struct WingPanel {     // classdef.f90:106-179
   }
 };
 
+// An airfoil table (libC81.f90:6-30): CL, CD, CM over angle of attack
+// (degrees) x Mach; C?(i, j) stored at i + N? * j.
+struct C81 {
+  int ML = 0, NL = 0, MD = 0, ND = 0, MM = 0, NM = 0;
+  std::vector<double> MaL, MaD, MaM, AL, AD, AM, CL, CD, CM;
+
+  // one Fortran Fw.0 input field of `w` characters at `pos` (blank: 0)
+  static double fld(const std::string& line, size_t pos, size_t w) {
+    if (pos >= line.size()) return 0.0;
+    std::string f = line.substr(pos, w);
+    size_t a = f.find_first_not_of(' ');
+    if (a == std::string::npos) return 0.0;
+    return std::strtod(f.c_str() + a, nullptr);
+  }
+  // libC81.f90:128-188: A30,6I2 header; per coefficient a Mach line
+  // (7X,9F7.0) and per angle a line (10F7.0: angle + 9 values), with a
+  // (7X,nF7.0) continuation line when there are more than 9 Mach numbers
+  void read(const std::string& path) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open C81 file " + path);
+    std::vector<std::string> L;
+    for (std::string line; std::getline(f, line);) {
+      if (!line.empty() && line.back() == '\r') line.pop_back();
+      L.push_back(line);
+    }
+    size_t k = 0;
+    auto next = [&]() -> const std::string& {
+      if (k >= L.size()) throw std::runtime_error("C81 file ends early: " + path);
+      return L[k++];
+    };
+    const std::string& h = next();
+    int* dims[6] = {&ML, &NL, &MD, &ND, &MM, &NM};
+    for (int i = 0; i < 6; ++i) *dims[i] = (int)fld(h, 30 + 2 * i, 2);
+    auto block = [&](int M, int N, std::vector<double>& Ma, std::vector<double>& A, std::vector<double>& C) {
+      if (M < 1 || N < 1 || M > 18) throw std::runtime_error("C81 table dimensions out of range: " + path);
+      Ma.assign(M, 0.0);
+      A.assign(N, 0.0);
+      C.assign((size_t)M * N, 0.0);
+      const std::string& m1 = next();
+      for (int j = 0; j < std::min(9, M); ++j) Ma[j] = fld(m1, 7 + 7 * j, 7);
+      if (M > 9) {
+        const std::string& m2 = next();
+        for (int j = 9; j < M; ++j) Ma[j] = fld(m2, 7 + 7 * (j - 9), 7);
+      }
+      for (int i = 0; i < N; ++i) {
+        const std::string& r1 = next();
+        A[i] = fld(r1, 0, 7);
+        for (int j = 0; j < std::min(9, M); ++j) C[i + (size_t)N * j] = fld(r1, 7 + 7 * j, 7);
+        if (M > 9) {
+          const std::string& r2 = next();
+          for (int j = 9; j < M; ++j) C[i + (size_t)N * j] = fld(r2, 7 + 7 * (j - 9), 7);
+        }
+      }
+    };
+    block(ML, NL, MaL, AL, CL);
+    block(MD, ND, MaD, AD, CD);
+    block(MM, NM, MaM, AM, CM);
+  }
+  // libC81.f90:302-332 (1-based indices out); the end tests use the
+  // single-precision epsilon(1.)
+  static void interval(const std::vector<double>& A, double x, int& i1, int& i2) {
+    const int n = (int)A.size();
+    i1 = 1;
+    i2 = n;
+    while (i1 != i2 && i2 != i1 + 1) {
+      const int i = (int)std::floor(double(float(i1 + i2) * 0.5f));
+      if (x < A[i - 1]) i2 = i;
+      else if (x > A[i - 1]) i1 = i;
+      else i1 = i2 = i;
+    }
+    const double epsf = (double)std::numeric_limits<float>::epsilon();
+    if (std::fabs(A[i1 - 1] - x) <= epsf) i2 = i1;
+    else if (std::fabs(A[i2 - 1] - x) <= epsf) i1 = i2;
+  }
+  // getCL / getCD / getCM (libC81.f90:190-300) with getBilinearInterp (:334-351)
+  static double lookup(const std::vector<double>& A, const std::vector<double>& Ma, const std::vector<double>& C,
+                       double alpha, double mach) {
+    const int N = (int)A.size();
+    int a1, a2, m1, m2;
+    interval(A, alpha, a1, a2);
+    interval(Ma, mach, m1, m2);
+    auto c = [&](int i, int j) { return C[(i - 1) + (size_t)N * (j - 1)]; };
+    if (a1 == a2) {
+      if (m1 == m2) return c(a1, m1);
+      return c(a1, m1) + ((mach - Ma[m1 - 1]) * (c(a1, m2) - c(a1, m1))) / (Ma[m2 - 1] - Ma[m1 - 1]);
+    }
+    if (m1 == m2) return c(a1, m1) + ((alpha - A[a1 - 1]) * (c(a2, m1) - c(a1, m1))) / (A[a2 - 1] - A[a1 - 1]);
+    const double x1 = A[a1 - 1], x2 = A[a2 - 1], y1 = Ma[m1 - 1], y2 = Ma[m2 - 1];
+    const double v1 = y2 - mach, v2 = mach - y1;
+    const double r1 = c(a1, m1) * v1 + c(a1, m2) * v2;
+    const double r2 = c(a2, m1) * v1 + c(a2, m2) * v2;
+    double g = (x2 - alpha) * r1 + (alpha - x1) * r2;
+    g = g / (x2 - x1) / (y2 - y1);
+    return g;
+  }
+  double getCL(double a, double m) const { return lookup(AL, MaL, CL, a, m); }
+  double getCD(double a, double m) const { return lookup(AD, MaD, CD, a, m); }
+  double getCM(double a, double m) const { return lookup(AM, MaM, CM, a, m); }
+};
+
 struct Blade {         // classdef.f90:238-358
   int nc = 0, ns = 0;
   std::vector<WingPanel> wiP;     // [i + nc*j]
@@ -456,7 +557,8 @@ struct Blade {         // classdef.f90:238-358
       secDragDir, secLiftInPlane, secLiftOutPlane, secLiftInPlaneUnsteady, secLiftOutPlaneUnsteady,
       secLiftUnsteady, secDrag, secDragInduced, secDragProfile, secDragUnsteady, secChordwiseResVel, secCP;
   std::vector<double> secChord, secArea, secAlpha, secPhi, secTheta, secViz, secVix, secCL, secCD, secCLu,
-      secMflap, secMflapArm;
+      secMflap, secMflapArm, secCM;
+  std::vector<int> airfoilNo;  // 1-based airfoil table of each section
   int spanwiseLiftSwitch = 0;
 
   WingPanel& w(int i, int j) { return wiP[i + nc * j]; }
@@ -480,6 +582,9 @@ struct Rotor {
   double thetaTwist = 0;
   int ductSwitch = 0, axisymmetrySwitch = 0, spanwiseLiftSwitch = 0, symmetricTau = 0;
   int customTrajectorySwitch = 0, forceCalcSwitch = 0, nAirfoils = 0;
+  std::vector<double> airfoilSectionLimit, alpha0v;
+  std::vector<std::string> airfoilFile;
+  std::vector<C81> c81;
   double pivotLE = 0, flapHinge = 0;
   double apparentViscCoeff = 0, decayCoeff = 0, spanwiseCore = 0;
   int wakeTruncateNt = 0, prescWakeAfterTruncNt = 0, prescWakeGenNt = 0, prescWakeNt = 0;
@@ -1432,7 +1537,73 @@ struct Sim {
       for (int ib = 1; ib < R.nb; ++ib)
         for (size_t k = 0; k < R.blade[ib].wiP.size(); ++k) R.blade[ib].wiP[k].velCPTotal = R.blade[0].wiP[k].velCPTotal;
     rotor_calc_secAlpha();
-    rotor_calc_force();
+    if (R.forceCalcSwitch == 1) rotor_calc_force_alpha();
+    else rotor_calc_force();
+  }
+  // classdef.f90:4734-4747 (rotor_calc_force_alpha) with blade_calc_force_alpha
+  // (:2091-2105), blade_lookup_secCoeffs (:2178-2195), blade_secCoeffsToSecForces
+  // (:2146-2176), blade_getSecDynamicPressure (:2058-2069), blade_sumSecToNetForces
+  // (:2368-2380) and rotor_sumBladeToNetForces (:4954-4988)
+  void rotor_calc_force_alpha() {
+    R.forceInertial = V3();
+    rotor_dirLiftDrag();
+    for (int ib = 0; ib < R.nb; ++ib) {
+      Blade& b = R.blade[ib];
+      const int ns = b.ns;
+      b.secCM.assign(ns, 0.0);
+      for (int is = 0; is < ns; ++is) {
+        const double mach = norm2(b.secChordwiseResVel[is]) / velSound;
+        const double aDeg = b.secAlpha[is] * RAD2DEG;
+        const C81& t = R.c81[b.airfoilNo[is] - 1];
+        b.secCL[is] = t.getCL(aDeg, mach);
+        b.secCD[is] = t.getCD(aDeg, mach);
+        b.secCM[is] = t.getCM(aDeg, mach);
+        b.secCLu[is] = 0.0;
+      }
+      for (int is = 0; is < ns; ++is) {
+        const double m = norm2(b.secChordwiseResVel[is]);
+        const double lead = ((0.5 * density) * (m * m)) * b.secArea[is];
+        b.secLift[is] = (b.secLiftDir[is] * lead) * b.secCL[is];
+        b.secLiftUnsteady[is] = (b.secLiftDir[is] * lead) * b.secCLu[is];
+        double gs = 0.0;
+        for (int ic = 0; ic < b.nc; ++ic) gs = gs + b.w(ic, is).vr.gam;
+        V3 fi = cross(b.yAxis, b.secChordwiseResVel[is]);
+        fi = fsign(1.0, gs) * unitVec(fi);
+        fi = norm2(b.secLift[is]) * fi;
+        fi = fi + norm2(b.secDrag[is]) * unitVec(b.secChordwiseResVel[is]);
+        b.secForceInertial[is] = fi;
+      }
+      for (int is = 0; is < ns; ++is) {
+        b.secDragInduced[is] = V3();
+        b.secDrag[is] = b.secDragProfile[is] + b.secDragInduced[is];
+      }
+      V3 fi, li, dr, lu, dp, di, du;
+      double mf = 0.0;
+      for (int is = 0; is < ns; ++is) {
+        fi = fi + b.secForceInertial[is];
+        li = li + b.secLift[is];
+        dr = dr + b.secDrag[is];
+        lu = lu + b.secLiftUnsteady[is];
+        dp = dp + b.secDragProfile[is];
+        di = di + b.secDragInduced[is];
+        du = du + b.secDragUnsteady[is];
+        mf = mf + b.secMflap[is];
+      }
+      b.forceInertial = fi; b.lift = li; b.drag = dr; b.liftUnsteady = lu;
+      b.dragProfile = dp; b.dragInduced = di; b.dragUnsteady = du; b.MflapLift = mf;
+    }
+    R.forceInertial = V3(); R.liftPrev = R.lift; R.lift = V3(); R.drag = V3(); R.liftUnsteady = V3();
+    R.dragInduced = V3(); R.dragProfile = V3(); R.dragUnsteady = V3();
+    for (int ib = 0; ib < R.nb; ++ib) {
+      Blade& b = R.blade[ib];
+      R.forceInertial = R.forceInertial + b.forceInertial;
+      R.lift = R.lift + b.lift;
+      R.drag = R.drag + b.drag;
+      R.liftUnsteady = R.liftUnsteady + b.liftUnsteady;
+      R.dragInduced = R.dragInduced + b.dragInduced;
+      R.dragProfile = R.dragProfile + b.dragProfile;
+      R.dragUnsteady = R.dragUnsteady + b.dragUnsteady;
+    }
   }
   // classdef.f90:4151-4179 + libMath.f90:48-83
   void calcAIC() {
@@ -1618,7 +1789,17 @@ struct Sim {
       }
     }
     if (R.ductSwitch != 0) throw std::runtime_error("ductSwitch is not supported by this oracle");
-    if (R.forceCalcSwitch != 0) throw std::runtime_error("only forceCalcSwitch = 0 is supported");
+    if (R.forceCalcSwitch < 0 || R.forceCalcSwitch > 1)
+      throw std::runtime_error("only forceCalcSwitch = 0 or 1 is supported");
+    // AIRFOILS (classdef.f90:2605, 2754-2765)
+    if (R.forceCalcSwitch > 0 && R.nAirfoils == 0) throw std::runtime_error("No. of airfoil tables set to 0 in geomXX.in");
+    for (int i = 0; i < R.nAirfoils; ++i) {
+      R.airfoilSectionLimit.push_back(g.d("AIRFOILS", "airfoilSectionLimit", 1.0, i));
+      R.alpha0v.push_back(g.d("AIRFOILS", "alpha0", 0.0, i));
+      R.airfoilFile.push_back(g.s("AIRFOILS", "airfoilFile", "0", i));
+    }
+    if (R.forceCalcSwitch == 1 && R.axisymmetrySwitch == 1)
+      throw std::runtime_error("forceCalcSwitch = 1 with axisymmetry is not supported");
     if (R.bladeDynamicsSwitch != 0 || R.bodyDynamicsSwitch != 0)
       throw std::runtime_error("blade/body dynamics are not supported");
     if (R.customTrajectorySwitch != 0 && R.customTrajectorySwitch != 1)
@@ -1957,6 +2138,30 @@ struct Sim {
       }
     } else {
       r.nonDimforceDenominator = ((0.5 * density) * ((r.radius * (1.0 - r.root_cut)) * r.chord)) * dot(r.velBody, r.velBody);
+    }
+    // section airfoils (classdef.f90:3693-3725)
+    if (r.nAirfoils > 0) {
+      r.c81.assign(r.nAirfoils, C81());
+      for (int i = 0; i < r.nAirfoils; ++i)
+        if (!r.airfoilFile[i].empty() && r.airfoilFile[i][0] != '0') {
+          const std::string& f = r.airfoilFile[i];
+          r.c81[i].read(f[0] == '/' || baseDir.empty() ? f : baseDir + "/" + f);
+        }
+      const double secCPLoc = 0.5;
+      for (auto& b : r.blade) {
+        b.airfoilNo.assign(ns, 1);
+        if (r.nAirfoils == 1) continue;
+        const V3 leftTip = b.w(0, 0).PC[3] * (1.0 - secCPLoc) + b.w(nc - 1, 0).PC[2] * secCPLoc;
+        for (int is = 0; is < ns; ++is) {
+          const double rbyR = std::fabs(dot(b.secCP[is] - leftTip, b.xAxis)) + r.root_cut;
+          if (rbyR > 1.0) throw std::runtime_error("r/R value is greater than 1 in airfoil selection");
+          for (int i = 0; i < r.nAirfoils; ++i)
+            if (r.airfoilSectionLimit[i] >= rbyR) {
+              b.airfoilNo[is] = i + 1;
+              break;
+            }
+        }
+      }
     }
     for (auto& b : r.blade) {
       if (NW > 0) {
@@ -2415,6 +2620,18 @@ int or_sys_start(void* h) { return guarded([&]() { static_cast<System*>(h)->star
 int or_sys_step(void* h, int n) {
   return guarded([&]() { for (int k = 0; k < n; ++k) static_cast<System*>(h)->step(); });
 }
+// Coefficient c (0 CL, 1 CD, 2 CM) of the C81 file at path, at
+// (alpha degrees, Mach) (libC81.f90 getCL/getCD/getCM); NaN on error.
+double or_c81_lookup(const char* path, int c, double alpha, double mach) {
+  double v = std::nan("");
+  guarded([&]() {
+    C81 t;
+    t.read(path);
+    v = c == 0 ? t.getCL(alpha, mach) : (c == 1 ? t.getCD(alpha, mach) : t.getCM(alpha, mach));
+  });
+  return v;
+}
+
 // Rotor ir (0-based) as a Sim handle for or_get / or_geti (owned by the system).
 void* or_sys_rotor(void* h, int ir) {
   System* y = static_cast<System*>(h);

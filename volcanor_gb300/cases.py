@@ -126,6 +126,49 @@ class Case:
         return d
 
 
+def c81_text(name: str, mach, alpha, cl, cd, cm) -> str:
+    """An airfoil table in the C81 layout the reference reads and writes
+    (libC81.f90:60-188): a 30-column name and six 2-digit counts (Mach
+    numbers and angles for lift, drag, moment), then per coefficient a line of
+    Mach numbers (7 blank columns, 7-column fields, 3 decimals) and per angle
+    a line of the angle (7 columns, 2 decimals) and the values (7 columns, 3
+    decimals); more than 9 Mach numbers continue on a second line.  cl, cd,
+    cm: arrays [angle][Mach]."""
+    import numpy as np
+    mach, alpha = np.asarray(mach, float), np.asarray(alpha, float)
+    M, N = len(mach), len(alpha)
+    if not (1 <= M <= 18):
+        raise ValueError("1 to 18 Mach numbers")
+    out = [f"{name[:30]:<30s}" + "".join(f"{v:02d}" for v in (M, N, M, N, M, N))]
+    f73 = lambda v: f"{v:7.3f}"
+    for tab in (cl, cd, cm):
+        tab = np.asarray(tab, float).reshape(N, M)
+        out.append(" " * 7 + "".join(f73(v) for v in mach[:9]))
+        if M > 9:
+            out.append(" " * 7 + "".join(f73(v) for v in mach[9:]))
+        for i in range(N):
+            out.append(f"{alpha[i]:7.2f}" + "".join(f73(v) for v in tab[i, :9]))
+            if M > 9:
+                out.append(" " * 7 + "".join(f73(v) for v in tab[i, 9:]))
+    return "\n".join(out) + "\n"
+
+
+def synthetic_airfoil(name: str, cl_slope: float = 6.0, alpha0_deg: float = 0.0, cd0: float = 0.008,
+                      nmach: int = 6) -> str:
+    """A smooth synthetic table: angles -20..20 deg (2 deg), Mach 0..0.75,
+    CL = slope sin(alpha - alpha0) / sqrt(1 - M^2) (Prandtl-Glauert), CD =
+    cd0 + 0.5 sin^2(alpha), CM = -0.02 - 0.05 sin(alpha)."""
+    import numpy as np
+    mach = np.linspace(0.0, 0.75, nmach)
+    alpha = np.arange(-20.0, 20.0 + 1e-9, 2.0)
+    a = np.radians(alpha)[:, None]
+    pg = 1.0 / np.sqrt(1.0 - mach[None, :] ** 2)
+    cl = cl_slope * np.sin(a - np.radians(alpha0_deg)) * pg
+    cd = cd0 + 0.5 * np.sin(a) ** 2 + 0 * pg
+    cm = -0.02 - 0.05 * np.sin(a) + 0 * pg
+    return c81_text(name, mach, alpha, cl, cd, cm)
+
+
 @dataclass
 class SystemCase:
     """Coupled rotors (nr > 1): one config.nml, geom01.nml .. geomNN.nml."""

@@ -218,6 +218,8 @@ struct Case {
     d.prescGenNt = P.prescWakeGenNt;
     d.skewLimit = P.skewLimit;
     d.chord = P.chord;
+    d.forceCalc = P.forceCalcSwitch;
+    d.velSound = W.velSound;
     d.fl = frame_layout(d.nb, d.nc, d.ns);
     if (d.nc > 64) throw StatusError(VLM_ERR_UNSUPPORTED, "nc > 64 chordwise panels");
     if (d.n > 8192) throw StatusError(VLM_ERR_UNSUPPORTED, "more than 8192 panels per rotor");
@@ -312,6 +314,15 @@ struct Case {
       return p;
     };
     s.wRvc = up(rvc);
+    if (d.forceCalc == 1) {
+      s.c81 = up(W.airfoils.data);
+      s.c81Off = dalloc<int>(W.airfoils.offset.size(), owned);
+      VLM_CUDA(cudaMemcpy(s.c81Off, W.airfoils.offset.data(), sizeof(int) * W.airfoils.offset.size(),
+                          cudaMemcpyHostToDevice));
+      s.airfoilNo = dalloc<int>(W.airfoilOfSection.size(), owned);
+      VLM_CUDA(cudaMemcpy(s.airfoilNo, W.airfoilOfSection.data(), sizeof(int) * W.airfoilOfSection.size(),
+                          cudaMemcpyHostToDevice));
+    }
     s.panArea = up(area);
     s.panMeanChord = up(mc);
     s.panMeanSpan = up(msp);

@@ -1241,6 +1241,51 @@ __global__ void k_step_begin(Dims d, DevState s) {
   if (threadIdx.x == 0) s.devIter[0] = it;
 }
 
+// ---- airfoil tables (libC81.f90:190-351) ------------------------------------
+// interval of x in the ascending axis A[0..n): 1-based (i1, i2) as the
+// reference's binary search leaves them, ends snapped within the
+// single-precision epsilon
+__device__ void c81_interval(const double* A, int n, double x, int& i1, int& i2) {
+  i1 = 1;
+  i2 = n;
+  while (i1 != i2 && i2 != i1 + 1) {
+    const int i = (i1 + i2) / 2;
+    if (x < A[i - 1]) i2 = i;
+    else if (x > A[i - 1]) i1 = i;
+    else i1 = i2 = i;
+  }
+  const double epsf = 1.1920928955078125e-07;  // epsilon(1.) of the default real kind
+  if (fabs(A[i1 - 1] - x) <= epsf) i2 = i1;
+  else if (fabs(A[i2 - 1] - x) <= epsf) i1 = i2;
+}
+// coefficient c (0 lift, 1 drag, 2 moment) of table T at (alpha degrees, Mach)
+__device__ double c81_get(const double* T, int c, double alpha, double mach) {
+  size_t o = 6;
+  int nm = 0, na = 0;
+  for (int k = 0; k <= c; ++k) {
+    nm = (int)T[2 * k];
+    na = (int)T[2 * k + 1];
+    if (k < c) o += (size_t)nm + na + (size_t)nm * na;
+  }
+  const double* Ma = T + o;
+  const double* A = Ma + nm;
+  const double* C = A + na;
+  int a1, a2, m1, m2;
+  c81_interval(A, na, alpha, a1, a2);
+  c81_interval(Ma, nm, mach, m1, m2);
+  auto v = [&](int i, int j) { return C[(i - 1) + (size_t)na * (j - 1)]; };
+  if (a1 == a2) {
+    if (m1 == m2) return v(a1, m1);
+    return v(a1, m1) + ((mach - Ma[m1 - 1]) * (v(a1, m2) - v(a1, m1))) / (Ma[m2 - 1] - Ma[m1 - 1]);
+  }
+  if (m1 == m2) return v(a1, m1) + ((alpha - A[a1 - 1]) * (v(a2, m1) - v(a1, m1))) / (A[a2 - 1] - A[a1 - 1]);
+  const double y2m = Ma[m2 - 1] - mach, my1 = mach - Ma[m1 - 1];
+  const double lo = v(a1, m1) * y2m + v(a1, m2) * my1;
+  const double hi = v(a2, m1) * y2m + v(a2, m2) * my1;
+  const double num = (A[a2 - 1] - alpha) * lo + (alpha - A[a1 - 1]) * hi;
+  return num / (A[a2 - 1] - A[a1 - 1]) / (Ma[m2 - 1] - Ma[m1 - 1]);
+}
+
 __global__ void k_loads(Dims d, DevState s, const double* fr, int iter) {
   if (iter < 0) iter = s.devIter[0];
   const int nsec = d.nbC * d.ns;
@@ -1283,8 +1328,42 @@ __global__ void k_loads(Dims d, DevState s, const double* fr, int iter) {
     st3(s.secLiftDir + 3 * (size_t)t, fsign1(d.omega) * unit3(cross3(dd, yAF)));
   }
   __syncthreads();
+  // phase B with airfoil tables (forceCalcSwitch 1: blade_calc_force_alpha,
+  // src/classdef.f90:2091-2105, 2146-2195, 2234-2250): sectional angle of
+  // attack from the resultant velocity, CL and CD from the section's table
+  // at that angle and Mach number, lift along the lift direction, the
+  // inertial force along y x V with the sign of the section's circulation;
+  // the sectional drag stays zero (the reference never assigns it here) and
+  // the panel pressures and gamPrev are not computed.
+  for (int t = threadIdx.x; d.forceCalc == 1 && t < nsec; t += blockDim.x) {
+    const int b = t / d.ns, is = t % d.ns;
+    const double* sec = fr + d.fl.sec + ((size_t)b * d.ns + is) * kSec;
+    const d3 rv = ld3(s.secResVel + 3 * (size_t)t);
+    const double alpha = atan2(dot3(rv, ld3(sec + 3)), dot3(rv, ld3(sec)));
+    const double m = norm3(rv);
+    const double* T = s.c81 + s.c81Off[s.airfoilNo[t]];
+    const double aDeg = alpha * kRad2Deg, mach = m / d.velSound;
+    const double cl = c81_get(T, 0, aDeg, mach);
+    const double cd = c81_get(T, 1, aDeg, mach);
+    const double lead = ((0.5 * d.density) * (m * m)) * s.secArea[t];
+    const d3 liftDir = ld3(s.secLiftDir + 3 * (size_t)t);
+    const d3 sL = (liftDir * lead) * cl;
+    const d3 sLU = (liftDir * lead) * 0.0;
+    double gs = 0.0;
+    for (int ic = 0; ic < d.nc; ++ic) gs = gs + s.wGam[(size_t)b * d.npan + ic + d.nc * is];
+    const d3 yAF = ld3(fr + d.fl.ax + 9 * b + 3);
+    d3 fi = fsign1(gs) * unit3(cross3(yAF, rv));
+    fi = norm3(sL) * fi;
+    fi = fi + 0.0 * unit3(rv);
+    st3(s.secForceInertial + 3 * (size_t)t, fi);
+    st3(s.secLift + 3 * (size_t)t, sL);
+    st3(s.secLiftUnsteady + 3 * (size_t)t, sLU);
+    s.secCL[t] = cl;
+    s.secCD[t] = cd;
+    s.secCLu[t] = 0.0;
+  }
   // phase B: panel pressures and sectional forces (blade_calc_force)
-  for (int t = threadIdx.x; t < nsec; t += blockDim.x) {
+  for (int t = threadIdx.x; d.forceCalc != 1 && t < nsec; t += blockDim.x) {
     const int b = t / d.ns, is = t % d.ns;
     const d3 liftDir = ld3(s.secLiftDir + 3 * (size_t)t);
     d3 sFI = zero3(), sL = zero3(), sLU = zero3();

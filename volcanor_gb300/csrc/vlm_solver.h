@@ -55,6 +55,10 @@ struct Dims {
   int prescNt, prescGenNt;
   // wake burst (src/classdef.f90:2306-2339): skew limit, large core radius
   double skewLimit, chord;
+  // loads from airfoil tables (forceCalcSwitch 1) and the speed of sound
+  // their Mach number uses
+  int forceCalc;
+  double velSound;
   FrameLayout fl;
 };
 
@@ -64,6 +68,10 @@ constexpr int kPresc = 240;
 struct DevState {
   // wing (static)
   double *wRvc, *panArea, *panMeanChord, *panMeanSpan, *secArea;
+  // forceCalcSwitch 1: airfoil tables (AirfoilTables layout), their offsets,
+  // the table of every blade section
+  double* c81;
+  int *c81Off, *airfoilNo;
   // frames [(nt+1) * fl.size]
   double* frames;
   // wing dynamic

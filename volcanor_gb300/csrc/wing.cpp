@@ -344,7 +344,15 @@ void Wing::readGeom(const Namelist& g) {
     r.camberFile.push_back(g.s("CAMBERSECTIONS", "camberFile", "0", k));
   }
   if (r.ductSwitch != 0) throw std::runtime_error("unsupported: ductSwitch");
-  if (r.forceCalcSwitch != 0) throw std::runtime_error("unsupported: forceCalcSwitch != 0 (C81 tables)");
+  if (r.forceCalcSwitch < 0 || r.forceCalcSwitch > 1)
+    throw std::runtime_error("unsupported: forceCalcSwitch 2 (alpha from the sectional circulation)");
+  if (r.forceCalcSwitch > 0 && r.nAirfoils == 0) throw std::runtime_error("No. of airfoil tables set to 0 in geomXX.in");
+  for (int a = 0; a < r.nAirfoils; ++a) {
+    r.airfoilSectionLimit.push_back(g.d("AIRFOILS", "airfoilSectionLimit", 1.0, a));
+    r.airfoilFile.push_back(g.s("AIRFOILS", "airfoilFile", "0", a));
+  }
+  if (r.forceCalcSwitch == 1 && r.axisymmetrySwitch == 1)
+    throw std::runtime_error("unsupported: forceCalcSwitch 1 with axisymmetrySwitch 1");
   if (r.bladeDynamicsSwitch != 0 || r.bodyDynamicsSwitch != 0)
     throw std::runtime_error("unsupported: blade/body dynamics");
   if (r.customTrajectorySwitch != 0 && r.customTrajectorySwitch != 1)
@@ -800,6 +808,79 @@ void Wing::init() {
     nonDimDenom = ((0.5 * density) * ((r.radius * (1.0 - r.root_cut)) * r.chord)) * dot3(r.velBody, r.velBody);
   }
   omegaSlow = sw.slowStart > 0 ? 0.0 : r.Omega;
+  // airfoil tables and the table of every section (classdef.f90:3693-3725):
+  // the first table whose r/R limit reaches the section's CP, r/R measured
+  // along the blade's x axis from the root section's point at half chord
+  if (r.forceCalcSwitch == 1) {
+    for (const std::string& f : r.airfoilFile) {
+      if (f.empty() || f[0] == '0') throw std::runtime_error("forceCalcSwitch 1 needs every airfoilFile");
+      airfoils.add_c81(f[0] == '/' || baseDir.empty() ? f : baseDir + "/" + f);
+    }
+    airfoilOfSection.assign((size_t)r.nb * r.ns, 0);
+    for (int ib = 0; ib < r.nb; ++ib) {
+      const Blade& b = bl[ib];
+      if (r.nAirfoils == 1) continue;
+      const d3 root = b.w(0, 0).PC[3] * 0.5 + b.w(r.nc - 1, 0).PC[2] * 0.5;
+      for (int is = 0; is < r.ns; ++is) {
+        const double rr = std::fabs(dot3(b.secCP[is] - root, b.xA)) + r.root_cut;
+        if (rr > 1.0) throw std::runtime_error("r/R value is greater than 1 in airfoil selection");
+        int a = 0;
+        while (a < r.nAirfoils && !(r.airfoilSectionLimit[a] >= rr)) ++a;
+        airfoilOfSection[(size_t)ib * r.ns + is] = a < r.nAirfoils ? a : 0;
+      }
+    }
+  }
+}
+
+// A C81 file into the flat table (the layout of AirfoilTables).
+void AirfoilTables::add_c81(const std::string& path) {
+  std::ifstream in(path);
+  if (!in) throw std::runtime_error("cannot open " + path);
+  std::vector<std::string> lines;
+  for (std::string t; std::getline(in, t);) {
+    if (!t.empty() && t.back() == '\r') t.pop_back();
+    lines.push_back(t);
+  }
+  auto column = [](const std::string& t, size_t at, size_t width) {
+    const std::string f = at < t.size() ? t.substr(at, width) : std::string();
+    const size_t b = f.find_first_not_of(' ');
+    return b == std::string::npos ? 0.0 : std::strtod(f.c_str() + b, nullptr);
+  };
+  size_t ln = 0;
+  auto line = [&]() -> const std::string& {
+    if (ln >= lines.size()) throw std::runtime_error("C81 file too short: " + path);
+    return lines[ln++];
+  };
+  const std::string head = line();
+  int cnt[6];
+  for (int k = 0; k < 6; ++k) cnt[k] = (int)column(head, 30 + 2 * (size_t)k, 2);
+  offset.push_back((int)data.size());
+  for (int k = 0; k < 6; ++k) data.push_back(cnt[k]);
+  for (int c = 0; c < 3; ++c) {
+    const int nm = cnt[2 * c], na = cnt[2 * c + 1];
+    if (nm < 1 || nm > 18 || na < 1) throw std::runtime_error("C81 table sizes out of range: " + path);
+    std::vector<double> mach(nm), alpha(na), val((size_t)na * nm);
+    // a row of values: up to 9 after `skip` columns, the rest on a second line
+    auto values = [&](const std::string& first, double* out, size_t stride) {
+      for (int j = 0; j < nm; ++j) {
+        if (j == 9) {
+          const std::string& more = line();
+          for (int jj = 9; jj < nm; ++jj) out[(size_t)jj * stride] = column(more, 7 + 7 * (size_t)(jj - 9), 7);
+          break;
+        }
+        out[(size_t)j * stride] = column(first, 7 + 7 * (size_t)j, 7);
+      }
+    };
+    values(line(), mach.data(), 1);
+    for (int i = 0; i < na; ++i) {
+      const std::string& row = line();
+      alpha[i] = column(row, 0, 7);
+      values(row, val.data() + i, (size_t)na);
+    }
+    data.insert(data.end(), mach.begin(), mach.end());
+    data.insert(data.end(), alpha.begin(), alpha.end());
+    data.insert(data.end(), val.begin(), val.end());
+  }
 }
 
 void Wing::start_pitch() {

@@ -62,6 +62,10 @@ struct RotorParams {  // rotor_readGeom inputs (src/classdef.f90:2541-2767)
   // camber sections (CAMBERSECTIONS namelist, src/classdef.f90:2614-2687)
   std::vector<double> camberSectionLimit;
   std::vector<std::string> camberFile;
+  // forceCalcSwitch 1: one airfoil table per entry of the AIRFOILS namelist
+  // (classdef.f90:2605, 2754-2765), sections up to airfoilSectionLimit (r/R)
+  std::vector<double> airfoilSectionLimit;
+  std::vector<std::string> airfoilFile;
   // read only to be echoed into rXXParams.json
   int imagePlane = 0, imageRotorNum = 0, nAirfoils = 0;
   double thetaTwist = 0, Iflap = 0, cflap = 0, kflap = 0, MflapConstant = 0, alpha0 = 0;
@@ -85,6 +89,20 @@ struct Blade {
   double theta = 0, psi = 0, pivotLE = 0, flap = 0, dflap = 0;
   Panel& w(int i, int j) { return p[i + nc * j]; }
   const Panel& w(int i, int j) const { return p[i + nc * j]; }
+};
+
+// The airfoil tables of a rotor in one flat array of doubles, as the loads
+// kernel reads them: per airfoil, at offset[a], the counts ML NL MD ND MM NM
+// then for lift, drag and moment in turn the Mach numbers, the angles of
+// attack (degrees) and the coefficients (angle fastest).  Read from C81
+// files (fixed columns: a 30-character name and six 2-digit counts, then
+// per coefficient a line of Mach numbers in 7-column fields after 7 blank
+// columns, and per angle a line of the angle and the values in 7-column
+// fields; more than 9 Mach numbers continue on a second line).
+struct AirfoilTables {
+  std::vector<double> data;
+  std::vector<int> offset;
+  void add_c81(const std::string& path);
 };
 
 // One case: parsed inputs, derived sizes and the moving lifting surface.
@@ -114,6 +132,10 @@ class Wing {
   d3 hub, cg, shaftAxis, xBody, yBody, zBody;
   std::vector<Blade> bl;
   std::string baseDir;
+  // forceCalcSwitch 1: the tables and each blade section's 0-based table
+  // (blade-major), assigned at initialisation (classdef.f90:3693-3725)
+  AirfoilTables airfoils;
+  std::vector<int> airfoilOfSection;
   bool member = false;  // a rotor of coupled rotors: nr > 1 allowed
 
  private:
