@@ -343,9 +343,14 @@ int vlm_batch_last_step_ms(vlm_batch* b, double* ms);
  * rotors' wings (:549-561), the loads without every rotor's bound vortices
  * (:632-652), and the wake-node velocities from every rotor's wing and wake
  * (:808-827, 1052-1076) -- with each do-ir loop of the iteration run over the
- * rotors in turn.  Every rotor is a lifting surface with a wake
- * (surfaceType >= 0, nNwake > 0); image and non-lifting surfaces and
- * sub-iterations (ntSub, ntSubInit) give VLM_ERR_UNSUPPORTED.  Rotor ir > 0
+ * rotors in turn.  Every rotor is a lifting surface with a wake (nNwake > 0)
+ * or an image of an earlier one (surfaceType -1, imagePlane 1..3,
+ * imageRotorNum; ground effect): its parameters are the source's, its
+ * geometry mirrored at initialisation, and each step its circulation, velCP
+ * and wake are the source's mirrored (rotor_mirrorGamma/VelCP/Wake,
+ * src/classdef.f90:4990-5131, in the reference's places of the loop).
+ * Non-lifting surfaces and sub-iterations (ntSub, ntSubInit) give
+ * VLM_ERR_UNSUPPORTED.  Rotor ir > 0
  * is initialised with dt, nt and the switches as rotor ir - 1 left them
  * (rotor_init's intent(inout) arguments, src/classdef.f90:2778-3011).  opt
  * applies to every rotor; all rotors run on one stream; no graph replay.

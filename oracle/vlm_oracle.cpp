@@ -718,6 +718,10 @@ struct Sim {
   std::vector<Sim*> sys;
   int self = 0;
   bool member = false;  // created as a rotor of a system: nr > 1 allowed
+  // an image rotor (surfaceType -1): the rotor it mirrors, initialised first
+  // (its parameters, classdef.f90:2797-2910, and its initial normals)
+  const Sim* imageOf = nullptr;
+  static double& comp(V3& v, int k) { return k == 1 ? v.x : (k == 2 ? v.y : v.z); }
 
   // ---- blade kinematics -------------------------------------------------
   // classdef.f90:1092-1112
@@ -1975,6 +1979,8 @@ struct Sim {
       }
       std::vector<double> zv((size_t)(nc + 1) * (ns + 1), 0.0);  // [i + (nc+1) j]
       if (r.nCamberFiles > 0) zv = getCamber(xVec, yv);
+      if (imageOf && r.imagePlane == 3)  // classdef.f90:3228-3230
+        for (auto& v : zv) v = -1.0 * v;
       auto z = [&](int i, int j) { return zv[(size_t)i + (size_t)(nc + 1) * j]; };
       for (auto& b : r.blade)
         for (int j = 0; j < ns; ++j)
@@ -1990,6 +1996,8 @@ struct Sim {
       std::string path = r.geometryFile;
       if (path[0] != '/' && !baseDir.empty()) path = baseDir + "/" + path;
       auto g = readPlot3d(path, nx, ny);
+      if (imageOf && r.imagePlane == 3)  // classdef.f90:3989-3995
+        for (auto& q : g) q.z = -1.0 * q.z;
       for (int ib = 0; ib < r.nbConvect; ++ib)
         for (int is = 0; is < ns; ++is)
           for (int ic = 0; ic < nc; ++ic) {
@@ -2069,6 +2077,13 @@ struct Sim {
           p.calc_area();
           p.calc_mean_dimensions();
         }
+      if (imageOf)  // classdef.f90:3434-3443: the source's normals, mirrored
+        for (int j = 0; j < ns; ++j)
+          for (int i = 0; i < nc; ++i) {
+            V3 n = imageOf->R.blade[ib].w(i, j).nCap;
+            comp(n, r.imagePlane) = -1.0 * comp(n, r.imagePlane);
+            b.w(i, j).nCap = n;
+          }
       for (int is = 0; is < ns; ++is) {
         double s = 0.0;
         for (int ic = 0; ic < nc; ++ic) s = s + b.w(ic, is).panelArea;
@@ -2202,11 +2217,19 @@ struct Sim {
   void startGeometry() {
     for (int ib = 0; ib < R.nb; ++ib) {
       Blade& b = R.blade[ib];
-      b.theta = gettheta(R.psiStart, ib + 1);
+      if (imageOf) {
+        // an image takes its source's pitch, negated in the z plane
+        b.theta = imageOf->R.blade[ib].theta;
+        if (R.imagePlane == 3) b.theta = -1.0 * b.theta;
+      } else {
+        b.theta = gettheta(R.psiStart, ib + 1);
+      }
       blade_rot_pitch(b, fsign(1.0, R.Omega) * b.theta);
     }
-    calcAIC();
-    if (!isInverse(R.AIC, R.AIC_inv, R.n())) throw std::runtime_error("Computed AIC_inv does not seem to be correct");
+    if (!imageOf) {
+      calcAIC();
+      if (!isInverse(R.AIC, R.AIC_inv, R.n())) throw std::runtime_error("Computed AIC_inv does not seem to be correct");
+    }
     R.omegaSlow = sw.slowStart > 0 ? 0.0 : R.Omega;
     t = 0.0;
     iter = 0;
@@ -2345,6 +2368,70 @@ struct Sim {
       for (size_t k = 0; k < b.velF.size(); ++k) f(b.velF[k], b.velF1[k], b.velF2[k], b.velF3[k], b.velFP[k], b.velFStep[k]);
     }
   }
+  // ---- image rotors (classdef.f90:4990-5131) ----------------------------------
+  // rotor_mirrorVelCP: velCP and velCPm of the source, the image-plane
+  // component negated
+  void mirrorVelCP() {
+    const int pl = R.imagePlane;
+    for (int ib = 0; ib < R.nb; ++ib)
+      for (size_t k = 0; k < R.blade[ib].wiP.size(); ++k) {
+        WingPanel& p = R.blade[ib].wiP[k];
+        const WingPanel& q = imageOf->R.blade[ib].wiP[k];
+        p.velCP = q.velCP;
+        p.velCPm = q.velCPm;
+        comp(p.velCP, pl) = -1.0 * comp(p.velCP, pl);
+        comp(p.velCPm, pl) = -1.0 * comp(p.velCPm, pl);
+      }
+  }
+  // rotor_mirrorGamma (after gamVecPrev = gamVec, main.f90:594-600) + map_gam
+  void mirrorGamma() {
+    R.gamVecPrev = R.gamVec;
+    for (size_t i = 0; i < R.gamVec.size(); ++i) R.gamVec[i] = -1.0 * imageOf->R.gamVec[i];
+    map_gam();
+  }
+  // rotor_mirrorWake: mode 'C' the active current wake, 'P' the active
+  // predicted wake, 'A' every row of the current wake; whole ring / filament
+  // objects copied, then their node coordinates in the image plane and their
+  // circulation negated (vr_mirror, Fwake_mirror: classdef.f90:722-735, 982-993)
+  void mirrorWake(char mode) {
+    const int pl = R.imagePlane, NW = R.nNwake, NF = R.nFwake;
+    const int r0 = mode == 'A' ? 0 : R.rowNear - 1, f0 = mode == 'A' ? 0 : R.rowFar - 1;
+    for (int ib = 0; ib < R.nb; ++ib) {
+      Blade& b = R.blade[ib];
+      const Blade& q = imageOf->R.blade[ib];
+      std::vector<VR>& wn = mode == 'P' ? b.waNP : b.waN;
+      const std::vector<VR>& qn = mode == 'P' ? q.waNP : q.waN;
+      std::vector<FW>& wf = mode == 'P' ? b.waFP : b.waF;
+      const std::vector<FW>& qf = mode == 'P' ? q.waFP : q.waF;
+      for (int j = 0; j < b.ns; ++j)
+        for (int i = r0; i < NW; ++i) {
+          VR& v = wn[i + NW * j];
+          v = qn[i + NW * j];
+          for (auto& f : v.vf) {
+            comp(f.fc1, pl) = -1.0 * comp(f.fc1, pl);
+            comp(f.fc2, pl) = -1.0 * comp(f.fc2, pl);
+          }
+          v.gam = -1.0 * v.gam;
+        }
+      for (int i = f0; i < NF; ++i) {
+        FW& f = wf[i];
+        f = qf[i];
+        comp(f.vf.fc1, pl) = -1.0 * comp(f.vf.fc1, pl);
+        comp(f.vf.fc2, pl) = -1.0 * comp(f.vf.fc2, pl);
+        f.gam = -1.0 * f.gam;
+      }
+    }
+  }
+  // the wake update of an image (main.f90:844-1439): no velocities; the
+  // source's wake mirrored where the source convects
+  void imageWakeStage(int st) {
+    if (st == 1) mirrorWake(predicts() ? 'P' : 'C');
+    else if (st == 3) {
+      if (predicts()) mirrorWake('C');
+      mirrorWake('A');
+    }
+  }
+
   // main.f90:799-1439, run as four stages so that a system of rotors runs
   // each stage for every rotor before the next (the reference's do-ir loops):
   // 0 the node velocities, 1 the scheme up to the predicted wake, 2 the
@@ -2520,9 +2607,34 @@ struct System {
       }
       Namelist g;
       g.parse(geoms[ir]);
-      s->readGeom(g);
-      if (s->R.surfaceType < 0 || std::abs(s->R.surfaceType) == 2)
-        throw std::runtime_error("system: image and non-lifting surfaces are not supported");
+      const int st = g.i("SURFACE", "surfaceType");
+      if (std::abs(st) == 2) throw std::runtime_error("system: non-lifting surfaces are not supported");
+      if (st < 0) {
+        // an image: its source's parameters (classdef.f90:2797-2910) with its
+        // own surface entries and geometry file, hub and cg mirrored
+        const int src = g.i("SURFACE", "imageRotorNum");
+        if (src < 1 || src > ir || r[src - 1]->imageOf)
+          throw std::runtime_error("system: an image rotor must mirror an earlier lifting rotor");
+        Namelist gs;
+        gs.parse(geoms[src - 1]);
+        s->readGeom(gs);
+        s->R.surfaceType = st;
+        s->R.imagePlane = g.i("SURFACE", "imagePlane");
+        s->R.imageRotorNum = src;
+        s->R.geometryFile = g.s("PANELS", "geometryFile", "0");
+        if (s->R.imagePlane < 1 || s->R.imagePlane > 3) throw std::runtime_error("imagePlane must be 1, 2 or 3");
+        const Rotor& q = r[src - 1]->R;
+        if (q.customTrajectorySwitch != 0 || q.prescWakeAfterTruncNt > 0)
+          throw std::runtime_error("system: images of rotors with custom trajectories or prescribed wakes");
+        s->imageOf = r[src - 1].get();
+        s->R.hubCoords = q.hubCoords;
+        s->R.cgCoords = q.cgCoords;
+        s->R.fromCoords = q.fromCoords;
+        comp(s->R.hubCoords, s->R.imagePlane) = -1.0 * comp(s->R.hubCoords, s->R.imagePlane);
+        comp(s->R.cgCoords, s->R.imagePlane) = -1.0 * comp(s->R.cgCoords, s->R.imagePlane);
+      } else {
+        s->readGeom(g);
+      }
       s->init();
       r.push_back(std::move(s));
     }
@@ -2534,10 +2646,17 @@ struct System {
     }
   }
   const Switches& sw() const { return r[0]->sw; }
+  static double& comp(V3& v, int k) { return Sim::comp(v, k); }
   void start() {
     for (auto& s : r) s->startGeometry();
-    for (auto& s : r) s->computeRHS(false);
-    for (auto& s : r) s->solveRHS();
+    for (auto& s : r) {
+      if (s->imageOf) s->mirrorVelCP();
+      else s->computeRHS(false);
+    }
+    for (auto& s : r) {
+      if (s->imageOf) s->mirrorGamma();
+      else s->solveRHS();
+    }
     for (auto& s : r) s->startWake();
     for (auto& s : r) s->startLoads();
     for (auto& s : r) s->started = true;
@@ -2547,8 +2666,14 @@ struct System {
     if (r[0]->iter >= r[0]->nt) throw std::runtime_error("all timesteps done");
     for (auto& s : r) s->advanceKinematics();
     for (auto& s : r) s->preWake();
-    for (auto& s : r) s->computeRHS(true);
-    for (auto& s : r) s->solveRHS();
+    for (auto& s : r) {
+      if (s->imageOf) s->mirrorVelCP();
+      else s->computeRHS(true);
+    }
+    for (auto& s : r) {
+      if (s->imageOf) s->mirrorGamma();
+      else s->solveRHS();
+    }
     if (sw().rotorForcePlot != 0 && r[0]->iter % sw().rotorForcePlot == 0)
       for (auto& s : r) {
         s->computeForces();
@@ -2557,7 +2682,10 @@ struct System {
     if (sw().wakeSuppress == 0)
       for (int st = 0; st < 4; ++st)
         for (auto& s : r)
-          if (s->R.nNwake > 0) s->wakeStage(st);
+          if (s->R.nNwake > 0) {
+            if (s->imageOf) s->imageWakeStage(st);
+            else s->wakeStage(st);
+          }
   }
 };
 

@@ -126,3 +126,27 @@ def test_case_directory_and_rotor_handles(tmp_path):
 
 
 STATE = 7  # VLM_ERR_STATE (include/vlm.h)
+
+
+@pytest.mark.parametrize("fd,nt", [(3, 40), (1, 16), (0, 16)])
+def test_ground_effect_image_rotor_fp64_bitwise(fd, nt):
+    """A hover rotor 0.6 R above the ground and its image (surfaceType -1,
+    imagePlane 3): the image's circulation, velCP and wake mirror the
+    rotor's; every rotor's state and loads are the oracle's bit for bit."""
+    sc = C.rotor_ground_effect(height=0.6, nt=nt, fd_scheme=fd)
+    o = oracle_system(sc, nt)
+    g, rows = gpu_system(sc, nt)
+    for ir in range(2):
+        assert_same_state(g.rotors[ir], o.rotors[ir], 2)
+    np.testing.assert_array_equal(g.rotors[1].get("gamVec"), -g.rotors[0].get("gamVec"))
+    wa, wb = g.rotors[0].get("waN", 1).reshape(-1, 3), g.rotors[1].get("waN", 1).reshape(-1, 3)
+    np.testing.assert_array_equal(wb[:, :2], wa[:, :2])
+    np.testing.assert_array_equal(wb[:, 2], -wa[:, 2])
+
+
+def test_ground_effect_fp32_within_ct_tolerance():
+    sc = C.rotor_ground_effect(height=0.6, nt=40)
+    _, r64 = gpu_system(sc, 40)
+    _, r32 = gpu_system(sc, 40, precision=lib.PREC_FP32_NEAR64)
+    rel = np.abs(r32[:, 0, 1] - r64[:, 0, 1]) / np.abs(r64[:, 0, 1])
+    assert rel.max() < 1e-4, rel.max()

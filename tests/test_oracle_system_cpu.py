@@ -51,3 +51,26 @@ def test_system_input_checks():
         assert "system" in str(e)
     else:
         raise AssertionError("nr = 2 accepted by a lone rotor")
+
+
+def test_ground_effect_image_rotor():
+    """A hover rotor at h = 0.5 R and its image in the ground plane
+    (surfaceType -1, imagePlane 3): the image's circulation and wake are the
+    exact mirror of the rotor's, and the ground raises its thrust against the
+    same rotor in free air, less so higher up."""
+    O.set_threads(4)
+    gains = []
+    for h in (0.5, 1.5):
+        sc = C.rotor_ground_effect(height=h, nt=30, n_nwake=12, truncate_nt=18)
+        y = O.System(sc.config, sc.geoms)
+        y.start()
+        y.step(30)
+        a, b = y.rotors
+        assert np.array_equal(b.get("gamVec"), -a.get("gamVec"))
+        wa, wb = a.get("waN", 1).reshape(-1, 3), b.get("waN", 1).reshape(-1, 3)
+        assert np.array_equal(wb[:, :2], wa[:, :2]) and np.array_equal(wb[:, 2], -wa[:, 2])
+        iso = O.Sim(sc.config.replace("nr = 2", "nr = 1"), sc.geoms[0])
+        iso.start()
+        iso.step(30)
+        gains.append(a.ct_hist()[-5:, 1].mean() / iso.ct_hist()[-5:, 1].mean() - 1.0)
+    assert gains[0] > gains[1] > 0.0

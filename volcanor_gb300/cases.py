@@ -204,6 +204,17 @@ def rotor_pair(nt: int = 60, ns: int = 8, n_nwake: int = 24, truncate_nt: int = 
     return SystemCase("rotor_pair", cfg, [g1, g2])
 
 
+def rotor_ground_effect(height: float = 0.6, nt: int = 60, ns: int = 8, n_nwake: int = 24, truncate_nt: int = 30,
+                        fd_scheme: int = 3) -> SystemCase:
+    """A 2-blade hover rotor (as rotor_pair's) with its hub `height` above the
+    ground plane z = 0, and its image below it: rotor 2 is surfaceType -1,
+    imagePlane 3, mirroring rotor 1 (the reference's ground-effect setup)."""
+    sc = rotor_pair(nt=nt, ns=ns, n_nwake=n_nwake, truncate_nt=truncate_nt, hub1=(0.0, 0.0, height),
+                    hub2=(0.0, 0.0, -height), omega2=100.0, fd_scheme=fd_scheme)
+    img = geom_text(surfaceType=-1, imagePlane=3, imageRotorNum=1, nb=2, nc=1, ns=ns, nNwake=n_nwake)
+    return SystemCase("rotor_ground_effect", sc.config, [sc.geoms[0], img])
+
+
 def wing_ar4(nt: int = 200, fd_scheme: int = 1, n_nwake: Optional[int] = None) -> Case:
     """Flat wing, c = 1 m, AR 4, 4 x 13 rings, alpha 5 deg, V = 10 m/s, dt = c/(4V)."""
     cfg = config_text(nt=nt, dt=0.025, density=1.0, fdScheme=fd_scheme, wakeDissipation=0)

@@ -183,15 +183,19 @@ struct Case {
   int prescRecords(int rowFar) const { return d.prescNt > 0 && rowFar <= d.NF ? kPresc : 0; }
 
   void create(const std::string& cfg, const std::string& geo, const std::string& base, const vlm_options* o,
-              const Case* prevRotor = nullptr, bool asMember = false, cudaStream_t sharedStream = nullptr) {
+              const Case* prevRotor = nullptr, bool asMember = false, cudaStream_t sharedStream = nullptr,
+              const Case* imageSource = nullptr) {
     vlm_default_options(&opt);
+    geomText = geo;
+    imgSrc = imageSource;
     if (o) opt = *o;
     if (opt.precision < 0 || opt.precision > 2) throw StatusError(VLM_ERR_INVALID, "precision must be 0, 1 or 2");
     if (opt.solve_mode < -1 || opt.solve_mode > 1) throw StatusError(VLM_ERR_INVALID, "solve_mode must be -1, 0 or 1");
     refine = opt.solve_mode == 1 || (opt.solve_mode == -1 && opt.precision != VLM_PREC_FP64);
     chunk64 = opt.sum_chunk;
     member = asMember;
-    if (member) W.loadMember(cfg, geo, base, prevRotor ? &prevRotor->W : nullptr);
+    if (imgSrc) W.loadImage(cfg, geo, imgSrc->geomText, base, prevRotor ? &prevRotor->W : nullptr, &imgSrc->W);
+    else if (member) W.loadMember(cfg, geo, base, prevRotor ? &prevRotor->W : nullptr);
     else W.load(cfg, geo, base);
     const RotorParams& P = W.P;
     d.nb = P.nb;
@@ -779,6 +783,8 @@ struct Case {
   bool member = false;
   int self = 0;
   std::vector<Case*> sys;
+  std::string geomText;          // this rotor's geomXX.nml (an image of it reads its parameters)
+  const Case* imgSrc = nullptr;  // an image rotor (surfaceType -1): the rotor it mirrors
   struct SysSeg {
     int jr = 0, lgoff = 0, lng = 0, nrec = 0, recOff = 0;  // source rotor, its local groups, records, offset
   };
@@ -908,6 +914,23 @@ struct Case {
     sysGather(se, k, false, k);
     evaluate(se.e, Mcp, 3, nullptr, sysOut, -1, se.nterms);
     launch_rhs_terms(d, s, frame(k), sysOut, se.nterms, stream);
+  }
+  // an image rotor's place in the RHS and solve loops (src/main.f90:584-598)
+  void imageMirrorVelCP() { launch_mirror_velcp(d, s, imgSrc->s.velCP, W.P.imagePlane, stream); }
+  void imageMirrorGamma() { launch_mirror_gamma(d, s, imgSrc->s.gamVec, stream); }
+  // an image rotor's wake update (src/main.f90:844-1439): no velocities; the
+  // source's wake mirrored where the source convects (its predicted wake at
+  // the predictor, its current wake at the corrector), then every row at the
+  // end of the step
+  void imageWakeStage(int k, int st) {
+    const StepPlan& pl = plans[k];
+    const int plane = W.P.imagePlane;
+    if (st == 1) {
+      launch_mirror_wake(d, s, imgSrc->s, predicts(k) ? 1 : 0, pl.rowNear, pl.rowFar, plane, stream);
+    } else if (st == 3) {
+      if (predicts(k)) launch_mirror_wake(d, s, imgSrc->s, 0, pl.rowNear, pl.rowFar, plane, stream);
+      launch_mirror_wake(d, s, imgSrc->s, 2, pl.rowNear, pl.rowFar, plane, stream);
+    }
   }
   // the loads with every rotor's bound vortices (src/main.f90:632-652)
   void sysLoads(int k) {
@@ -2110,8 +2133,18 @@ struct vlm_system {
     const int nr = (int)geoms.size();
     if (nr < 1) throw StatusError(VLM_ERR_INVALID, "a system needs at least one rotor");
     for (int ir = 0; ir < nr; ++ir) {
+      Namelist g;
+      g.parse(geoms[ir]);
+      const int st = g.i("SURFACE", "surfaceType");
+      const Case* src = nullptr;
+      if (st < 0) {
+        const int sr = g.i("SURFACE", "imageRotorNum");
+        if (sr < 1 || sr > ir || rotor(sr - 1).imgSrc)
+          throw StatusError(VLM_ERR_UNSUPPORTED, "unsupported: an image rotor must mirror an earlier lifting rotor");
+        src = &rotor(sr - 1);
+      }
       auto c = std::make_unique<vlm_case>();
-      c->c.create(cfg, geoms[ir], base, o, ir ? &rotor(ir - 1) : nullptr, true, ir ? stream() : nullptr);
+      c->c.create(cfg, geoms[ir], base, o, ir ? &rotor(ir - 1) : nullptr, true, ir ? stream() : nullptr, src);
       if (c->c.W.nr != nr)
         throw StatusError(VLM_ERR_INVALID, "config.nml nr = " + std::to_string(c->c.W.nr) + " but " +
                                                std::to_string(nr) + " rotor geometries");
@@ -2131,10 +2164,17 @@ struct vlm_system {
   // rotors' wings, the first shed row and the loads of iteration 0
   void start() {
     if (started) throw StatusError(VLM_ERR_STATE, "system already started");
-    for (auto& c : r) c->c.aicFactor();
+    for (auto& c : r)
+      if (!c->c.imgSrc) c->c.aicFactor();
     cudaStream_t st = stream();
-    for (auto& c : r) c->c.sysRhsPhase(0);
-    for (auto& c : r) launch_solve_only(c->c.d, c->c.s, st);
+    for (auto& c : r) {
+      if (c->c.imgSrc) c->c.imageMirrorVelCP();
+      else c->c.sysRhsPhase(0);
+    }
+    for (auto& c : r) {
+      if (c->c.imgSrc) c->c.imageMirrorGamma();
+      else launch_solve_only(c->c.d, c->c.s, st);
+    }
     for (auto& c : r) launch_shed(c->c.d, c->c.s, c->c.frame(0), c->c.d.NW + 1, false, st);
     if (rotor(0).W.sw.rotorForcePlot != 0)
       for (auto& c : r) c->c.sysLoads(0);
@@ -2160,13 +2200,22 @@ struct vlm_system {
     VLM_CUDA(cudaEventRecord(c0.ev0, st));
     for (int k = iter + 1; k <= iter + nsteps; ++k) {
       for (auto& c : r) c->c.prePhase(k);
-      for (auto& c : r) c->c.sysRhsPhase(k);
-      for (auto& c : r) launch_solve_only(c->c.d, c->c.s, st);
+      for (auto& c : r) {
+        if (c->c.imgSrc) c->c.imageMirrorVelCP();
+        else c->c.sysRhsPhase(k);
+      }
+      for (auto& c : r) {
+        if (c->c.imgSrc) c->c.imageMirrorGamma();
+        else launch_solve_only(c->c.d, c->c.s, st);
+      }
       if (sw.rotorForcePlot != 0 && k % sw.rotorForcePlot == 0)
         for (auto& c : r) c->c.sysLoads(k);
       if (sw.wakeSuppress == 0)
         for (int stg = 0; stg < 4; ++stg)
-          for (auto& c : r) c->c.wakeStage(k, stg);
+          for (auto& c : r) {
+            if (c->c.imgSrc) c->c.imageWakeStage(k, stg);
+            else c->c.wakeStage(k, stg);
+          }
     }
     VLM_CUDA(cudaEventRecord(c0.ev1, st));
     VLM_CUDA(cudaGetLastError());

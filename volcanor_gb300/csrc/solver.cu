@@ -1151,6 +1151,70 @@ __global__ void k_bound_foreign(Dims dt, const double* frt, Dims ds, DevState ss
   st3(out + 3 * (size_t)t, bound);
 }
 
+// ---- image rotors (src/classdef.f90:4990-5131) ------------------------------
+// rotor_mirrorVelCP: the source's velCP with the image-plane component negated
+__global__ void k_mirror_velcp(Dims d, DevState s, const double* __restrict__ src, int plane) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.nb * d.npan) return;
+  for (int c = 0; c < 3; ++c) {
+    const double v = src[3 * (size_t)t + c];
+    s.velCP[3 * (size_t)t + c] = c == plane - 1 ? -1.0 * v : v;
+  }
+}
+// gamVecPrev = gamVec, rotor_mirrorGamma (gamVec = -source gamVec), map_gam
+__global__ void k_mirror_gamma(Dims d, DevState s, const double* __restrict__ src) {
+  for (int i = threadIdx.x; i < d.n; i += blockDim.x) {
+    s.gamVecPrev[i] = s.gamVec[i];
+    s.gamVec[i] = -1.0 * src[i];
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < d.nbC * d.npan; r += blockDim.x) s.wGam[r] = s.gamVec[r];
+  __syncthreads();
+  if (d.axisym)
+    for (int r = d.npan + threadIdx.x; r < d.nb * d.npan; r += blockDim.x) s.wGam[r] = s.wGam[r % d.npan];
+}
+// rotor_mirrorWake: mode 0 the active current wake, 1 the active predicted
+// wake (node positions; the predicted wake's circulation and cores are the
+// current ones, which already mirror the source's), 2 every row of the
+// current wake; node coordinates in the image plane and circulation negated
+// (vr_mirror, Fwake_mirror: src/classdef.f90:722-735, 982-993)
+__global__ void k_mirror_wake(Dims d, DevState dst, DevState src, int mode, int rowNear, int rowFar, int plane) {
+  const int r0 = mode == 2 ? 0 : rowNear - 1, f0 = mode == 2 ? 0 : rowFar - 1;
+  const long nNear = (long)d.nb * (d.NW - r0) * d.ns;
+  const long nFar = d.NF - f0 > 0 ? (long)d.nb * (d.NF - f0) : 0;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int k0 = plane - 1;
+  if (t < nNear) {
+    const int rows = d.NW - r0;
+    const int b = (int)(t / ((long)rows * d.ns)), rem = (int)(t % ((long)rows * d.ns));
+    const int j = rem / rows, i = r0 + rem % rows;
+    const size_t idx = ringI(d, b, i, j);
+    const double* sc = (mode == 1 ? src.nCP : src.nC) + 12 * idx;
+    double* dc = (mode == 1 ? dst.nCP : dst.nC) + 12 * idx;
+    for (int k = 0; k < 12; ++k) dc[k] = k % 3 == k0 ? -1.0 * sc[k] : sc[k];
+    if (mode != 1) {
+      dst.nGam[idx] = -1.0 * src.nGam[idx];
+      for (int q = 0; q < 4; ++q) dst.nRvc[4 * idx + q] = src.nRvc[4 * idx + q];
+      dst.nAge[idx] = src.nAge[idx];
+    }
+  } else if (t < nNear + nFar) {
+    const long u = t - nNear;
+    const int b = (int)(u / (d.NF - f0)), i = f0 + (int)(u % (d.NF - f0));
+    const size_t f = (size_t)b * d.NF + i;
+    const double* sc = (mode == 1 ? src.fCP : src.fC) + 6 * f;
+    double* dc = (mode == 1 ? dst.fCP : dst.fC) + 6 * f;
+    for (int k = 0; k < 6; ++k) dc[k] = k % 3 == k0 ? -1.0 * sc[k] : sc[k];
+    if (mode != 1) {
+      dst.fGam[f] = -1.0 * src.fGam[f];
+      dst.fRvc[f] = src.fRvc[f];
+      dst.fRvc0[f] = src.fRvc0[f];
+      dst.fL0[f] = src.fL0[f];
+      dst.fLc[f] = src.fLc[f];
+      dst.fAge[f] = src.fAge[f];
+    }
+  }
+}
+
 // velCP = kinematic velocity + each term in turn (coupled rotors:
 // src/main.f90:549-561, the wake of every rotor and the wing of the others,
 // one per-rotor sum per term); RHS = velCP . nCap
@@ -1639,6 +1703,22 @@ void launch_rhs_terms(const Dims& d, const DevState& s, const double* frame, con
                       cudaStream_t st) {
   count_launch();
   k_rhs_terms<<<nblk(d.nbC * d.npan, 128), 128, 0, st>>>(d, s, frame, terms, nterms, d.nbC * d.npan);
+}
+void launch_mirror_velcp(const Dims& d, const DevState& s, const double* srcVelCP, int plane, cudaStream_t st) {
+  count_launch();
+  k_mirror_velcp<<<nblk(d.nb * d.npan, 128), 128, 0, st>>>(d, s, srcVelCP, plane);
+}
+void launch_mirror_gamma(const Dims& d, const DevState& s, const double* srcGamVec, cudaStream_t st) {
+  count_launch();
+  k_mirror_gamma<<<1, 1024, 0, st>>>(d, s, srcGamVec);
+}
+void launch_mirror_wake(const Dims& d, const DevState& dst, const DevState& src, int mode, int rowNear, int rowFar,
+                        int plane, cudaStream_t st) {
+  const int r0 = mode == 2 ? 0 : rowNear - 1, f0 = mode == 2 ? 0 : rowFar - 1;
+  const long n = (long)d.nb * (d.NW - r0) * d.ns + (d.NF - f0 > 0 ? (long)d.nb * (d.NF - f0) : 0);
+  if (n <= 0) return;
+  count_launch();
+  k_mirror_wake<<<nblk(n, 256), 256, 0, st>>>(d, dst, src, mode, rowNear, rowFar, plane);
 }
 void launch_solve_only(const Dims& d, const DevState& s, cudaStream_t st) {
   count_launch();

@@ -185,6 +185,13 @@ void launch_loads(const Dims& d, const DevState& s, const double* frame, int sum
 void launch_rhs_terms(const Dims& d, const DevState& s, const double* frame, const double* terms, int nterms,
                       cudaStream_t st);
 void launch_solve_only(const Dims& d, const DevState& s, cudaStream_t st);
+// Image rotors (src/classdef.f90:4990-5131): velCP and the circulation of the
+// source mirrored; its wake mirrored (mode 0 the active current wake, 1 the
+// active predicted wake, 2 every row of the current wake; d, rows of the image)
+void launch_mirror_velcp(const Dims& d, const DevState& s, const double* srcVelCP, int plane, cudaStream_t st);
+void launch_mirror_gamma(const Dims& d, const DevState& s, const double* srcGamVec, cudaStream_t st);
+void launch_mirror_wake(const Dims& d, const DevState& dst, const DevState& src, int mode, int rowNear, int rowFar,
+                        int plane, cudaStream_t st);
 void launch_bound_foreign(const Dims& dt, const double* frameT, const Dims& ds, const DevState& ss,
                           const double* frameS, double* out, cudaStream_t st);
 

@@ -231,6 +231,42 @@ void Wing::loadMember(const std::string& configText, const std::string& geomText
   init();
 }
 
+void Wing::loadImage(const std::string& configText, const std::string& imageGeomText,
+                     const std::string& sourceGeomText, const std::string& base, const Wing* prev, const Wing* src) {
+  baseDir = base;
+  member = true;
+  imageOf = src;
+  Namelist c, gi, gs;
+  c.parse(configText);
+  gi.parse(imageGeomText);
+  gs.parse(sourceGeomText);
+  readConfig(c);
+  if (prev) {
+    dt = prev->dt;
+    nt = prev->nt;
+    sw = prev->sw;
+  }
+  readGeom(gs);
+  RotorParams& r = P;
+  r.surfaceType = gi.i("SURFACE", "surfaceType");
+  r.imagePlane = gi.i("SURFACE", "imagePlane");
+  r.imageRotorNum = gi.i("SURFACE", "imageRotorNum");
+  r.geometryFile = gi.s("PANELS", "geometryFile", "0");
+  if (r.surfaceType != -1) throw std::runtime_error("unsupported: image of a non-lifting surface");
+  if (r.imagePlane < 1 || r.imagePlane > 3) throw std::runtime_error("imagePlane must be 1, 2 or 3");
+  if (src->P.customTrajectorySwitch != 0 || src->P.prescWakeNt > 0 || src->P.forceCalcSwitch != 0)
+    throw std::runtime_error("unsupported: an image of a rotor with a custom trajectory, a prescribed wake or airfoil "
+                             "tables");
+  auto mir = [&](d3 v) {
+    (r.imagePlane == 1 ? v.x : (r.imagePlane == 2 ? v.y : v.z)) *= -1.0;
+    return v;
+  };
+  r.hubCoords = mir(src->initHub);
+  r.cgCoords = mir(src->initCg);
+  r.fromCoords = src->P.fromCoords;
+  init();
+}
+
 // src/libCommon.f90:51-108
 void Wing::readConfig(const Namelist& c) {
   const std::string ver = c.s("VERSION", "fileFormatVersion", "");
@@ -636,6 +672,8 @@ void Wing::init() {
     const auto yv = spacing(r.spanSpacing, r.root_cut * r.radius, r.radius, ns + 1);
     std::vector<double> zv((size_t)(nc + 1) * (ns + 1), 0.0);  // [i + (nc+1) j]
     if (r.nCamberFiles > 0) zv = getCamber(xv, yv);
+    if (imageOf && r.imagePlane == 3)
+      for (auto& v : zv) v = -1.0 * v;
     auto z = [&](int i, int j) { return zv[(size_t)i + (size_t)(nc + 1) * j]; };
     for (auto& b : bl)
       for (int j = 0; j < ns; ++j)
@@ -664,6 +702,8 @@ void Wing::init() {
           d3& q = grid[i + (size_t)nx * j];
           (c == 0 ? q.x : (c == 1 ? q.y : q.z)) = v;
         }
+    if (imageOf && r.imagePlane == 3)
+      for (auto& q : grid) q.z = -1.0 * q.z;
     for (int ib = 0; ib < nbConvect; ++ib)
       for (int is = 0; is < ns; ++is)
         for (int ic = 0; ic < nc; ++ic) {
@@ -740,6 +780,12 @@ void Wing::init() {
         p.meanSpan = 0.5 * (norm3(p.PC[3] - p.PC[0]) + norm3(p.PC[2] - p.PC[1]));
         p.meanChord = 0.5 * (norm3(p.PC[1] - p.PC[0]) + norm3(p.PC[2] - p.PC[3]));
       }
+    if (imageOf)
+      for (size_t k = 0; k < b.p.size(); ++k) {
+        d3 n = imageOf->initNCap[ib][k];
+        (r.imagePlane == 1 ? n.x : (r.imagePlane == 2 ? n.y : n.z)) *= -1.0;
+        b.p[k].nCap = n;
+      }
     for (int is = 0; is < ns; ++is) {
       double s = 0.0;
       for (int ic = 0; ic < nc; ++ic) s = s + b.w(ic, is).area;
@@ -808,6 +854,11 @@ void Wing::init() {
     nonDimDenom = ((0.5 * density) * ((r.radius * (1.0 - r.root_cut)) * r.chord)) * dot3(r.velBody, r.velBody);
   }
   omegaSlow = sw.slowStart > 0 ? 0.0 : r.Omega;
+  initHub = hub;
+  initCg = cg;
+  initNCap.assign(r.nb, {});
+  for (int ib = 0; ib < r.nb; ++ib)
+    for (const Panel& q : bl[ib].p) initNCap[ib].push_back(q.nCap);
   // airfoil tables and the table of every section (classdef.f90:3693-3725):
   // the first table whose r/R limit reaches the section's CP, r/R measured
   // along the blade's x axis from the root section's point at half chord
@@ -886,7 +937,13 @@ void AirfoilTables::add_c81(const std::string& path) {
 void Wing::start_pitch() {
   for (int ib = 0; ib < P.nb; ++ib) {
     Blade& b = bl[ib];
-    b.theta = gettheta(P.psiStart, ib + 1);
+    if (imageOf) {
+      // src/main.f90:45-50: the source's initial pitch, negated in the z plane
+      b.theta = imageOf->gettheta(imageOf->P.psiStart, ib + 1);
+      if (P.imagePlane == 3) b.theta = -1.0 * b.theta;
+    } else {
+      b.theta = gettheta(P.psiStart, ib + 1);
+    }
     blade_rot_pitch(b, fsign1(P.Omega) * b.theta);
   }
   if (P.customTrajectorySwitch == 1) {  // src/main.f90:111-116, before the initial solve

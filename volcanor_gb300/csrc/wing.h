@@ -116,6 +116,15 @@ class Wing {
   // rotor ir - 1 left (prev; null for the first rotor).
   void loadMember(const std::string& configText, const std::string& geomText, const std::string& baseDir,
                   const Wing* prev);
+  // An image rotor (surfaceType -1) of rotor `src` (initialised before it):
+  // the reference copies every parameter from the source except the image's
+  // surfaceType, imagePlane, imageRotorNum and geometryFile, mirrors hub and
+  // cg in the image plane, z-mirrors the geometry for imagePlane 3 and takes
+  // the source's initial normals mirrored (src/classdef.f90:2797-2910,
+  // 3228-3230, 3434-3443, 3989-3995); the source's geomXX.nml text supplies
+  // the shared parameters.
+  void loadImage(const std::string& configText, const std::string& imageGeomText, const std::string& sourceGeomText,
+                 const std::string& baseDir, const Wing* prev, const Wing* src);
   void start_pitch();                  // src/main.f90:43-58
   void advance(int iter);              // src/main.f90:412-463 kinematics of one step
   void write_frame(double* out) const;  // see vlm_solver.h for the layout
@@ -137,6 +146,10 @@ class Wing {
   AirfoilTables airfoils;
   std::vector<int> airfoilOfSection;
   bool member = false;  // a rotor of coupled rotors: nr > 1 allowed
+  const Wing* imageOf = nullptr;  // an image rotor: its source
+  // the state at the end of initialisation that an image of this rotor copies
+  d3 initHub, initCg;
+  std::vector<std::vector<d3>> initNCap;  // [blade][panel]
 
  private:
   void readConfig(const Namelist& c);
