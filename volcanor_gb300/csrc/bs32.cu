@@ -330,6 +330,9 @@ __device__ __forceinline__ void rec_lat_packed(const float4* __restrict__ R4, co
 // per SM) are template arguments; kPartial32Shapes lists the compiled ones,
 // among which the case autotuner picks per evaluation.
 constexpr int kTileW = 128;                 // records per stage (24 KB)
+// evaluations with at most this many targets find their near pairs by
+// testing every (record, target) pair (k_near_find_small)
+constexpr int kNearSmallTargets = 1024;
 constexpr int kConsumerWarps = 8;
 constexpr int kBlockW = (kConsumerWarps + 1) * 32;
 
@@ -669,6 +672,73 @@ __device__ __forceinline__ d3 fil_near64(d3 p, d3 a, d3 b, double rvc) {
 // near_factor rvc, on the FP32 kernel's own FP32 values -- is appended to the
 // near list (one atomic per warp and batch; ctl[1] counts, ctl[0] = 3 if the
 // list is full).
+// Near pairs of an evaluation with few targets (the collocation points):
+// every (record, target) pair gets k_near_find's test directly, one thread
+// per pair -- the same pairs without building a grid of the targets or
+// walking every filament through it.
+__global__ void __launch_bounds__(256) k_near_find_small(const float* __restrict__ rec32, int nrec,
+                                                         const Chunk* __restrict__ chunks, int nchunks,
+                                                         const double* __restrict__ P, int M,
+                                                         NearPair* __restrict__ near, int near_cap,
+                                                         int* __restrict__ ctl) {
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const bool live = t < (size_t)nrec * M;
+  const int r = live ? (int)(t / M) : 0, m = live ? (int)(t % M) : 0;
+  const float px = (float)P[3 * (size_t)m], py = (float)P[3 * (size_t)m + 1], pz = (float)P[3 * (size_t)m + 2];
+  const float* R = rec32 + (size_t)r * kRec32;
+  int q = 0;
+  {
+    int hi = nchunks - 1;
+    while (q < hi) {
+      const int mid = (q + hi + 1) >> 1;
+      if (chunks[mid].rec_begin <= r) q = mid;
+      else hi = mid - 1;
+    }
+  }
+  for (int k = 0; k < 4; ++k) {
+    bool isnear = false;
+    const float thr = R[32 + k];
+    if (live && thr >= 0.f) {
+      const int j = (k + 1) & 3;
+      const float ax = R[3 * k], ay = R[3 * k + 1], az = R[3 * k + 2];
+      const float ex = R[3 * j] - ax, ey = R[3 * j + 1] - ay, ez = R[3 * j + 2] - az;
+      const float eev = R[24 + k];
+      const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+      if (ee > 0.f && eev != 0.f) {
+        const float len = sqrtf(ee);
+        const float z = sqrtf(thr) / len;
+        const float iee = 1.f / ee, z2 = z * z, tlo = -z * len, thi = fmaf(z, len, ee);
+        const float dx = px - ax, dy = py - ay, dz = pz - az;
+        const float tr = fmaf(dx, ex, fmaf(dy, ey, dz * ez));
+        const float tn = tr * iee;
+        const float qx = fmaf(-tn, ex, dx), qy = fmaf(-tn, ey, dy), qz = fmaf(-tn, ez, dz);
+        isnear = fmaf(qx, qx, fmaf(qy, qy, qz * qz)) < z2 && tr > tlo && tr < thi;
+      }
+    }
+    const unsigned mask = __ballot_sync(kFull, isnear);
+    if (mask) {
+      int base_slot = 0;
+      if (lane == 0) base_slot = atomicAdd(ctl + 1, __popc(mask));
+      base_slot = __shfl_sync(kFull, base_slot, 0);
+      if (isnear) {
+        const int slot = base_slot + __popc(mask & lt);
+        if (slot < near_cap) {
+          NearPair np_;
+          np_.m = m;
+          np_.q = q;
+          np_.rec = r;
+          np_.k = k;
+          near[slot] = np_;
+        } else {
+          atomicExch(ctl, 3);
+        }
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ rec32, int nrec,
                                                    const Chunk* __restrict__ chunks, int nchunks,
                                                    const double* __restrict__ P, int M,
@@ -1033,6 +1103,23 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   const int cap = (int)std::min<size_t>((near_bytes - gridBytes) / sizeof(NearPair), (size_t)1 << 30);
   const GridLayout L = grid_layout(M);
   const int T = grid_buckets(M);
+  const int sms = device_sm_count();
+  if (M <= kNearSmallTargets && (size_t)nrec * M <= ((size_t)1 << 26)) {
+    // few targets: every pair tested directly
+    count_launches(2);
+    k_near_find_small<<<(unsigned)(((size_t)nrec * M + 255) / 256), 256, 0, ns>>>(rec32, nrec, chunks, nchunks, P, M,
+                                                                                   list, cap, ctl);
+    k_near_fix<<<4 * sms, 128, 0, ns>>>(list, cap, rec32, rec64, ew, P, M,
+                                        reinterpret_cast<unsigned long long*>(nacc), ctl);
+    if (ns != s) {
+      cudaEventRecord(ov->join, ns);
+      cudaStreamWaitEvent(s, ov->join, 0);
+    }
+    const size_t n = (size_t)M * nchunks * 3;
+    count_launch();
+    k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * sms), 256, 0, s>>>(part, nacc, n);
+    return;
+  }
   count_launches(7);
   k_grid_init<<<1, 1, 0, ns>>>(g, T);
   k_zone_mean<<<(nrec + 255) / 256, 256, 0, ns>>>(rec32, nrec, g);
@@ -1043,7 +1130,6 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
   k_near_find<<<(unsigned)(((size_t)nrec * 4 * 32 + 255) / 256), 256, 0, ns>>>(rec32, nrec, chunks, nchunks, P, M,
                                                                                g, list, cap, ctl);
-  const int sms = device_sm_count();
   k_near_fix<<<4 * sms, 128, 0, ns>>>(list, cap, rec32, rec64, ew, P, M, reinterpret_cast<unsigned long long*>(nacc),
                                       ctl);
   if (ns != s) {
