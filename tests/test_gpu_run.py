@@ -40,3 +40,21 @@ def test_run_writes_filament_files(tmp_path):
     assert F.vr_wing.shape == (8, 50) and F.vr_nwake.shape == (16, 50) and F.vf_te.shape == (4, 12)
     assert np.all(np.isfinite(F.vf_far)) and len(F.gam_far) > 0
     assert (case / "Results" / "r01ForceNonDim.csv").exists()
+
+
+def test_run_coupled_rotor_directory(tmp_path):
+    """A case directory with nr = 2 (a rotor and its ground image) writes
+    r01 and r02 force files; their CT rows are the system's."""
+    sc = C.rotor_ground_effect(height=0.8, nt=12, n_nwake=6, truncate_nt=9)
+    d = sc.write(tmp_path / "ge")
+    s = RUN.run_case(d, lib.PREC_FP64, results_dir=tmp_path / "out")
+    assert s["rotors"] == 2 and s["steps"] == 12
+    y = lib.System(sc.config, sc.geoms, d)
+    y.start()
+    rows = y.step(12)
+    for ir in (1, 2):
+        hist = np.loadtxt(tmp_path / "out" / f"r{ir:02d}ForceNonDim.csv", skiprows=1)
+        assert hist.shape == (13, 10)
+        np.testing.assert_allclose(hist[1:, 1], rows[:, ir - 1, 1], rtol=1e-6)  # E15.7 text
+        assert (tmp_path / "out" / f"r{ir:02d}Params.json").exists()
+        assert (tmp_path / "out" / f"r{ir:02d}b01ForceDist00012.csv").exists()

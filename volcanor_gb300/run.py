@@ -16,11 +16,18 @@ between its loads and its wake update; the others run in batches.  The
 reference's own post-processing (tests/test_*.py, parseResults.py) reads the
 directory unchanged.
 
+A case directory of coupled rotors (``nr > 1`` in config.nml, geom01.nml ..
+geomNN.nml, image rotors included) runs as a system (lib.System) and writes
+every rotor's ``rXXParams.json`` and force files (ForceNonDim, ForceDim,
+bYYForceDistNNNNN) at the reference's iterations; the plot files are
+written for single-rotor cases only.
+
     python -m volcanor_gb300.run <case dir> [--precision fp64|fp32|fp32near] [--steps N]
 """
 from __future__ import annotations
 
 import argparse
+import re
 import sys
 import time
 from pathlib import Path
@@ -44,13 +51,53 @@ def _due(sw: dict, k: int) -> dict:
             "probe": on("probe")}
 
 
+def rotor_count(config_text: str) -> int:
+    """nr of a config.nml (1 when absent)."""
+    m = re.search(r"^\s*nr\s*=\s*(\d+)", config_text, flags=re.I | re.M)
+    return int(m.group(1)) if m else 1
+
+
+def run_system(case_dir, precision: int = lib.PREC_FP64, steps: int | None = None, results_dir=None,
+               sum_chunk: int | None = None) -> dict:
+    """Runs a case directory of coupled rotors (nr > 1); writes every rotor's
+    Params.json and force files; returns a summary (steps, wall time, the last
+    CT row of every rotor)."""
+    d = Path(case_dir)
+    out = Path(results_dir) if results_dir is not None else d / "Results"
+    cfg = (d / "config.nml").read_text()
+    nr = rotor_count(cfg)
+    geoms = [(d / f"geom{i:02d}.nml").read_text() for i in range(1, nr + 1)]
+    y = lib.System(cfg, geoms, d, precision=precision, sum_chunk=sum_chunk)
+    t0 = time.perf_counter()
+    y.start()
+    writers = [ResultsWriter(r, out, rotor=i + 1) for i, r in enumerate(y.rotors)]
+    for w in writers:
+        w.start()
+    nt = y.rotors[0].geti("nt") if steps is None else min(int(steps), y.rotors[0].geti("nt"))
+    plot = writers[0].plot
+    it, last = 0, None
+    while it < nt:
+        n = nt - it
+        if plot > 0:
+            n = min(n, plot - it % plot)  # up to the next written iteration
+        rows = y.step(n)
+        last = rows[-1]
+        it += n
+        if plot > 0 and it % plot == 0:
+            for ir, w in enumerate(writers):
+                w._write_iteration(rows[-1, ir])
+    return {"steps": nt, "wall_s": time.perf_counter() - t0, "last_row": last, "rotors": nr}
+
+
 def run_case(case_dir, precision: int = lib.PREC_FP64, steps: int | None = None, results_dir=None,
              grid_plot: int | None = None, sum_chunk: int | None = None) -> dict:
     """Runs the case in case_dir; returns a summary (steps, wall time, last
     CT row, written plot and filament files).  sum_chunk fixes the
-    Biot-Savart summation blocks (lib.Case)."""
+    Biot-Savart summation blocks (lib.Case).  Coupled rotors: run_system."""
     d = Path(case_dir)
     out = Path(results_dir) if results_dir is not None else d / "Results"
+    if rotor_count((d / "config.nml").read_text()) > 1:
+        return run_system(case_dir, precision, steps, results_dir, sum_chunk)
     cfg, geo = (d / "config.nml").read_text(), (d / "geom01.nml").read_text()
     case = lib.Case(cfg, geo, d, precision=precision, sum_chunk=sum_chunk)
     t0 = time.perf_counter()
@@ -125,7 +172,9 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=None, help="stop after this many steps (default: nt)")
     a = ap.parse_args(argv)
     s = run_case(a.case_dir, PRECISIONS[a.precision], a.steps)
-    print(f"{s['steps']} steps in {s['wall_s']:.2f} s; last CT row {list(s['last_row'])}")
+    last = s["last_row"]
+    shown = [list(r) for r in last] if last is not None and getattr(last, "ndim", 1) == 2 else list(last)
+    print(f"{s['steps']} steps in {s['wall_s']:.2f} s; last CT row {shown}")
     return 0
 
 
