@@ -211,7 +211,8 @@ int vlm_case_get_int(vlm_case* c, const char* name, int64_t* value);
  * live wake-node and collocation-point evaluations with each compiled tile
  * shape (0: 512 targets per block, 4 stages, 2 blocks per SM; 1: 256 targets
  * per block, 3 stages, 3 blocks per SM) at the wave model's chunk count and at
- * 1/2, 3/4, 3/2 and 2 times it, and keeps the fastest (vlm_case_get
+ * 1/2, 3/4, 3/2 and 2 times it, then the best shape at +-1, 2, 3 chunks of
+ * its best count, and keeps the fastest (vlm_case_get
  * "autotune").  This call re-plans every step after the current one with
  * `shape` and `chunks` chunks for the largest group of each evaluation (0 =
  * the wave model's count) and turns the tuner off; shape -1 turns it back

@@ -330,8 +330,8 @@ __device__ __forceinline__ void rec_lat_packed(const float4* __restrict__ R4, co
 // per SM) are template arguments; kPartial32Shapes lists the compiled ones,
 // among which the case autotuner picks per evaluation.
 constexpr int kTileW = 128;                 // records per stage (24 KB)
-// evaluations with at most this many targets find their near pairs by
-// testing every (record, target) pair (k_near_find_small)
+// evaluations with at most this many targets (and at most 2^22 record-target
+// pairs) find their near pairs by testing every pair (k_near_find_small)
 constexpr int kNearSmallTargets = 1024;
 constexpr int kConsumerWarps = 8;
 constexpr int kBlockW = (kConsumerWarps + 1) * 32;
@@ -1104,7 +1104,7 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
   const GridLayout L = grid_layout(M);
   const int T = grid_buckets(M);
   const int sms = device_sm_count();
-  if (M <= kNearSmallTargets && (size_t)nrec * M <= ((size_t)1 << 26)) {
+  if (M <= kNearSmallTargets && (size_t)nrec * M <= ((size_t)1 << 22)) {
     // few targets: every pair tested directly
     count_launches(2);
     k_near_find_small<<<(unsigned)(((size_t)nrec * M + 255) / 256), 256, 0, ns>>>(rec32, nrec, chunks, nchunks, P, M,

@@ -518,7 +518,8 @@ struct Case {
       launch_pack32(s.rec64, e.nrec, nearOn ? opt.near_factor : 0.0, s.rec32, stream, s.edgeW);
       VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
       launch_partial32(s.rec32, s.rec64, ch, e.nchunks, e.nrec, P, M, s.part, s.err + 2,
-                       nearOn ? s.nearScratch : nullptr, s.nearBytes, s.nacc, stream, s.edgeW, e.shape, &nearOv);
+                       nearOn ? s.nearScratch : nullptr, s.nearBytes, s.nacc, stream, s.edgeW, e.shape,
+                       opt.nbody_slots > 0 ? nullptr : &nearOv);  // a batch's cases already run side by side
     }
     if (e.nchunks == 0) {
       VLM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)M * std::max(nterms, 1), stream));
@@ -537,8 +538,9 @@ struct Case {
   // every later step of a truncated wake repeats, and the one captured as a
   // graph -- the case times, on its live state, the wake-node and the
   // collocation-point evaluations for both tile shapes at the model's chunk
-  // count and at 1/2, 3/4, 3/2 and 2 times it (5 launches each after a warm
-  // one, CUDA events), and keeps the fastest for every later step of that
+  // count and at 1/2, 3/4, 3/2 and 2 times it, then the best shape at +-1, 2
+  // and 3 chunks of its best count (5 launches each after a warm one, CUDA
+  // events), and keeps the fastest for every later step of that
   // signature if it beats the model's plan by more than 3 % (near ties keep
   // the model's plan, so that a choice does not flip with timing noise).
   // Only the FP32 pair kernel is timed (the near-field correction does not
@@ -704,46 +706,53 @@ struct Case {
       double* dpart = dalloc<double>((size_t)kMaxTunePart * 3, tmp);
       bestMs = 1e30;
       curMs = 1e30;
-      int modelN = 0;
-      for (int shape = 0; shape < kPartial32Shapes; ++shape) {
-        const int tpb = partial32_targets_per_block(shape);
-        const int n0 = plan_count32(g0.data(), e.ngroups, M, partial32_slots(shape), cap, tpb);
-        int maxRec = 0;
-        for (const Group& g : g0) maxRec = std::max(maxRec, g.rec_count);
-        const int ns[5] = {n0, std::max(1, n0 / 2), std::max(1, 3 * n0 / 4), (3 * n0 + 1) / 2, 2 * n0};
-        std::vector<int> seen;
-        for (int n : ns) {
-          n = std::min(n, std::max(1, maxRec));
-          if (std::find(seen.begin(), seen.end(), n) != seen.end()) continue;
-          seen.push_back(n);
-          std::vector<Group> g = g0;
-          std::vector<Chunk> ch((size_t)cap);
-          const int nq = build_chunks32(g.data(), e.ngroups, n, ch.data(), cap);
-          if (nq <= 0 || (int64_t)nq * M > kMaxTunePart) continue;
-          VLM_CUDA(cudaMemcpyAsync(dch, ch.data(), sizeof(Chunk) * nq, cudaMemcpyHostToDevice, stream));
-          auto launch = [&]() {
-            launch_partial32(s.rec32, s.rec64, dch, nq, e.nrec, s.targets, M, dpart, s.err + 2, nullptr, 0, nullptr,
-                             stream, s.edgeW, shape);
-          };
-          launch();
-          VLM_CUDA(cudaEventRecord(t0, stream));
-          for (int r = 0; r < kReps; ++r) launch();
-          VLM_CUDA(cudaEventRecord(t1, stream));
-          VLM_CUDA(cudaEventSynchronize(t1));
-          float ms = 0.f;
-          VLM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
-          const double per = ms / kReps;
-          ++tr.candidates;
-          if (shape == 0 && n == n0) {
-            curMs = per;
-            modelN = n0;
-          }
-          if (per < bestMs) {
-            bestMs = per;
-            bestShape = shape;
-            bestN = n;
-          }
+      int modelN = 0;  // the wave model's count for shape 0
+      int maxRec = 0;
+      for (const Group& g : g0) maxRec = std::max(maxRec, g.rec_count);
+      std::vector<std::pair<int, int>> seen;
+      // one candidate (tile shape, chunk count of the largest group) timed;
+      // skipped when already timed or too large for the timing buffer
+      auto timeOne = [&](int shape, int n) {
+        n = std::min(n, std::max(1, maxRec));
+        if (n < 1 || std::find(seen.begin(), seen.end(), std::make_pair(shape, n)) != seen.end()) return;
+        seen.emplace_back(shape, n);
+        std::vector<Group> g = g0;
+        std::vector<Chunk> ch((size_t)cap);
+        const int nq = build_chunks32(g.data(), e.ngroups, n, ch.data(), cap);
+        if (nq <= 0 || (int64_t)nq * M > kMaxTunePart) return;
+        VLM_CUDA(cudaMemcpyAsync(dch, ch.data(), sizeof(Chunk) * nq, cudaMemcpyHostToDevice, stream));
+        auto launch = [&]() {
+          launch_partial32(s.rec32, s.rec64, dch, nq, e.nrec, s.targets, M, dpart, s.err + 2, nullptr, 0, nullptr,
+                           stream, s.edgeW, shape);
+        };
+        launch();
+        VLM_CUDA(cudaEventRecord(t0, stream));
+        for (int r = 0; r < kReps; ++r) launch();
+        VLM_CUDA(cudaEventRecord(t1, stream));
+        VLM_CUDA(cudaEventSynchronize(t1));
+        float ms = 0.f;
+        VLM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+        const double per = ms / kReps;
+        ++tr.candidates;
+        if (shape == 0 && n == modelN) curMs = per;
+        if (per < bestMs) {
+          bestMs = per;
+          bestShape = shape;
+          bestN = n;
         }
+      };
+      modelN = plan_count32(g0.data(), e.ngroups, M, partial32_slots(0), cap, partial32_targets_per_block(0));
+      // coarse: each shape at its wave model's count and 1/2, 3/4, 3/2, 2 x it
+      for (int shape = 0; shape < kPartial32Shapes; ++shape) {
+        const int n0 = plan_count32(g0.data(), e.ngroups, M, partial32_slots(shape), cap,
+                                    partial32_targets_per_block(shape));
+        for (int n : {n0, std::max(1, n0 / 2), std::max(1, 3 * n0 / 4), (3 * n0 + 1) / 2, 2 * n0}) timeOne(shape, n);
+      }
+      // fine: the best shape at +-1, 2, 3 chunks of its best count (the last
+      // wave of blocks is what a chunk count moves)
+      if (bestN > 0) {
+        const int cs = bestShape, cn = bestN;
+        for (int dn : {-3, -2, -1, 1, 2, 3}) timeOne(cs, cn + dn);
       }
       if (bestN <= 0) continue;
       // near ties keep the wave model's plan
