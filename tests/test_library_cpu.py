@@ -5,6 +5,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 from volcanor_gb300 import build as vbuild
 from volcanor_gb300 import cases as C
@@ -107,3 +108,34 @@ def test_fortran_interfaces_match_header():
     for args, name in found:
         n = len([a for a in args.split(",") if a.strip()])
         assert arity[name] == n, (name, arity[name], n)
+
+
+def test_system_argument_checks_without_gpu():
+    """vlm_system_create rejects missing rotors and texts on the host."""
+    L = lib.load()
+    h = ctypes.c_void_p()
+    geoms = (ctypes.c_char_p * 1)(b"&PANELS nb = 1 /")
+    assert L.vlm_system_create(b"&PARAMS nt = 5 /", 0, geoms, b"", None, ctypes.byref(h)) == 1
+    assert L.vlm_system_create(None, 1, geoms, b"", None, ctypes.byref(h)) == 1
+    assert not h.value
+    assert L.vlm_system_rotor_count(None) == -1
+    assert L.vlm_system_start(None) == 1
+
+
+def test_airfoil_tables_read_on_the_host(tmp_path):
+    """A forceCalcSwitch 1 case reads its C81 files when the library builds
+    its geometry (vlm_params_json runs that on the host): present files
+    load, a missing one is reported, axisymmetry is refused."""
+    from volcanor_gb300 import cases as C
+    c = C.rotor_2blade_hover(nt=10, n_nwake=4, truncate_nt=6)
+    (tmp_path / "a.C81").write_text(C.synthetic_airfoil("a", nmach=11))
+    (tmp_path / "b.C81").write_text(C.synthetic_airfoil("b"))
+    geo = (c.geom.replace("forceCalcSwitch = 0", "forceCalcSwitch = 1").replace("nAirfoils = 0", "nAirfoils = 2")
+           .replace("airfoilSectionLimit = 1.0", "airfoilSectionLimit = 0.6, 1.0")
+           .replace("airfoilFile = 0", "airfoilFile = a.C81, b.C81"))
+    text = lib.params_json(c.config, geo, tmp_path)
+    assert '"forceCalcSwitch"' in text
+    with pytest.raises(lib.VlmError):
+        lib.params_json(c.config, geo.replace("b.C81", "missing.C81"), tmp_path)
+    with pytest.raises(lib.VlmError):
+        lib.params_json(c.config, geo.replace("axisymmetrySwitch = 0", "axisymmetrySwitch = 1"), tmp_path)
