@@ -61,6 +61,12 @@ typedef struct vlm_options {
                           filament shared by two rings once with their circulation
                           difference (0 = ring by ring as the reference; -1 / nonzero =
                           lattice form, the default).  No effect on VLM_PREC_FP64. */
+  int incremental;     /* FP32 precisions, schemes with a predictor (fdSchemeSwitch 1, 3, 4, 5):
+                          the predicted-wake velocities as the current-wake ones plus the
+                          changed sources' difference, and the full sum at the moved wake nodes
+                          only, on steps whose (rowNear, rowFar) signature lasts more than one
+                          step (1 = on, the default; 0 = the full sum).  A lone case only (not
+                          a batch, a coupled rotor or the surrogate); no effect on FP64. */
 } vlm_options;
 
 /* ---- library ------------------------------------------------------------ */

@@ -19,6 +19,7 @@ module vlm_gb300
     integer(c_int) :: solve_mode
     integer(c_int) :: nbody_slots
     integer(c_int) :: lattice
+    integer(c_int) :: incremental
   end type
 
   interface

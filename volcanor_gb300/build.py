@@ -1,6 +1,6 @@
 """Builds libvlm_gb300.so in-tree (volcanor_gb300/_build/) for sm_103a.
 
-FP64 translation units (bs64.cu, solver.cu) are compiled with -fmad=false and
+FP64 translation units (bs64.cu, solver.cu, incr.cu) are compiled with -fmad=false and
 the host units with -ffp-contract=off so that every FP64 operation rounds as
 in the reference arithmetic; the FP32 kernel unit (bs32.cu) keeps FMA
 contraction and flushes FP32 denormals (-ftz=true), which lets rsqrtf map to
@@ -19,7 +19,7 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libvlm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_EXACT = ["bs64.cu", "solver.cu"]
+CU_EXACT = ["bs64.cu", "solver.cu", "incr.cu"]
 CU_FAST = ["bs32.cu"]
 CU_PLAIN = ["noalloc.cu", "mlp.cu", "mlp_tc.cu", "surrogate.cu", "peak.cu"]
 CXX = ["wing.cpp", "case.cpp", "plan.cpp"]

@@ -1071,7 +1071,8 @@ int partial32_targets_per_block(int shape) { return kConsumerWarps * 32 * (shape
 
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
                       const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
-                      long long* nacc, cudaStream_t s, const double* ew, int shape, const NearOverlap* ov) {
+                      long long* nacc, cudaStream_t s, const double* ew, int shape, const NearOverlap* ov,
+                      bool reuse_grid) {
   if (M <= 0 || nchunks <= 0) return;
   ensure_smem_attrs();
   const int tpb = partial32_targets_per_block(shape);
@@ -1120,14 +1121,17 @@ void launch_partial32(const float* rec32, const double* rec64, const Chunk* chun
     k_near_apply<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)8 * sms), 256, 0, s>>>(part, nacc, n);
     return;
   }
-  count_launches(7);
-  k_grid_init<<<1, 1, 0, ns>>>(g, T);
-  k_zone_mean<<<(nrec + 255) / 256, 256, 0, ns>>>(rec32, nrec, g);
-  cudaMemsetAsync(g + L.key, 0xFF, (size_t)T * sizeof(unsigned long long), ns);
-  cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), ns);
-  k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
-  k_grid_scan<<<1, 1024, 0, ns>>>(M, g);
-  k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
+  if (!reuse_grid) {
+    count_launches(5);
+    k_grid_init<<<1, 1, 0, ns>>>(g, T);
+    k_zone_mean<<<(nrec + 255) / 256, 256, 0, ns>>>(rec32, nrec, g);
+    cudaMemsetAsync(g + L.key, 0xFF, (size_t)T * sizeof(unsigned long long), ns);
+    cudaMemsetAsync(g + L.count, 0, (size_t)T * sizeof(int), ns);
+    k_tgrid_insert<0><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
+    k_grid_scan<<<1, 1024, 0, ns>>>(M, g);
+    k_tgrid_insert<1><<<(M + 255) / 256, 256, 0, ns>>>(P, M, g);
+  }
+  count_launches(2);
   k_near_find<<<(unsigned)(((size_t)nrec * 4 * 32 + 255) / 256), 256, 0, ns>>>(rec32, nrec, chunks, nchunks, P, M,
                                                                                g, list, cap, ctl);
   k_near_fix<<<4 * sms, 128, 0, ns>>>(list, cap, rec32, rec64, ew, P, M, reinterpret_cast<unsigned long long*>(nacc),

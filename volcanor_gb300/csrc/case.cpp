@@ -103,6 +103,15 @@ struct Case {
     for (void* p : owned) cudaFree(p);
     for (void* p : scratchOwned) cudaFree(p);
     for (void* p : surrOwned) cudaFree(p);
+    if (incrStream) cudaStreamSynchronize(incrStream);
+    if (incrOv.stream) cudaStreamSynchronize(incrOv.stream);
+    for (void* p : incrOwned) cudaFree(p);
+    if (incrFork) cudaEventDestroy(incrFork);
+    if (incrJoin) cudaEventDestroy(incrJoin);
+    if (incrOv.fork) cudaEventDestroy(incrOv.fork);
+    if (incrOv.join) cudaEventDestroy(incrOv.join);
+    if (incrOv.stream) cudaStreamDestroy(incrOv.stream);
+    if (incrStream) cudaStreamDestroy(incrStream);
     surr.net.destroy();
     if (gexec) cudaGraphExecDestroy(gexec);
     if (hIter) cudaFreeHost(hIter);
@@ -782,6 +791,216 @@ struct Case {
     tuned.push_back(tr);
   }
 
+  // ---- incremental predicted-wake evaluation (incr.cu) ---------------------
+  // The predictor of the Adams-Moulton / predictor-corrector schemes moves a
+  // few node rows and the far wake; every other record and target of the
+  // predicted-wake evaluation equals the current-wake evaluation's of the same
+  // step.  On the FP32 precisions the predicted-wake velocity is then the
+  // current-wake velocity (still in s.outv) plus the changed records' new minus
+  // old contributions at every target, and the full sum at the moved targets
+  // alone.  The changed records and moved targets are found on the device by
+  // a bit-by-bit comparison every step; their numbers, fixed by the wake's
+  // structure for a (rowNear, rowFar) signature, are measured once at the
+  // first step of a signature that lasts at least kIncrMinRun steps (a host
+  // synchronisation), and size the fixed-capacity buffers a captured step
+  // graph needs.  A signature whose incremental work is not below half the
+  // full evaluation's keeps the full evaluation.  The choice depends only on
+  // the case and the signature, so runs resumed anywhere give the same bits.
+  struct IncrPlan {
+    int rN = 0, rF = 0;
+    bool on = false;
+    int nrec = 0, M = 0, changed = 0, moved = 0;
+    int dcap = 0, mcap = 0;           // delta records (2 per changed record + inert), moved targets
+    int dq = 0, dmaxq = 0, mq = 0, mmaxq = 0, mng = 0;
+    Group *dG = nullptr, *mG = nullptr;
+    Chunk *dC = nullptr, *mC = nullptr;
+    double *dRec = nullptr, *dEw = nullptr, *outD = nullptr, *tPos = nullptr, *tOut = nullptr;
+    double *dPart = nullptr, *mPart = nullptr;
+    long long *dNacc = nullptr, *mNacc = nullptr;
+    int* tIdx = nullptr;
+    // the moved targets' evaluation runs beside the delta set's: its own
+    // FP32 records, near-field scratch and streams
+    float* mRec32 = nullptr;
+    void* mNear = nullptr;
+    size_t mNearBytes = 0;
+  };
+  static constexpr int kMaxIncrPlans = 8;
+  std::vector<IncrPlan> incr;
+  std::vector<void*> incrOwned;
+  double *recP = nullptr, *ewP = nullptr, *tgtP = nullptr;  // the predicted records, edge weights, targets
+  int* incrCnt = nullptr;                                   // [0] changed records, [1] moved targets
+  int* incrBlk = nullptr;                                   // per-tile offsets: records, then targets
+  cudaStream_t incrStream = nullptr;                        // the moved targets' evaluation
+  NearOverlap incrOv{nullptr, nullptr, nullptr};            // its near-field chain
+  cudaEvent_t incrFork = nullptr, incrJoin = nullptr;
+  int* incrCtl = nullptr;  // the moved targets' evaluation's error code and near-pair cursor
+
+  bool incrAllowed() const {
+    return opt.incremental != 0 && opt.precision != VLM_PREC_FP64 && opt.nbody_slots <= 0 && !member && !surr.on &&
+           d.NW > 0;
+  }
+  bool sameSig(int a, int b) const {
+    return a >= 1 && b >= 1 && a <= W.nt && b <= W.nt && plans[a].rowNear == plans[b].rowNear &&
+           plans[a].rowFar == plans[b].rowFar;
+  }
+  int incrIndex(int k) const {
+    for (size_t i = 0; i < incr.size(); ++i)
+      if (incr[i].rN == plans[k].rowNear && incr[i].rF == plans[k].rowFar) return (int)i;
+    return -1;
+  }
+  // steps in the run of consecutive steps with step k's signature
+  mutable std::vector<int> sigRunLen;
+  int sigRun(int k) const {
+    if (sigRunLen.empty()) {
+      sigRunLen.assign((size_t)W.nt + 1, 0);
+      for (int a = 1; a <= W.nt;) {
+        int b = a;
+        while (b + 1 <= W.nt && sameSig(a, b + 1)) ++b;
+        for (int i = a; i <= b; ++i) sigRunLen[i] = b - a + 1;
+        a = b + 1;
+      }
+    }
+    return k >= 1 && k <= W.nt ? sigRunLen[k] : 0;
+  }
+  static constexpr int kIncrMinRun = 16;  // a signature worth a measurement lasts this many steps
+  // step k's predicted-wake evaluation measures its signature first
+  bool incrMeasureDue(int k) const {
+    return incrAllowed() && predicts(k) && incrIndex(k) < 0 && (int)incr.size() < kMaxIncrPlans &&
+           sigRun(k) >= kIncrMinRun;
+  }
+  void allocIncrBase() {
+    if (recP) return;
+    recP = dalloc<double>((size_t)maxRecords * kRec64, incrOwned);
+    ewP = lattice() ? dalloc<double>((size_t)maxRecords * 4, incrOwned) : nullptr;
+    tgtP = dalloc<double>((size_t)maxTargets * 3, incrOwned);
+    incrCnt = dalloc<int>(2, incrOwned);
+    incrCtl = dalloc<int>(2, incrOwned);
+    incrBlk = dalloc<int>((size_t)incr_diff_blocks(maxRecords) + incr_diff_blocks(maxTargets) + 2, incrOwned);
+    VLM_CUDA(cudaStreamCreateWithFlags(&incrStream, cudaStreamNonBlocking));
+    VLM_CUDA(cudaStreamCreateWithFlags(&incrOv.stream, cudaStreamNonBlocking));
+    VLM_CUDA(cudaEventCreateWithFlags(&incrOv.fork, cudaEventDisableTiming));
+    VLM_CUDA(cudaEventCreateWithFlags(&incrOv.join, cudaEventDisableTiming));
+    VLM_CUDA(cudaEventCreateWithFlags(&incrFork, cudaEventDisableTiming));
+    VLM_CUDA(cudaEventCreateWithFlags(&incrJoin, cudaEventDisableTiming));
+  }
+  // the predicted targets and records beside the current ones, and the
+  // comparison (counts and per-tile offsets)
+  void incrDiff(int k, int M) {
+    const StepPlan& pl = plans[k];
+    const EvalPlan& e = pl.node;
+    launch_node_targets(d, s, pl.rowNear, pl.rowFar, true, tgtP, stream);
+    DevState sp = s;
+    sp.rec64 = recP;
+    sp.edgeW = s.edgeW ? ewP : nullptr;
+    launch_gather(d, sp, stepFrame(k), dGroups + e.goff, e.ngroups, e.nrec, pl.rowNear, pl.rowFar, true, stream);
+    launch_diff_count(recP, s.rec64, kRec64, sp.edgeW, s.edgeW, e.nrec, incrBlk, incrCnt, stream);
+    launch_diff_count(tgtP, s.targets, 3, nullptr, nullptr, M, incrBlk + incr_diff_blocks(e.nrec), incrCnt + 1,
+                      stream);
+  }
+  static int roundUp(int x, int m) { return (x + m - 1) / m * m; }
+  void measureIncr(int k, int M) {
+    const EvalPlan& e = plans[k].node;
+    IncrPlan ip;
+    ip.rN = plans[k].rowNear;
+    ip.rF = plans[k].rowFar;
+    ip.nrec = e.nrec;
+    ip.M = M;
+    if (M > 0 && e.nrec > 0) {
+      allocIncrBase();
+      incrDiff(k, M);
+      int cnt[2] = {0, 0};
+      VLM_CUDA(cudaMemcpyAsync(cnt, incrCnt, sizeof(cnt), cudaMemcpyDeviceToHost, stream));
+      VLM_CUDA(cudaStreamSynchronize(stream));
+      ip.changed = cnt[0];
+      ip.moved = cnt[1];
+      // slack for records or targets that happened not to move this step
+      ip.dcap = 2 * roundUp(cnt[0] + cnt[0] / 32 + 16, 32);
+      ip.mcap = roundUp(cnt[1] + cnt[1] / 32 + 16, 32);
+      const double full = (double)e.nrec * M;
+      const double inc = (double)ip.dcap * M + (double)e.nrec * ip.mcap + (double)(1 << 23);
+      ip.on = ip.dcap <= e.nrec && ip.mcap < M && inc < 0.5 * full;
+    }
+    if (ip.on) buildIncr(ip, e);
+    incr.push_back(ip);
+  }
+  void buildIncr(IncrPlan& ip, const EvalPlan& e) {
+    const int slots = partial32_slots(0), tpb = partial32_targets_per_block(0);
+    // the delta set: one wake group of dcap records at the M targets
+    Group g{};
+    g.rec_begin = 0;
+    g.rec_count = ip.dcap;
+    g.kind = 1;
+    std::vector<Chunk> dch((size_t)ip.dcap + 2);
+    const int dn = plan_count32(&g, 1, ip.M, slots, ip.dcap + 2, tpb);
+    ip.dq = build_chunks32(&g, 1, std::max(dn, 1), dch.data(), ip.dcap + 2);
+    ip.dmaxq = g.chunk_count;
+    // the moved targets: the node evaluation's groups re-chunked for mcap targets
+    std::vector<Group> mg(hGroups.begin() + e.goff, hGroups.begin() + e.goff + e.ngroups);
+    const int mcapCh = e.nrec + e.ngroups + 1;
+    std::vector<Chunk> mch((size_t)mcapCh);
+    const int mn = plan_count32(mg.data(), e.ngroups, ip.mcap, slots, mcapCh, tpb);
+    ip.mq = build_chunks32(mg.data(), e.ngroups, std::max(mn, 1), mch.data(), mcapCh);
+    if (ip.dq <= 0 || ip.mq <= 0) throw std::runtime_error("chunk table overflow");
+    ip.mng = e.ngroups;
+    ip.mmaxq = 0;
+    for (const Group& x : mg) ip.mmaxq = std::max(ip.mmaxq, x.chunk_count);
+    ip.dG = dalloc<Group>(1, incrOwned);
+    ip.dC = dalloc<Chunk>((size_t)ip.dq, incrOwned);
+    ip.mG = dalloc<Group>((size_t)e.ngroups, incrOwned);
+    ip.mC = dalloc<Chunk>((size_t)ip.mq, incrOwned);
+    VLM_CUDA(cudaMemcpy(ip.dG, &g, sizeof(Group), cudaMemcpyHostToDevice));
+    VLM_CUDA(cudaMemcpy(ip.dC, dch.data(), sizeof(Chunk) * ip.dq, cudaMemcpyHostToDevice));
+    VLM_CUDA(cudaMemcpy(ip.mG, mg.data(), sizeof(Group) * e.ngroups, cudaMemcpyHostToDevice));
+    VLM_CUDA(cudaMemcpy(ip.mC, mch.data(), sizeof(Chunk) * ip.mq, cudaMemcpyHostToDevice));
+    ip.dRec = dalloc<double>((size_t)ip.dcap * kRec64, incrOwned);
+    ip.dEw = lattice() ? dalloc<double>((size_t)ip.dcap * 4, incrOwned) : nullptr;
+    ip.outD = dalloc<double>((size_t)ip.M * 3, incrOwned);
+    ip.tIdx = dalloc<int>((size_t)ip.mcap, incrOwned);
+    ip.tPos = dalloc<double>((size_t)ip.mcap * 3, incrOwned);
+    ip.tOut = dalloc<double>((size_t)ip.mcap * 3, incrOwned);
+    const bool nearOn = opt.precision == VLM_PREC_FP32_NEAR64;
+    const size_t nd = (size_t)ip.dq * ip.M * 3, nm = (size_t)ip.mq * ip.mcap * 3;
+    ip.dPart = dalloc<double>(nd, incrOwned);
+    ip.mPart = dalloc<double>(nm, incrOwned);
+    // zero (dalloc), and every near-field evaluation leaves them zero
+    ip.dNacc = dalloc<long long>(nearOn ? nd : 1, incrOwned);
+    ip.mNacc = dalloc<long long>(nearOn ? nm : 1, incrOwned);
+    ip.mRec32 = dalloc<float>((size_t)ip.nrec * kRec32, incrOwned);
+    ip.mNearBytes = nearOn ? near_scratch_bytes(ip.mcap, (size_t)256 * ip.mcap) : 0;
+    ip.mNear = nearOn ? (void*)dalloc<unsigned char>(ip.mNearBytes, incrOwned) : nullptr;
+  }
+  // the predicted-wake velocities into s.outv, which holds the current-wake ones
+  void evalPredIncr(int k, int M, const IncrPlan& ip) {
+    const EvalPlan& e = plans[k].node;
+    const bool nearOn = opt.precision == VLM_PREC_FP32_NEAR64;
+    const double nf = nearOn ? opt.near_factor : 0.0;
+    incrDiff(k, M);
+    const double* ew = s.edgeW ? ewP : nullptr;
+    launch_moved_targets(tgtP, s.targets, M, incrBlk + incr_diff_blocks(e.nrec), incrCnt + 1, ip.tIdx, ip.tPos,
+                         ip.mcap, s.err + 2, stream);
+    // every predicted record at the moved targets, on its own streams
+    VLM_CUDA(cudaEventRecord(incrFork, stream));
+    VLM_CUDA(cudaStreamWaitEvent(incrStream, incrFork, 0));
+    launch_pack32(recP, e.nrec, nf, ip.mRec32, incrStream, ew);
+    VLM_CUDA(cudaMemsetAsync(incrCtl + 1, 0, sizeof(int), incrStream));
+    launch_partial32(ip.mRec32, recP, ip.mC, ip.mq, e.nrec, ip.tPos, ip.mcap, ip.mPart, incrCtl, ip.mNear,
+                     ip.mNearBytes, ip.mNacc, incrStream, ew, 0, &incrOv);
+    launch_combine_unordered(ip.mPart, ip.mcap, ip.mG, ip.mng, ip.mmaxq, 0, ip.tOut, incrStream);
+    VLM_CUDA(cudaEventRecord(incrJoin, incrStream));
+    // the changed records (new +, old -) at every target: the current-wake
+    // targets, whose near-field grid the current-wake evaluation left in the
+    // scratch (the moved targets' results are replaced below)
+    launch_delta_records(recP, s.rec64, ew, s.edgeW, e.nrec, incrBlk, incrCnt, ip.dRec, ip.dEw, ip.dcap, s.err + 2,
+                         stream);
+    launch_pack32(ip.dRec, ip.dcap, nf, s.rec32, stream, ip.dEw);
+    VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
+    launch_partial32(s.rec32, ip.dRec, ip.dC, ip.dq, ip.dcap, s.targets, M, ip.dPart, s.err + 2,
+                     nearOn ? s.nearScratch : nullptr, s.nearBytes, ip.dNacc, stream, ip.dEw, 0, &nearOv, true);
+    launch_combine_unordered(ip.dPart, M, ip.dG, 1, ip.dmaxq, 0, ip.outD, stream);
+    VLM_CUDA(cudaStreamWaitEvent(stream, incrJoin, 0));
+    launch_incr_merge(s.outv, ip.outD, M, ip.tIdx, ip.tOut, incrCnt + 1, ip.mcap, incrCtl, s.err + 2, stream);
+  }
+
   // ---- coupled rotors (nr > 1, vlm_system) ----------------------------------
   // Every rotor of a system is a Case on the system's one stream.  Its RHS
   // and wake-node evaluations sum the records of every rotor: each source
@@ -1179,6 +1398,18 @@ struct Case {
   void evalNodes(int k, bool pred) {
     const StepPlan& pl = plans[k];
     const int M = node_target_count(d, pl.rowNear, pl.rowFar);
+    if (pred && !replaying && incrMeasureDue(k)) measureIncr(k, M);
+    const int ii = pred && incrAllowed() ? incrIndex(k) : -1;
+    if (ii >= 0 && incr[ii].on) {
+      evalPredIncr(k, M, incr[ii]);
+    } else {
+      evalNodesFull(k, pred, M);
+    }
+    const double iwv = k < W.sw.initWakeVelNt ? W.P.initWakeVel : 0.0;
+    launch_scatter_nodes(d, s, stepFrame(k), pl.rowNear, pl.rowFar, pred, iwv, stream);
+  }
+  void evalNodesFull(int k, bool pred, int M) {
+    const StepPlan& pl = plans[k];
     launch_node_targets(d, s, pl.rowNear, pl.rowFar, pred, s.targets, stream);
     if (member) {
       const SysEval& se = sysNode[k];
@@ -1206,8 +1437,6 @@ struct Case {
                     pred, stream);
       evaluate(pl.node, M, 0);
     }
-    const double iwv = k < W.sw.initWakeVelNt ? W.P.initWakeVel : 0.0;
-    launch_scatter_nodes(d, s, stepFrame(k), pl.rowNear, pl.rowFar, pred, iwv, stream);
   }
 
   // The AIC of the initial geometry, its FP64 LU and explicit inverse, the
@@ -1444,7 +1673,7 @@ struct Case {
   }
   void enqueueOne(int k) {
     if (tuneOn() && sigRepeats(k) && !tunedFor(plans[k])) autotune(k);
-    if (steadyStep(k)) {
+    if (steadyStep(k) && !incrMeasureDue(k)) {
       replayStep(k);
       return;
     }
@@ -1464,6 +1693,8 @@ struct Case {
     const int err = errs[2];
     if (err == 3) throw StatusError(VLM_ERR_CUDA, "near-field pair list overflowed");
     if (err == 4) throw StatusError(VLM_ERR_NONFINITE, "near-field velocity outside the fixed-point range");
+    if (err == 5)
+      throw StatusError(VLM_ERR_CUDA, "predicted wake: more changed records or moved targets than its plan holds");
     if (err) throw StatusError(VLM_ERR_CUDA, "device wait limit expired in a Biot-Savart tile pipeline");
     if (errs[1]) throw StatusError(VLM_ERR_SINGULAR, "FP32 LU iterative refinement left a relative residual above 1e-9");
     if (ctRows)
@@ -1865,6 +2096,13 @@ struct Case {
     else if (bok && b < d.nbC && k == "forceDist") v = forceDist(b);
     else if (k == "forceDim") v = forceDim();
     else if (k == "profileWork") v = {profileWork[0], profileWork[1]};
+    else if (k == "incremental") {
+      // per measured signature: rowNear, rowFar, used (0/1), changed records,
+      // moved targets, record capacity, target capacity, records, targets
+      for (const IncrPlan& ip : incr)
+        v.insert(v.end(), {(double)ip.rN, (double)ip.rF, ip.on ? 1.0 : 0.0, (double)ip.changed, (double)ip.moved,
+                           (double)ip.dcap, (double)ip.mcap, (double)ip.nrec, (double)ip.M});
+    }
     else if (k == "autotune") {
       // per tuned signature: rowNear, rowFar, candidates timed, then for the
       // wake nodes and the collocation points: shape, chunk count of the
@@ -2287,6 +2525,7 @@ void vlm_default_options(vlm_options* o) {
   o->solve_mode = -1;
   o->nbody_slots = 0;
   o->lattice = -1;
+  o->incremental = 1;
 }
 
 int vlm_device_info(int device, int* sm_count, int* cc_major, int* cc_minor) {

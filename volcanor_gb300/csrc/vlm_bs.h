@@ -179,6 +179,9 @@ void launch_partial64(const double* rec, const Chunk* chunks, int nchunks, const
 // by ew[4 rec + k] instead of the record's circulation), or null.
 // A second stream and two events on which launch_partial32 runs the
 // near-field detection and correction alongside the pair kernel.
+// reuse_grid: near_scratch already holds the target grid of these M targets P
+// (built by the previous near-field evaluation at the same targets, whose
+// records set its cell size), so only the pair search over these records runs.
 struct NearOverlap {
   cudaStream_t stream;
   cudaEvent_t fork, join;
@@ -186,7 +189,7 @@ struct NearOverlap {
 void launch_partial32(const float* rec32, const double* rec64, const Chunk* chunks, int nchunks, int nrec,
                       const double* P, int M, double* part, int* ctl, void* near_scratch, size_t near_bytes,
                       long long* nacc, cudaStream_t s, const double* ew = nullptr, int shape = 0,
-                      const NearOverlap* ov = nullptr);
+                      const NearOverlap* ov = nullptr, bool reuse_grid = false);
 // Converts FP64 records to FP32 records (near_factor <= 0 disables near-field);
 // ew as above (null: every active filament of a record carries its gam).
 void launch_pack32(const double* rec64, int nrec, double near_factor, float* rec32, cudaStream_t s,
@@ -213,6 +216,28 @@ void launch_combine_unordered(const double* part, int M, const Group* groups, in
 // else the FP32 paths' fixed tree.
 void launch_combine_terms(const double* part, int M, const Group* groups, int ngroups, int max_chunks, int mode,
                           bool ordered, double* out, cudaStream_t s);
+
+// Incremental predicted-wake evaluation (incr.cu).  Items of two sets that
+// differ bit by bit (records: kRec64 doubles and, with ea/eb, 4 edge weights;
+// targets: 3 doubles): launch_diff_count leaves per-tile exclusive offsets in
+// blockCount (incr_diff_blocks(n) entries) and the number in *total.
+int incr_diff_blocks(int n);
+void launch_diff_count(const double* a, const double* b, int stride, const double* ea, const double* eb, int n,
+                       int* blockCount, int* total, cudaStream_t s);
+// The delta set of the changed records (predicted +, current with negated
+// circulation -), padded to cap (even) with inert records; ctl = 5 when more
+// than cap / 2 records changed.
+void launch_delta_records(const double* recP, const double* recC, const double* ewP, const double* ewC, int nrec,
+                          const int* blockOff, const int* total, double* dRec, double* dEw, int cap, int* ctl,
+                          cudaStream_t s);
+// The moved targets' indices and positions, padded to cap; ctl = 5 when more than cap moved.
+void launch_moved_targets(const double* tP, const double* tC, int M, const int* blockOff, const int* total, int* idx,
+                          double* pos, int cap, int* ctl, cudaStream_t s);
+// out[m] += delta[m] at every target, then out[idx[i]] = moved[i] for the
+// moved ones; a nonzero subCtl[0] (the moved targets' evaluation's launch_partial32
+// code) is passed on to ctl.
+void launch_incr_merge(double* out, const double* delta, int M, const int* idx, const double* moved,
+                       const int* total, int cap, const int* subCtl, int* ctl, cudaStream_t s);
 
 // Launches a wait that nothing releases, bounded by `limit` polls: 1 if it
 // gave up and reported (the expected outcome), 0 if it did not, -1 on a CUDA

@@ -36,7 +36,8 @@ class VlmError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("sum_chunk", ctypes.c_int), ("near_factor", ctypes.c_double),
                 ("device", ctypes.c_int), ("use_graph", ctypes.c_int), ("solve_mode", ctypes.c_int),
-                ("nbody_slots", ctypes.c_int), ("lattice", ctypes.c_int)]
+                ("nbody_slots", ctypes.c_int), ("lattice", ctypes.c_int),
+                ("incremental", ctypes.c_int)]
 
 
 class SurrogateOptions(ctypes.Structure):
@@ -287,7 +288,7 @@ class Case:
     def __init__(self, config_text: str, geom_text: str, base_dir: str | os.PathLike = "",
                  precision: int = PREC_FP64, sum_chunk: Optional[int] = None, near_factor: Optional[float] = None,
                  solve_mode: Optional[int] = None, use_graph: bool = True, nbody_slots: int = 0,
-                 device: int = 0, lattice: Optional[bool] = None):
+                 device: int = 0, lattice: Optional[bool] = None, incremental: Optional[bool] = None):
         L = load()
         self._h = _vp()
         self.opt = options(precision, sum_chunk, near_factor, device=device, use_graph=use_graph,
@@ -295,6 +296,8 @@ class Case:
         self.opt.nbody_slots = nbody_slots
         if lattice is not None:
             self.opt.lattice = 1 if lattice else 0
+        if incremental is not None:
+            self.opt.incremental = 1 if incremental else 0
         _err(L.vlm_case_create(config_text.encode(), geom_text.encode(), str(base_dir).encode(),
                                ctypes.byref(self.opt), ctypes.byref(self._h)))
 
