@@ -64,9 +64,10 @@ typedef struct vlm_options {
   int incremental;     /* FP32 precisions, schemes with a predictor (fdSchemeSwitch 1, 3, 4, 5):
                           the predicted-wake velocities as the current-wake ones plus the
                           changed sources' difference, and the full sum at the moved wake nodes
-                          only, on steps whose (rowNear, rowFar) signature lasts more than one
-                          step (1 = on, the default; 0 = the full sum).  A lone case only (not
-                          a batch, a coupled rotor or the surrogate); no effect on FP64. */
+                          only, on steps whose (rowNear, rowFar) signature lasts at least 16
+                          steps and where that is less than half the full sum's work (1 = on,
+                          the default; 0 = the full sum).  Not for coupled rotors or with the
+                          surrogate; no effect on FP64. */
 } vlm_options;
 
 /* ---- library ------------------------------------------------------------ */

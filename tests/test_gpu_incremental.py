@@ -112,3 +112,22 @@ def test_incremental_not_used_where_it_does_not_apply():
     h.step(60, with_ct=False)
     p = plan_rows(h)
     assert p.shape[0] == 1 and p[0, 2] == 0
+
+
+def test_incremental_in_a_batch():
+    """Cases of a batch (one graph launch per step) take the same plans as
+    lone cases; their loads agree with the full evaluation's."""
+    cs = [hover(3), hover(1)]
+    rows = {}
+    for inc in (True, False):
+        b = lib.Batch([(c.config, c.geom, "") for c in cs], precision=lib.PREC_FP32_NEAR64, incremental=inc)
+        b.start()
+        rows[inc] = b.step(NT)
+        for i in range(len(cs)):
+            p = plan_rows(b.case(i))
+            assert p.shape[0] == (1 if inc else 0)
+            if inc:
+                assert p[0, 2] == 1
+    ri, rf = rows[True], rows[False]
+    assert np.array_equal(ri[:, :STEADY - 1], rf[:, :STEADY - 1])
+    assert np.max(np.abs(ri[..., 1] - rf[..., 1]) / np.abs(rf[..., 1])) < 2e-6

@@ -527,7 +527,18 @@ __global__ void k_grid_init(unsigned char* scratch, int T) {
   H->zsum = 0.0;
   H->zcount = 0u;
   H->T = T;
+  for (int a = 0; a < 3; ++a) {
+    H->lo[a] = INT_MAX;
+    H->hi[a] = INT_MIN;
+  }
 }
+
+// a float's order-preserving int code (finite values) and back
+__device__ __forceinline__ int ord_code(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float ord_value(int c) { return __int_as_float(c >= 0 ? c : c ^ 0x7FFFFFFF); }
 
 // Sum and count of the near-zone radii near_factor rvc_k = sqrt([32 + k]) /
 // |e_k| of the active filaments (the cell size is twice their mean).
@@ -569,6 +580,19 @@ __device__ __forceinline__ float grid_h(const GridHdr* H) {
 template <int PASS>
 __global__ void k_tgrid_insert(const double* __restrict__ P, int M, unsigned char* __restrict__ scratch) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (PASS == 0) {
+    // the targets' bounding box: one min and one max per axis and warp
+    GridHdr* Hw = reinterpret_cast<GridHdr*>(scratch);
+    for (int a = 0; a < 3; ++a) {
+      const int c = m < M ? ord_code((float)P[3 * (size_t)m + a]) : 0;
+      const int cmin = __reduce_min_sync(kFull, m < M ? c : INT_MAX);
+      const int cmax = __reduce_max_sync(kFull, m < M ? c : INT_MIN);
+      if ((threadIdx.x & 31) == 0 && cmin <= cmax) {
+        atomicMin(&Hw->lo[a], cmin);
+        atomicMax(&Hw->hi[a], cmax);
+      }
+    }
+  }
   if (m >= M) return;
   const GridHdr* H = reinterpret_cast<const GridHdr*>(scratch);
   const float h = grid_h(H);
@@ -789,6 +813,12 @@ __global__ void __launch_bounds__(256, 4) k_near_find(const float* __restrict__ 
     const int np = max(1, min(4096, (int)ceilf(len * invh)));
     const float amax = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az)) + len;
     const float grow = 1.42f * z * 1.0001f + 1e-6f + 4e-7f * amax;
+    // a near zone wholly outside the targets' bounding box holds none of
+    // them (the cells walked below lie within the segment's box +- grow)
+    if (fmaxf(ax, bx) + grow < ord_value(H->lo[0]) || fminf(ax, bx) - grow > ord_value(H->hi[0]) ||
+        fmaxf(ay, by) + grow < ord_value(H->lo[1]) || fminf(ay, by) - grow > ord_value(H->hi[1]) ||
+        fmaxf(az, bz) + grow < ord_value(H->lo[2]) || fminf(az, bz) - grow > ord_value(H->hi[2]))
+      return;
     const float reach = 1.4143f * z * 1.0001f + 0.8661f * h + 1e-6f + 4e-7f * amax;
     const float reach2 = reach * reach;
     for (int pc = 0; pc < np; ++pc) {

@@ -836,8 +836,7 @@ struct Case {
   int* incrCtl = nullptr;  // the moved targets' evaluation's error code and near-pair cursor
 
   bool incrAllowed() const {
-    return opt.incremental != 0 && opt.precision != VLM_PREC_FP64 && opt.nbody_slots <= 0 && !member && !surr.on &&
-           d.NW > 0;
+    return opt.incremental != 0 && opt.precision != VLM_PREC_FP64 && !member && !surr.on && d.NW > 0;
   }
   bool sameSig(int a, int b) const {
     return a >= 1 && b >= 1 && a <= W.nt && b <= W.nt && plans[a].rowNear == plans[b].rowNear &&
@@ -978,15 +977,20 @@ struct Case {
     const double* ew = s.edgeW ? ewP : nullptr;
     launch_moved_targets(tgtP, s.targets, M, incrBlk + incr_diff_blocks(e.nrec), incrCnt + 1, ip.tIdx, ip.tPos,
                          ip.mcap, s.err + 2, stream);
-    // every predicted record at the moved targets, on its own streams
-    VLM_CUDA(cudaEventRecord(incrFork, stream));
-    VLM_CUDA(cudaStreamWaitEvent(incrStream, incrFork, 0));
-    launch_pack32(recP, e.nrec, nf, ip.mRec32, incrStream, ew);
-    VLM_CUDA(cudaMemsetAsync(incrCtl + 1, 0, sizeof(int), incrStream));
+    // every predicted record at the moved targets, on its own streams (a
+    // batch's case on its own stream: the batch's cases already run side by side)
+    const bool side = opt.nbody_slots <= 0;
+    cudaStream_t ms = side ? incrStream : stream;
+    if (side) {
+      VLM_CUDA(cudaEventRecord(incrFork, stream));
+      VLM_CUDA(cudaStreamWaitEvent(incrStream, incrFork, 0));
+    }
+    launch_pack32(recP, e.nrec, nf, ip.mRec32, ms, ew);
+    VLM_CUDA(cudaMemsetAsync(incrCtl + 1, 0, sizeof(int), ms));
     launch_partial32(ip.mRec32, recP, ip.mC, ip.mq, e.nrec, ip.tPos, ip.mcap, ip.mPart, incrCtl, ip.mNear,
-                     ip.mNearBytes, ip.mNacc, incrStream, ew, 0, &incrOv);
-    launch_combine_unordered(ip.mPart, ip.mcap, ip.mG, ip.mng, ip.mmaxq, 0, ip.tOut, incrStream);
-    VLM_CUDA(cudaEventRecord(incrJoin, incrStream));
+                     ip.mNearBytes, ip.mNacc, ms, ew, 0, side ? &incrOv : nullptr);
+    launch_combine_unordered(ip.mPart, ip.mcap, ip.mG, ip.mng, ip.mmaxq, 0, ip.tOut, ms);
+    if (side) VLM_CUDA(cudaEventRecord(incrJoin, incrStream));
     // the changed records (new +, old -) at every target: the current-wake
     // targets, whose near-field grid the current-wake evaluation left in the
     // scratch (the moved targets' results are replaced below)
@@ -995,9 +999,10 @@ struct Case {
     launch_pack32(ip.dRec, ip.dcap, nf, s.rec32, stream, ip.dEw);
     VLM_CUDA(cudaMemsetAsync(s.err + 3, 0, sizeof(int), stream));
     launch_partial32(s.rec32, ip.dRec, ip.dC, ip.dq, ip.dcap, s.targets, M, ip.dPart, s.err + 2,
-                     nearOn ? s.nearScratch : nullptr, s.nearBytes, ip.dNacc, stream, ip.dEw, 0, &nearOv, true);
+                     nearOn ? s.nearScratch : nullptr, s.nearBytes, ip.dNacc, stream, ip.dEw, 0,
+                     side ? &nearOv : nullptr, true);
     launch_combine_unordered(ip.dPart, M, ip.dG, 1, ip.dmaxq, 0, ip.outD, stream);
-    VLM_CUDA(cudaStreamWaitEvent(stream, incrJoin, 0));
+    if (side) VLM_CUDA(cudaStreamWaitEvent(stream, incrJoin, 0));
     launch_incr_merge(s.outv, ip.outD, M, ip.tIdx, ip.tOut, incrCnt + 1, ip.mcap, incrCtl, s.err + 2, stream);
   }
 
@@ -2646,6 +2651,12 @@ struct vlm_batch {
       if (!c->c.steadyStep(k)) return false;
     return true;
   }
+  // a case's first step of a signature measures its incremental predicted-wake plan (not in a graph)
+  bool anyMeasureDue(int k) const {
+    for (vlm_case* c : cases)
+      if (c->c.incrMeasureDue(k)) return true;
+    return false;
+  }
 
   void capture(int k) {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -2698,7 +2709,7 @@ struct vlm_batch {
     VLM_CUDA(cudaEventRecord(ev0, origin));
     joinAll();  // the frames are in
     for (int k = it0 + 1; k <= it0 + nsteps; ++k) {
-      if (allSteady(k)) {
+      if (allSteady(k) && !anyMeasureDue(k)) {
         if (!sigMatches(k)) capture(k);
         // device step counters for replay (the graph advances them)
         for (vlm_case* c : cases) {

@@ -81,6 +81,7 @@ struct GridHdr {
   double zsum;         // sum of the near-zone radii (the cell size is a multiple of their mean)
   unsigned int zcount;
   int T;               // table slots
+  int lo[3], hi[3];    // bounding box of the binned FP32 target positions (order-preserving int codes)
 };
 VLM_BS_HD constexpr int grid_buckets(int M) {
   int T = 1024;

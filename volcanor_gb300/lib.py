@@ -582,7 +582,8 @@ class Batch:
     steady state); cases = [(config_text, geom_text, base_dir), ...]."""
 
     def __init__(self, cases, precision: int = PREC_FP64, sum_chunk: Optional[int] = None,
-                 nbody_slots: int = 0, use_graph: bool = True, lattice: Optional[bool] = None):
+                 nbody_slots: int = 0, use_graph: bool = True, lattice: Optional[bool] = None,
+                 incremental: Optional[bool] = None):
         n = len(cases)
         enc = lambda i: (ctypes.c_char_p * n)(*[str(c[i]).encode() for c in cases])
         self._cfg, self._geo, self._dir = enc(0), enc(1), enc(2)
@@ -590,6 +591,8 @@ class Batch:
         self.opt.nbody_slots = nbody_slots
         if lattice is not None:
             self.opt.lattice = 1 if lattice else 0
+        if incremental is not None:
+            self.opt.incremental = 1 if incremental else 0
         self.n = n
         self._h = _vp()
         _err(load().vlm_batch_create(n, self._cfg, self._geo, self._dir, ctypes.byref(self.opt), ctypes.byref(self._h)))
