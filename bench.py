@@ -378,6 +378,16 @@ def run_ours(args):
         "ct_last": float(rows[-1, 1]),
     }
     out["pairs_per_s"] = round(rp / (ms_l / 1e3), 1)
+    if prec != lib.PREC_FP64:
+        inc = case.get("incremental").reshape(-1, 9)
+        if inc.shape[0]:
+            r = inc[-1]
+            out["incremental_predicted_wake"] = {
+                "signature": [int(r[0]), int(r[1])], "used": bool(r[2]), "changed_records": int(r[3]),
+                "moved_nodes": int(r[4]), "record_capacity": int(r[5]), "node_capacity": int(r[6]),
+                "records": int(r[7]), "nodes": int(r[8]),
+                "note": "predicted-wake velocities = current-wake ones + the changed records' (new - old) sums; "
+                        "full sums at the moved nodes only"}
     if rank == 0 and not args.no_accuracy:
         # the plain FP64 GPU form over the same K steps from the same state:
         # its rate, and this precision's CT error against it on the timed

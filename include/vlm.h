@@ -255,6 +255,10 @@ int vlm_case_set_tile(vlm_case* c, int shape, int chunks);
  *                                   the collocation points: chosen tile shape, chunk
  *                                   count of the largest group, ms per launch of the
  *                                   choice, ms of the wave model's plan (11 per signature)
+ *   incremental                     per measured signature of the incremental predicted-wake
+ *                                   evaluation: rowNear, rowFar, used (0/1), changed records,
+ *                                   moved nodes, record capacity, node capacity, records,
+ *                                   nodes (9 per signature)
  *   hub                             (3) hub coordinates; yAxis (blade) (3) the blade's y axis;
  *   secCP (blade)                   (3, ns) section points -- all of the current iteration
  *                                   (of the open step between its phases)
