@@ -464,10 +464,10 @@ def run_ours(args):
                               "core 0.002)")
             out[key] = k3
     tmpdir.cleanup()
-    if rank == 0 and not args.no_batch:
+    if rank == 0 and args.batch and not args.no_batch:
         # the batched sweep of 256 uneven cases (its own steady state first)
         out["batch"] = measure_batch(args, args.batch_cases, args.batch_steps, 3)
-    if rank == 0 and not args.no_forward4:
+    if rank == 0 and args.forward4 and not args.no_forward4:
         # the 4-blade forward-flight rotor: FP32 forms against the plain FP64
         # form over the same steps, the surrogate, 8 batched copies
         out["forward4"] = measure_forward4(args, args.forward_step, K, W)
@@ -713,9 +713,14 @@ def main():
     ap.add_argument("--workload", default="hover2", choices=["hover2", "batch", "forward4"],
                     help="hover2: the headline 2-blade hover case; batch: 256 uneven cases in one graph launch")
     ap.add_argument("--batch-cases", type=int, default=256)
-    ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batch key of the default line")
-    ap.add_argument("--no-batch", action="store_true", help="leave the batched sweep out of the default line")
-    ap.add_argument("--no-forward4", action="store_true", help="leave the 4-blade forward-flight key out")
+    ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batch key")
+    # the batched sweep and the forward-flight rotor spend minutes of host
+    # launches in their transients: opt-in keys of the line (or their own
+    # --workload), so that the default run stays short
+    ap.add_argument("--batch", action="store_true", help="add the batched sweep as a key of the line")
+    ap.add_argument("--forward4", action="store_true", help="add the 4-blade forward-flight key")
+    ap.add_argument("--no-batch", action="store_true", help="(default) no batch key")
+    ap.add_argument("--no-forward4", action="store_true", help="(default) no forward-flight key")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
