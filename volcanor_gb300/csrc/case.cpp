@@ -792,8 +792,9 @@ struct Case {
   }
 
   // ---- incremental predicted-wake evaluation (incr.cu) ---------------------
-  // The predictor of the Adams-Moulton / predictor-corrector schemes moves a
-  // few node rows and the far wake; every other record and target of the
+  // The predictor of the Adams-Moulton / predictor-corrector schemes moves the
+  // first near-wake node row (the reference's 'P' loop `do i = 1, rowNear,
+  // nNwake`, src/classdef.f90:1549-1575) and the far wake; every other record and target of the
   // predicted-wake evaluation equals the current-wake evaluation's of the same
   // step.  On the FP32 precisions the predicted-wake velocity is then the
   // current-wake velocity (still in s.outv) plus the changed records' new minus

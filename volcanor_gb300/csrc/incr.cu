@@ -1,8 +1,9 @@
 // Incremental predicted-wake evaluation (FP32 precisions).
 //
-// The predictor of the reference's Adams-Moulton / predictor-corrector
-// schemes (src/main.f90:1012-1110; classdef.f90:1515-1575 with the predicted
-// loop visiting the first near-wake row only) moves a small part of the wake:
+// The predictor of the reference's predictor-corrector and Adams-Moulton
+// schemes (fdSchemeSwitch 1, 3, 4, 5: src/main.f90:844-1406) moves a small
+// part of the wake -- its 'P' convection loops `do i = 1, rowNear, nNwake`
+// and so visits the first near-wake row only (src/classdef.f90:1549-1575):
 // the predicted wake differs from the current one in a few node rows and the
 // far-wake filaments.  Every source record and every target point that did not
 // move gives the same FP32 pair in both evaluations, so the predicted-wake
