@@ -2931,6 +2931,7 @@ long or_geti(void* h, const char* name) {
 //   waN                             [i + NW*j][filament][fc1, fc2] (all rows)
 //   waN_gam, waN_rvc                [i + NW*j], [i + NW*j][filament]
 //   waF                             [i][fc1, fc2]; waF_gam, waF_rvc  [i]
+//   waNP, waFP                      the predicted wake of the last predictor, as waN, waF
 //   velN                            [i + NW*j][xyz] (j to ns), velF [i][xyz]
 long or_get(void* h, const char* name, int ib, double* out, long cap) {
   Sim* s = static_cast<Sim*>(h);
@@ -2992,6 +2993,9 @@ long or_get(void* h, const char* name, int ib, double* out, long cap) {
     else if (k == "waN_gam") { for (auto& w : b->waN) v.push_back(w.gam); }
     else if (k == "waN_rvc") { for (auto& w : b->waN) for (int f = 0; f < 4; ++f) v.push_back(w.vf[f].rVc); }
     else if (k == "waF") { for (auto& f : b->waF) { push3(f.vf.fc1); push3(f.vf.fc2); } }
+    // the predicted wake of the last predictor (the layouts of waN, waF)
+    else if (k == "waNP") { for (auto& w : b->waNP) for (int f = 0; f < 4; ++f) { push3(w.vf[f].fc1); push3(w.vf[f].fc2); } }
+    else if (k == "waFP") { for (auto& f : b->waFP) { push3(f.vf.fc1); push3(f.vf.fc2); } }
     else if (k == "waF_gam") { for (auto& f : b->waF) v.push_back(f.gam); }
     else if (k == "waF_rvc") { for (auto& f : b->waF) v.push_back(f.vf.rVc); }
     else if (k == "velN") { for (auto& a : b->velN) push3(a); }
