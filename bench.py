@@ -551,9 +551,9 @@ def measure_batch(args, n: int, K: int, W: int, budget_s: float = None):
     done = 0
     while done < steady + W:
         if budget_s is not None and time.perf_counter() - t0 > budget_s:
-            # the transient is launch-bound on the host (each case's steps
-            # launched one by one until every case is steady): a slow host
-            # ends the measurement instead of the whole run
+            # the transient (each case's steps launched one by one until
+            # every case is steady) takes minutes: a slow box ends the
+            # measurement instead of the whole run
             b.close()
             return {"metric": "batched free-wake case-timesteps/s", "value": None, "unit": "case-timesteps/s",
                     "skipped": f"transient not finished within {budget_s:.0f} s of wall time ({done} of "
@@ -722,7 +722,7 @@ def main():
                     help="hover2: the headline 2-blade hover case; batch: 256 uneven cases in one graph launch")
     ap.add_argument("--batch-cases", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batch key")
-    # the batched sweep's transient is launch-bound on the host (~3 min):
+    # the batched sweep's transient takes ~3 min (581 steps of 256 cases):
     # a key of the default line with a wall-clock budget; the forward-flight
     # rotor is an opt-in key (or its own --workload)
     ap.add_argument("--batch-budget-s", type=float, default=240.0,
