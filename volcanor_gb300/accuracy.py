@@ -9,7 +9,7 @@ difference grows until the two wakes are different samples of the same
 flow), so the per-step error after many revolutions measures that growth,
 and the revolution-averaged CT measures the answer.
 
-    python -m volcanor_gb300.accuracy --case hover2 [--nt 1440] [--out file.npz]
+    python -m volcanor_gb300.accuracy --case hover2 [--nt 1440] [--out file.npz] [--no-incremental]
 """
 import argparse
 import json
@@ -30,11 +30,11 @@ DEFAULT_NT = {"hover2": 1440, "forward4": 2880, "wing": 200}
 STEPS_PER_REV = 72
 
 
-def run(case_name: str, nt: int, precision: int, sum_chunk=None, chunk_steps: int = 100):
+def run(case_name: str, nt: int, precision: int, sum_chunk=None, chunk_steps: int = 100, incremental=None):
     c = CASES[case_name](nt)
     with tempfile.TemporaryDirectory() as d:
         c.write(d)
-        g = lib.Case.from_case_dir(d, precision=precision, sum_chunk=sum_chunk)
+        g = lib.Case.from_case_dir(d, precision=precision, sum_chunk=sum_chunk, incremental=incremental)
     g.start()
     rows = []
     t0 = time.perf_counter()
@@ -69,6 +69,8 @@ def main():
     ap.add_argument("--avg-revs", type=int, default=2)
     ap.add_argument("--out", default=None)
     ap.add_argument("--no-floor", action="store_true", help="skip the second FP64 run")
+    ap.add_argument("--no-incremental", action="store_true",
+                    help="FP32 modes with the full predicted-wake sum (vlm_options.incremental = 0)")
     args = ap.parse_args()
     nt = args.nt or DEFAULT_NT[args.case]
     avg = args.avg_revs * STEPS_PER_REV
@@ -80,8 +82,9 @@ def main():
         x, w = run(args.case, nt, lib.PREC_FP64, sum_chunk=0)
         hist["fp64_chunk0"] = x
         res["fp64_chunk0"] = compare(ref, x, avg) | {"wall_s": round(w, 2)}
+    res["incremental"] = not args.no_incremental
     for name, p in (("fp32near", lib.PREC_FP32_NEAR64), ("fp32", lib.PREC_FP32)):
-        x, w = run(args.case, nt, p)
+        x, w = run(args.case, nt, p, incremental=False if args.no_incremental else None)
         hist[name] = x
         res[name] = compare(ref, x, avg) | {"wall_s": round(w, 2)}
     if args.out:

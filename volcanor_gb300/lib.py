@@ -334,6 +334,12 @@ class Case:
         evaluation (wake nodes, collocation points) shape, chunks, ms, model ms."""
         return self.get("autotune").reshape(-1, 11)
 
+    def incremental_plans(self) -> np.ndarray:
+        """Incremental predicted-wake evaluation, one row per measured wake
+        signature: rowNear, rowFar, used (0/1), changed records, moved nodes,
+        record capacity, node capacity, records, nodes."""
+        return self.get("incremental").reshape(-1, 9)
+
     # the step as separate calls (include/vlm.h): solve -> [loads] -> wake
     def aic_factor(self):
         _err(load().vlm_case_aic_factor(self._h))
