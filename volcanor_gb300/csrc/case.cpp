@@ -794,19 +794,21 @@ struct Case {
   // ---- incremental predicted-wake evaluation (incr.cu) ---------------------
   // The predictor of the Adams-Moulton / predictor-corrector schemes moves the
   // first near-wake node row (the reference's 'P' loop `do i = 1, rowNear,
-  // nNwake`, src/classdef.f90:1549-1575) and the far wake; every other record and target of the
-  // predicted-wake evaluation equals the current-wake evaluation's of the same
-  // step.  On the FP32 precisions the predicted-wake velocity is then the
-  // current-wake velocity (still in s.outv) plus the changed records' new minus
-  // old contributions at every target, and the full sum at the moved targets
-  // alone.  The changed records and moved targets are found on the device by
-  // a bit-by-bit comparison every step; their numbers, fixed by the wake's
-  // structure for a (rowNear, rowFar) signature, are measured once at the
-  // first step of a signature that lasts at least kIncrMinRun steps (a host
-  // synchronisation), and size the fixed-capacity buffers a captured step
-  // graph needs.  A signature whose incremental work is not below half the
-  // full evaluation's keeps the full evaluation.  The choice depends only on
-  // the case and the signature, so runs resumed anywhere give the same bits.
+  // nNwake`, src/classdef.f90:1549-1575) and the far wake; every other
+  // record and target of the predicted-wake evaluation equals the
+  // current-wake evaluation's of the same step.  On the FP32 precisions the
+  // predicted-wake velocity is then the current-wake velocity (still in
+  // s.outv) plus the changed records' new minus old contributions at every
+  // target, and the full sum at the moved targets alone.  The changed records
+  // and moved targets are found on the device by a bit-by-bit comparison
+  // every step; their numbers, fixed by the wake's structure for a (rowNear,
+  // rowFar) signature, are measured once -- at the case's first
+  // predicted-wake evaluation of a signature that lasts at least kIncrMinRun
+  // steps, never inside a captured graph (a host synchronisation) -- and size
+  // the fixed-capacity buffers a captured step graph needs.  A signature whose
+  // incremental work is not below half the full evaluation's keeps the full
+  // evaluation.  The choice depends only on the case and the signature, so
+  // runs resumed anywhere give the same bits.
   struct IncrPlan {
     int rN = 0, rF = 0;
     bool on = false;
